@@ -1,0 +1,329 @@
+#!/usr/bin/env python
+"""Benchmark: SSA reaction events/s of the dimerization ensemble on one GB300.
+
+A step is one pass of the direct method over the whole ensemble: 1e5
+independent dimerization trajectories (gene, mRNA, protein, dimer; x0 =
+(1, 0, 0, 0); rates 25, 1000, 0.001, 0.1, 1; tmax = 1, 101 regular samples),
+about 1.7e9 reaction events.  ``value`` times the kernel on HBM-resident
+inputs (CUDA events on the launching stream, L2 flushed between steps);
+``e2e`` times the C-ABI host call ``rb_ensemble_run`` from page-locked host
+buffers, copies included.  ``--impl reference`` times the CPU restatement of
+the reference on all host cores instead.  Under torchrun each rank simulates
+its own 1e5 trajectories (weak scaling; seeds keyed by global trajectory id).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DIMER = dict(
+    name="dimer",
+    desc=("dimerization ensemble: gene,mRNA,protein,dimer x0=(1,0,0,0); G->G+M 25, M->M+P 1000, "
+          "2P->D 0.001, M->0 0.1, P->0 1; tmax=1.0, nb_steps=100"),
+    S=4,
+    reactions=[(25.0, [1, 0, 0, 0], [0, 1, 0, 0]), (1000.0, [0, 1, 0, 0], [0, 0, 1, 0]),
+               (0.001, [0, 0, 2, 0], [0, 0, -2, 1]), (0.1, [0, 1, 0, 0], [0, -1, 0, 0]),
+               (1.0, [0, 0, 1, 0], [0, 0, -1, 0])],
+    x0=[1, 0, 0, 0], tmax=1.0, nb_steps=100, n_traj=100_000, cpu_sample=20_000,
+)
+SIR = dict(
+    name="sir",
+    desc="SIR: S,I,R x0=(999,1,0); S+I->2I 1e-4, I->R 0.01; tmax=250, nb_steps=250",
+    S=3,
+    reactions=[(1e-4, [1, 1, 0], [-1, 1, 0]), (0.01, [0, 1, 0], [0, -1, 1])],
+    x0=[999, 1, 0], tmax=250.0, nb_steps=250, n_traj=10_000, cpu_sample=10_000,
+)
+WORKLOADS = {"dimer": DIMER, "sir": SIR}
+
+
+def f_event(w) -> int:
+    """Algorithmic binary64 operations per event of the direct method with full
+    recompute: sum of reactant orders (LMA multiplies) + R (running sum) + R
+    (choice compares) + 4 (U scaling, total*U, Exp1/total, clock add)."""
+    R = len(w["reactions"])
+    return sum(sum(e) for _, e, _ in w["reactions"]) + 2 * R + 4
+
+
+def seeds_for(rank: int, step: int, n: int) -> np.ndarray:
+    rng = np.random.default_rng([20260101, rank, step])
+    return rng.integers(np.iinfo(np.uint64).max, size=n, dtype=np.uint64)
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock, power and throttle reasons."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines: list[str] = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_reference(w, n_traj: int, steps: int, warmup: int, threads: int) -> dict:
+    from oracle import oracle as O
+
+    net = O.OracleNet(w["S"])
+    for k, e, d in w["reactions"]:
+        net.add_lma(k, e, d)
+    tot_ev, tot_s = 0, 0.0
+    for step in range(warmup + steps):
+        seeds = seeds_for(0, 1000 + step, n_traj)
+        t0 = time.perf_counter()
+        _, _, ev, _ = net.run_ensemble(w["x0"], seeds, w["tmax"], w["nb_steps"], n_threads=threads)
+        dt = time.perf_counter() - t0
+        if step >= warmup:
+            tot_ev += ev
+            tot_s += dt
+    return {"value": tot_ev / tot_s, "events": tot_ev, "seconds": tot_s}
+
+
+def run_reference_arm(args, w):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = args.cpu_sample or w["cpu_sample"]
+    r = cpu_reference(w, n, args.steps, args.warmup, threads)
+    sample = (f"{n} of the {w['n_traj']} trajectories per step ({w['name']}), oracle port of the "
+              f"reference's CPU path, {threads} threads")
+    line = {
+        "impl": "reference", "metric": "SSA reaction events/sec", "value": r["value"], "unit": "events/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * r["seconds"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+int64", "data": "synthetic",
+        "config": {"workload": w["desc"], "n_traj": w["n_traj"], "sample_traj_per_step": n},
+        "cpu_baseline": {"value": r["value"], "unit": "events/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": r["value"], "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU side
+def read_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / f"{kernel}_{workload}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(args, w):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    import rebop_gb300 as rb
+    from rebop_gb300._lib import lib as rblib
+
+    net = rb.Network(w["S"])
+    for k, e, d in w["reactions"]:
+        net.add_reaction(rb.Rate.lma(k, e), d)
+    n = args.n_traj or w["n_traj"]
+    NT, S = w["nb_steps"] + 1, w["S"]
+    stream = torch.cuda.current_stream()
+    sid = stream.cuda_stream
+    d_x0 = torch.tensor(w["x0"], dtype=torch.int64, device="cuda")
+    d_seeds = [torch.from_numpy(seeds_for(rank, s, n).view(np.int64)).cuda() for s in range(args.warmup + args.steps)]
+    d_out = torch.empty((NT, S, n), dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def launch(seeds):
+        net.run_ensemble_device(n, d_x0.data_ptr(), False, seeds.data_ptr(), w["tmax"], w["nb_steps"],
+                                d_out.data_ptr(), stream=sid)
+
+    for s in range(args.warmup):
+        launch(d_seeds[s])
+    torch.cuda.synchronize()
+    peak_ops = rblib.rbg_internal_fp64_fma_rate(sid)  # DFMA instructions / s, measured live
+
+    vis = [v for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    clocks = ClockSampler(int(vis[local]) if local < len(vis) and vis[local].strip().isdigit() else local)
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    events_per_step = []
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    for s in range(args.steps):
+        flush.zero_()  # L2 flush between timed steps (256 MB > 129 MB L2)
+        ev0[s].record(stream)
+        launch(d_seeds[args.warmup + s])
+        ev1[s].record(stream)
+        events_per_step.append(net.last_events())
+    torch.cuda.synchronize()
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    dev_s = sum(step_ms) / 1e3
+    ev_total = sum(events_per_step)
+    if dist is not None:
+        t = torch.tensor([dev_s, float(ev_total)], dtype=torch.float64, device="cuda")
+        tmax_t = t.clone()
+        dist.all_reduce(tmax_t[:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        dev_s_all, ev_all = float(tmax_t[0]), float(t[1])
+    else:
+        dev_s_all, ev_all = dev_s, float(ev_total)
+    value = ev_all / dev_s_all
+
+    # e2e: the C-ABI host call with page-locked buffers, copies in the timed region.
+    pin_out = torch.empty((NT, S, n), dtype=torch.int64, pin_memory=True).numpy()
+    pin_seeds = [torch.from_numpy(seeds_for(rank, 500 + s, n).view(np.int64)).pin_memory().numpy().view(np.uint64)
+                 for s in range(args.steps + 1)]
+    x0_host = np.asarray(w["x0"], dtype=np.int64)
+    net.run_ensemble(x0_host, pin_seeds[0], w["tmax"], w["nb_steps"], out=pin_out, want_events=False)
+    barrier()
+    e2e_ev, e2e_s, h2d, d2h = 0, 0.0, 0, 0
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        res = net.run_ensemble(x0_host, pin_seeds[1 + s], w["tmax"], w["nb_steps"], out=pin_out,
+                               want_events=False)
+        e2e_s += time.perf_counter() - t0
+        e2e_ev += res.total_events
+        h2d, d2h = res.stats["h2d_bytes"], res.stats["d2h_bytes"]
+    if dist is not None:
+        t = torch.tensor([e2e_s, float(e2e_ev)], dtype=torch.float64, device="cuda")
+        m = t.clone()
+        dist.all_reduce(m[:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        e2e_s, e2e_ev = float(m[0]), float(t[1])
+    e2e_value = e2e_ev / e2e_s
+
+    # roofline of the dominant kernel (binary64 pipe)
+    avg_launch_s = dev_s / args.steps
+    fe = f_event(w)
+    achieved = (ev_total / args.steps) * fe / avg_launch_s / 1e9
+    peak = peak_ops / 1e9
+    traffic = read_traffic("ssa_thread_kernel", w["name"])
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        nb = args.cpu_sample or w["cpu_sample"]
+        r = cpu_reference(w, nb, 1, 0, threads)
+        cpu = {"value": r["value"], "unit": "events/s", "cores": threads, "kind": "port",
+               "sample": f"{nb} trajectories of the same workload, oracle port of the reference CPU path, "
+                         f"{threads} threads"}
+
+    if rank == 0:
+        line = {
+            "metric": "SSA reaction events/sec", "value": value, "unit": "events/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s_all / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+int64",
+            "data": "synthetic",
+            "config": {"workload": w["desc"], "n_traj_per_gpu": n, "events_per_step": ev_total / args.steps,
+                       "rng": "reference stream: xoshiro256++/SplitMix64 seeds, ziggurat Exp1",
+                       "mapping": "thread per trajectory", "l2": "flushed between steps (256 MB write)",
+                       "wall_s": t_wall},
+            "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "Gop/s (binary64)",
+                         "frac": achieved / peak if peak else None, "traffic": traffic,
+                         "ops_per_event": fe,
+                         "peak_source": "DFMA throughput measured live in this run (not in MEASURED_PEAKS.json)"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="dimer")
+    ap.add_argument("--n-traj", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference_arm(args, w)
+    else:
+        run_ours(args, w)
+
+
+if __name__ == "__main__":
+    main()

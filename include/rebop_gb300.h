@@ -1,0 +1,190 @@
+/*
+ * rebop_gb300.h -- C ABI of the GB300 ensemble engine for rebop's run-time
+ * Gillespie direct method.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status (RB_OK = 0) and never aborts: where the reference panics or
+ * raises, this library returns RB_ERR_INVALID and keeps a message that
+ * rb_last_error() copies out (per calling thread).  Host buffers stay owned
+ * by the caller; device buffers, streams and the per-device tables belong to
+ * the library unless a *_device entry point is used, in which case the
+ * caller owns the device buffers and the stream.
+ *
+ * Arithmetic contract: species counts are int64 (the reference's isize),
+ * propensities, their running sums and the clock are IEEE binary64 evaluated
+ * in the reference's order, and the random stream is the reference's
+ * generator stack (xoshiro256++ seeded by SplitMix64, a 256-layer ziggurat for
+ * Exp1, 53-bit uniforms), one stream per trajectory seed.  A trajectory run
+ * with seed s therefore follows the reference's
+ * `Gillespie::new_with_seed(x0, sparse, s)` event for event.
+ *
+ * Citations are to files of the rebop v0.9.7 source tree.
+ */
+#ifndef REBOP_GB300_H
+#define REBOP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define RB_OK 0
+#define RB_ERR_INVALID 1     /* bad argument: the reference's assert!/ValueError */
+#define RB_ERR_CUDA 2        /* a CUDA runtime call failed (message has details) */
+#define RB_ERR_NOMEM 3       /* host or device allocation failed */
+#define RB_ERR_PARSE 4       /* define_system! text not understood */
+#define RB_ERR_UNSUPPORTED 5 /* network shape outside every kernel's range */
+#define RB_ERR_TIMEOUT 6     /* a kernel hit its event budget (see rb_run_stats) */
+
+/* Library version string ("<major>.<minor>.<patch>"). */
+const char *rb_version(void);
+
+/* Copy the calling thread's last error message into buf (always
+ * NUL-terminated when len > 0).  Returns the message length. */
+size_t rb_last_error(char *buf, size_t len);
+
+/* Per-call statistics, filled when a non-NULL pointer is passed. */
+typedef struct {
+    uint64_t events;       /* accepted reaction events, all trajectories    */
+    double kernel_ms;      /* device time of the simulation kernel(s)       */
+    double total_ms;       /* wall time of the whole call                   */
+    uint64_t h2d_bytes;    /* host->device bytes copied by the call         */
+    uint64_t d2h_bytes;    /* device->host bytes copied by the call         */
+    int32_t kernel_launches;
+    int32_t mapping;       /* 0 = thread per trajectory, 1 = warp per trajectory */
+} rb_run_stats;
+
+/* ------------------------------------------------- reaction network -----
+ * A network is the packed reaction descriptor every kernel reads.  It is
+ * built the way the reference builds a Gillespie's reaction list
+ * (src/gillespie.rs:225-244): each reaction is a mass-action rate and a
+ * vector of species differences. */
+typedef struct rb_network rb_network;
+
+/* Empty network over n_species species.  Replaces the species-count part of
+ * Gillespie::new (src/gillespie.rs:168-176). */
+int rb_network_create(int32_t n_species, rb_network **out);
+void rb_network_destroy(rb_network *net);
+int32_t rb_network_nb_species(const rb_network *net);   /* gillespie.rs:199-201 */
+int32_t rb_network_nb_reactions(const rb_network *net); /* gillespie.rs:209-211 */
+
+/* add_reaction(Rate::lma(rate, exponents), differences):
+ * src/gillespie.rs:24-26 and :225-244.  n_exponents and n_differences must
+ * both equal the species count (the reference's assert_eq!). */
+int rb_network_add_reaction_lma(rb_network *net, double rate, const uint32_t *exponents,
+                                int32_t n_exponents, const int64_t *differences,
+                                int32_t n_differences);
+
+/* add_reaction(Rate::lma_sparse(rate, pairs), differences):
+ * src/gillespie.rs:29-31 and :225-244.  The (species, exponent) pairs are
+ * multiplied in the order given, as Rate::rate's sparse arm does
+ * (gillespie.rs:79-86); an index out of range is RB_ERR_INVALID (the
+ * reference's issue-85 assert, gillespie.rs:229-233 and :496-502). */
+int rb_network_add_reaction_lma_sparse(rb_network *net, double rate, const uint32_t *species,
+                                       const uint32_t *exponents, int32_t n_pairs,
+                                       const int64_t *differences, int32_t n_differences);
+
+/* Lower a define_system! body (src/gillespie_macro.rs:50-58):
+ *     p1 p2 ...;  Name { A, B, ... }  rname: [k] A + ... => [k] B + ... @ rate ...
+ * `rate` is a parameter name or a numeric literal.  Parameters start as NaN,
+ * as the macro's `new()` leaves them (gillespie_macro.rs:71-78); set them with
+ * rb_network_set_param.  The network keeps the macro's arithmetic: integer
+ * falling factorials per reactant term in written order, and the
+ * first-match choice chain (gillespie_macro.rs:106, :133-171). */
+int rb_network_from_dsl(const char *text, rb_network **out);
+int rb_network_set_param(rb_network *net, const char *name, double value);
+int32_t rb_network_nb_params(const rb_network *net);
+int rb_network_param_name(const rb_network *net, int32_t idx, char *buf, size_t len);
+int rb_network_species_name(const rb_network *net, int32_t idx, char *buf, size_t len);
+int rb_network_name(const rb_network *net, char *buf, size_t len);
+/* Rate constant of reaction r (after parameter substitution). */
+int rb_network_reaction_rate(const rb_network *net, int32_t r, double *rate);
+
+/* ---------------------------------------------------- ensemble runs -----
+ * The batched entry point: n_traj independent trajectories of one network,
+ * each the reference's Python-API run (src/pyo3_gillespie.rs:168-208) with its
+ * own seed: t starts at 0, and for i = 0..nb_steps the trajectory is
+ * advanced to tmax*i/nb_steps (gillespie.rs:315-344) and the saved species
+ * are recorded.
+ *
+ *   x0        [S] shared initial counts, or [n_traj][S] when x0_per_traj
+ *   rates     NULL: the network's rate constants; else [R] or
+ *             [n_traj][R] (rates_per_traj) per-trajectory rate constants
+ *   seeds     [n_traj] one u64 seed per trajectory
+ *   save_idx  [n_save] species to record (NULL with n_save < 0: all)
+ *   out       [nb_steps+1][n_save][n_traj] recorded counts
+ *   times     [nb_steps+1] sample times, may be NULL
+ *   events    [n_traj] accepted events per trajectory, may be NULL
+ *   final_species [n_traj][S], may be NULL
+ *
+ * rb_ensemble_run takes host buffers and does the copies itself;
+ * rb_ensemble_run_device takes device buffers and a cudaStream_t (NULL:
+ * the legacy default stream) and returns once the work is enqueued. */
+int rb_ensemble_run(const rb_network *net, int64_t n_traj, const int64_t *x0, int32_t x0_per_traj,
+                    const double *rates, int32_t rates_per_traj, const uint64_t *seeds, double tmax,
+                    int64_t nb_steps, const int32_t *save_idx, int32_t n_save, int64_t *out,
+                    double *times, uint64_t *events, int64_t *final_species, rb_run_stats *stats);
+
+int rb_ensemble_run_device(const rb_network *net, int64_t n_traj, const int64_t *d_x0,
+                           int32_t x0_per_traj, const double *d_rates, int32_t rates_per_traj,
+                           const uint64_t *d_seeds, double tmax, int64_t nb_steps,
+                           const int32_t *save_idx, int32_t n_save, int64_t *d_out,
+                           uint64_t *d_events, int64_t *d_final_species, void *stream);
+
+/* Sum of accepted events of the last rb_ensemble_run_device on this network
+ * (synchronises with that run's stream). */
+int rb_ensemble_last_events(const rb_network *net, uint64_t *events);
+
+/* Every-event run of one trajectory, src/pyo3_gillespie.rs:209-223: records
+ * (t, saved species) at t = 0 and after each reaction while t < tmax; the
+ * last record is the first event at or after tmax, or t = +inf when the
+ * total propensity vanishes (gillespie.rs:275-297).  Writes at most `cap`
+ * records and returns their full number in *n_records. */
+int rb_run_all_events(const rb_network *net, const int64_t *x0, uint64_t seed, double tmax,
+                      const int32_t *save_idx, int32_t n_save, double *times, int64_t *out,
+                      int64_t cap, int64_t *n_records);
+
+/* One trajectory whose state the caller keeps: species[S], *t and the
+ * 4-word generator state are read and updated in place by one GPU
+ * advance_until(tmax).  The define_system! struct's advance_until
+ * (src/gillespie_macro.rs:98-126) maps here, as does any checkpoint/resume. */
+int rb_trajectory_advance_until(const rb_network *net, int64_t *species, double *t, uint64_t *rng_state,
+                                double tmax);
+/* The generator state SmallRng::seed_from_u64(seed) starts from
+ * (src/gillespie.rs:184; gillespie_macro.rs:81-84). */
+void rb_rng_state_from_seed(uint64_t seed, uint64_t *state);
+
+/* ------------------------------------------ stateful single trajectory ---
+ * The Rust API's `Gillespie` object (src/gillespie.rs:157-344) with the same
+ * methods; every advance runs on the GPU. */
+typedef struct rb_gillespie rb_gillespie;
+
+/* Gillespie::new (gillespie.rs:168-176): seed drawn from OS entropy. */
+int rb_gillespie_new(const int64_t *species, int32_t n_species, int32_t sparse, rb_gillespie **out);
+/* Gillespie::new_with_seed (gillespie.rs:179-187). */
+int rb_gillespie_new_with_seed(const int64_t *species, int32_t n_species, int32_t sparse,
+                               uint64_t seed, rb_gillespie **out);
+void rb_gillespie_free(rb_gillespie *g);
+int rb_gillespie_seed(rb_gillespie *g, uint64_t seed);         /* gillespie.rs:189-191 */
+int32_t rb_gillespie_nb_species(const rb_gillespie *g);        /* gillespie.rs:199-201 */
+int32_t rb_gillespie_nb_reactions(const rb_gillespie *g);      /* gillespie.rs:209-211 */
+int rb_gillespie_add_reaction_lma(rb_gillespie *g, double rate, const uint32_t *exponents,
+                                  int32_t n_exponents, const int64_t *differences,
+                                  int32_t n_differences);      /* gillespie.rs:225-244 */
+int rb_gillespie_add_reaction_lma_sparse(rb_gillespie *g, double rate, const uint32_t *species,
+                                         const uint32_t *exponents, int32_t n_pairs,
+                                         const int64_t *differences, int32_t n_differences);
+double rb_gillespie_get_time(const rb_gillespie *g);           /* gillespie.rs:246-248 */
+void rb_gillespie_set_time(rb_gillespie *g, double t);         /* gillespie.rs:250-252 */
+int rb_gillespie_get_species(const rb_gillespie *g, int32_t s, int64_t *value); /* :260-262 */
+int rb_gillespie_set_species(rb_gillespie *g, const int64_t *species, int32_t n); /* :264-267 */
+int rb_gillespie_advance_until(rb_gillespie *g, double tmax);  /* gillespie.rs:315-344 */
+int rb_gillespie_advance_one_reaction(rb_gillespie *g);        /* gillespie.rs:269-272 */
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* REBOP_GB300_H */

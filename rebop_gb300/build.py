@@ -1,0 +1,89 @@
+"""Build the engine's shared library in-tree (no CMake, no torch extension).
+
+CUDA sources are compiled by nvcc for sm_103a only; host C++ by g++.  Objects
+compile in parallel and link into ``rebop_gb300/_build/librebop_gb300.so``
+with the CUDA runtime linked statically, so the library's only run-time
+dependency is the NVIDIA driver.  ``python -m rebop_gb300.build`` runs it.
+"""
+
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = BUILD / "librebop_gb300.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CUDA_SOURCES = ["ssa_thread.cu", "fp64_peak.cu"]
+CXX_SOURCES = ["network.cpp", "engine.cpp", "capi.cpp"]
+
+
+def cuda_home() -> Path:
+    env = os.environ.get("CUDA_HOME") or os.environ.get("CUDA_PATH")
+    if env:
+        return Path(env)
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return Path(nvcc).resolve().parent.parent
+    return Path("/usr/local/cuda")
+
+
+def _sources() -> list[Path]:
+    return ([CSRC / s for s in CUDA_SOURCES + CXX_SOURCES] + sorted(CSRC.glob("*.hpp"))
+            + sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "rebop_gb300.h"])
+
+
+def up_to_date() -> bool:
+    if not LIB.exists():
+        return False
+    t = LIB.stat().st_mtime
+    return all(p.stat().st_mtime <= t for p in _sources() if p.exists())
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    if not force and up_to_date():
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    cuda = cuda_home()
+    nvcc = str(cuda / "bin" / "nvcc")
+    inc = ["-I", str(ROOT / "include"), "-I", str(CSRC)]
+    jobs = []
+    for s in CUDA_SOURCES:
+        obj = BUILD / (s + ".o")
+        jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC",
+                     "-Xcompiler", "-ffp-contract=off", *inc, "-c", str(CSRC / s), "-o", str(obj)])
+    for s in CXX_SOURCES:
+        obj = BUILD / (s + ".o")
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
+                     "-Wall", "-Wno-unused-function", *inc, "-I", str(cuda / "include"), "-c", str(CSRC / s),
+                     "-o", str(obj)])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        return r.stderr
+
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        for err in ex.map(run, jobs):
+            if verbose and err:
+                print(err)
+    objs = [str(BUILD / (s + ".o")) for s in CUDA_SOURCES + CXX_SOURCES]
+    tmp = BUILD / f"librebop_gb300.{os.getpid()}.so"
+    run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *objs, "-lpthread", "-ldl", "-lrt"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

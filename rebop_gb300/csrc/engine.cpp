@@ -1,0 +1,210 @@
+// Host engine implementation.
+#include "engine.hpp"
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+
+namespace rbg {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string &msg) { g_last_error = msg; }
+const std::string &last_error() { return g_last_error; }
+
+static bool cuda_ok(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return true;
+    set_error(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+    return false;
+}
+
+// ZIGNOR construction (Doornik 2005) of the 256-layer exponential ziggurat:
+// x[0] = v / f(r), x[1] = r, x[i] = f^-1(v / x[i-1] + f(x[i-1])), x[256] = 0,
+// f(x) = exp(-x); r and v are the tail start and the common layer area.
+void zig_tables_host(double *x, double *f) {
+    const double r = 7.69711747013104972;
+    const double v = 0.0039496598225815571993;
+    x[0] = v / std::exp(-r);
+    x[1] = r;
+    for (int i = 2; i < kZigLayers; i++) x[i] = -std::log(v / x[i - 1] + std::exp(-x[i - 1]));
+    x[kZigLayers] = 0.0;
+    for (int i = 0; i < kZigTable; i++) f[i] = std::exp(-x[i]);
+}
+
+static std::mutex g_ctx_mu;
+static std::map<int, DeviceCtx *> g_ctx;
+
+DeviceCtx *device_ctx() {
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return nullptr;
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    auto it = g_ctx.find(dev);
+    if (it != g_ctx.end()) return it->second;
+    auto *c = new DeviceCtx();
+    c->device = dev;
+    cudaDeviceProp prop;
+    if (!cuda_ok(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties")) {
+        delete c;
+        return nullptr;
+    }
+    if (prop.major < 10) {
+        set_error(std::string("device ") + prop.name + " is not a Blackwell-class GPU (sm_103a build)");
+        delete c;
+        return nullptr;
+    }
+    c->sm_count = prop.multiProcessorCount;
+    c->smem_optin = prop.sharedMemPerBlockOptin;
+    std::vector<double> tab(2 * kZigTable);
+    zig_tables_host(tab.data(), tab.data() + kZigTable);
+    if (!cuda_ok(cudaMalloc(&c->zig, sizeof(double) * 2 * kZigTable), "cudaMalloc(zig)") ||
+        !cuda_ok(cudaMemcpy(c->zig, tab.data(), sizeof(double) * 2 * kZigTable, cudaMemcpyHostToDevice),
+                 "cudaMemcpy(zig)")) {
+        delete c;
+        return nullptr;
+    }
+    g_ctx[dev] = c;
+    return c;
+}
+
+DeviceNet::~DeviceNet() {
+    // Teardown after the CUDA runtime has shut down must not fault; errors
+    // are ignored here.
+    if (desc) cudaFree(desc);
+    if (scratch) cudaFree(scratch);
+    if (io) cudaFree(io);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_stop) cudaEventDestroy(ev_stop);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+bool ensure_device(const Network &net) {
+    DeviceCtx *ctx = device_ctx();
+    if (!ctx) return false;
+    if (net.dev && net.dev->device != ctx->device) net.dev.reset();
+    if (!net.dev) {
+        auto dn = std::make_unique<DeviceNet>();
+        dn->device = ctx->device;
+        if (!cuda_ok(cudaStreamCreateWithFlags(&dn->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+            !cuda_ok(cudaEventCreate(&dn->ev_start), "cudaEventCreate") ||
+            !cuda_ok(cudaEventCreate(&dn->ev_stop), "cudaEventCreate") ||
+            !cuda_ok(cudaMalloc(&dn->scratch, 2 * sizeof(unsigned long long)), "cudaMalloc(scratch)"))
+            return false;
+        net.dev = std::move(dn);
+    }
+    DeviceNet &dn = *net.dev;
+    if (dn.version == net.version) return true;
+    Packed p = net.pack();
+    const size_t R = p.R, P = p.P, Q = p.Q;
+    size_t off_rate = 0;
+    size_t off_jd = align_up(off_rate + sizeof(double) * std::max<size_t>(R, 1), 16);
+    size_t off_fsp = align_up(off_jd + sizeof(int64_t) * std::max<size_t>(R * Q, 1), 16);
+    size_t off_ford = align_up(off_fsp + sizeof(int32_t) * std::max<size_t>(R * P, 1), 16);
+    size_t off_jsp = align_up(off_ford + sizeof(int32_t) * std::max<size_t>(R * P, 1), 16);
+    size_t total = align_up(off_jsp + sizeof(int32_t) * std::max<size_t>(R * Q, 1), 16);
+    if (dn.desc) {
+        cudaFree(dn.desc);
+        dn.desc = nullptr;
+    }
+    if (!cuda_ok(cudaMalloc(&dn.desc, total), "cudaMalloc(descriptor)")) return false;
+    std::vector<unsigned char> img(total, 0);
+    if (R) {
+        std::memcpy(img.data() + off_rate, p.rate.data(), sizeof(double) * R);
+        std::memcpy(img.data() + off_jd, p.jmp_d.data(), sizeof(int64_t) * R * Q);
+        std::memcpy(img.data() + off_fsp, p.fac_sp.data(), sizeof(int32_t) * R * P);
+        std::memcpy(img.data() + off_ford, p.fac_ord.data(), sizeof(int32_t) * R * P);
+        std::memcpy(img.data() + off_jsp, p.jmp_sp.data(), sizeof(int32_t) * R * Q);
+    }
+    if (!cuda_ok(cudaMemcpy(dn.desc, img.data(), total, cudaMemcpyHostToDevice), "cudaMemcpy(descriptor)"))
+        return false;
+    unsigned char *b = static_cast<unsigned char *>(dn.desc);
+    dn.rate = reinterpret_cast<double *>(b + off_rate);
+    dn.jmp_d = reinterpret_cast<int64_t *>(b + off_jd);
+    dn.fac_sp = reinterpret_cast<int32_t *>(b + off_fsp);
+    dn.fac_ord = reinterpret_cast<int32_t *>(b + off_ford);
+    dn.jmp_sp = reinterpret_cast<int32_t *>(b + off_jsp);
+    dn.packed = std::move(p);
+    dn.version = net.version;
+    return true;
+}
+
+bool ensure_io(DeviceNet &dn, size_t bytes) {
+    if (dn.io_bytes >= bytes) return true;
+    if (dn.io) {
+        cudaStreamSynchronize(dn.stream);
+        cudaFree(dn.io);
+        dn.io = nullptr;
+        dn.io_bytes = 0;
+    }
+    size_t want = std::max(bytes, dn.io_bytes * 3 / 2);
+    if (!cuda_ok(cudaMalloc(&dn.io, want), "cudaMalloc(staging)")) return false;
+    dn.io_bytes = want;
+    return true;
+}
+
+std::vector<double> sample_times(double tmax, int64_t nb_steps) {
+    std::vector<double> t((size_t)nb_steps + 1);
+    for (int64_t i = 0; i <= nb_steps; i++) t[(size_t)i] = tmax * (double)i / (double)nb_steps;
+    return t;
+}
+
+bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStream_t stream, bool timed,
+                    int *mapping) {
+    DeviceCtx *ctx = device_ctx();
+    if (!ctx) return false;
+    const Packed &p = dn.packed;
+    SsaArgs a{};
+    a.S = p.S;
+    a.R = p.R;
+    a.P = p.P;
+    a.Q = p.Q;
+    a.macro_mode = p.macro_mode;
+    a.rate = r.rates ? r.rates : dn.rate;
+    a.rate_stride = r.rates ? r.rate_stride : 0;
+    a.fac_sp = dn.fac_sp;
+    a.fac_ord = dn.fac_ord;
+    a.jmp_sp = dn.jmp_sp;
+    a.jmp_d = dn.jmp_d;
+    a.n_traj = r.n_traj;
+    a.x0 = r.x0;
+    a.x0_stride = r.x0_stride;
+    a.seeds = r.seeds;
+    a.in_species = r.in_species;
+    a.in_t = r.in_t;
+    a.in_rng = r.in_rng;
+    a.sample_t = r.sample_t;
+    a.n_samples = r.n_samples;
+    a.save_idx = r.save_idx;
+    a.n_save = r.n_save;
+    a.out = r.out;
+    a.fin_species = r.fin_species;
+    a.fin_t = r.fin_t;
+    a.fin_rng = r.fin_rng;
+    a.events = r.events;
+    a.work = dn.scratch;
+    a.zig = ctx->zig;
+    if (!cuda_ok(cudaMemsetAsync(dn.scratch, 0, 2 * sizeof(unsigned long long), stream), "cudaMemsetAsync"))
+        return false;
+    if (r.n_traj == 0) return true;
+    int block = ssa_thread_max_block(a, ctx->smem_optin);
+    if (block == 0) {
+        set_error("network too large for the thread-per-trajectory kernel (" + std::to_string(p.S) +
+                  " species, " + std::to_string(p.R) + " reactions)");
+        return false;
+    }
+    size_t smem = ssa_thread_smem(a, block);
+    int per_sm = ssa_thread_occupancy(a, block, smem);
+    if (per_sm < 1) per_sm = 1;
+    int64_t want = (r.n_traj + block - 1) / block;
+    int64_t cap = (int64_t)ctx->sm_count * per_sm;
+    int grid = (int)std::max<int64_t>(1, std::min(want, cap));
+    if (timed && !cuda_ok(cudaEventRecord(dn.ev_start, stream), "cudaEventRecord")) return false;
+    int err = launch_ssa_thread(a, block, grid, smem, stream);
+    if (err != 0) return cuda_ok((cudaError_t)err, "ssa_thread_kernel launch");
+    if (timed && !cuda_ok(cudaEventRecord(dn.ev_stop, stream), "cudaEventRecord")) return false;
+    if (mapping) *mapping = 0;
+    return true;
+}
+
+}  // namespace rbg

@@ -1,0 +1,86 @@
+// Host engine: per-device context, descriptor upload, kernel launches.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "network.hpp"
+#include "ssa_args.hpp"
+
+namespace rbg {
+
+// Thread-local error channel of the C ABI.
+void set_error(const std::string &msg);
+const std::string &last_error();
+
+// Per-device immutable state: ziggurat tables and device properties.
+struct DeviceCtx {
+    int device = -1;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    double *zig = nullptr;  // device [2][257]
+};
+// Context of the current device (created on first use); nullptr + error on failure.
+DeviceCtx *device_ctx();
+// Host copy of the Exp1 ziggurat tables (x[257], f[257]).
+void zig_tables_host(double *x, double *f);
+
+// Device copy of one network's packed descriptor, its scratch words and the
+// staging buffers of host-pointer calls.
+struct DeviceNet {
+    int device = -1;
+    uint64_t version = 0;
+    Packed packed;
+    void *desc = nullptr;               // rate | jmp_d | fac_sp | fac_ord | jmp_sp
+    double *rate = nullptr;
+    int64_t *jmp_d = nullptr;
+    int32_t *fac_sp = nullptr, *fac_ord = nullptr, *jmp_sp = nullptr;
+    unsigned long long *scratch = nullptr;  // [2]: trajectory ticket, event total
+    void *io = nullptr;                 // staging for rb_ensemble_run & friends
+    size_t io_bytes = 0;
+    cudaStream_t stream = nullptr;      // library stream of host-pointer calls
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    cudaStream_t last_stream = nullptr; // stream of the last device-pointer run
+    ~DeviceNet();
+};
+
+// Make net.dev current for the active device and descriptor version.
+// Caller holds net.mu.  Returns false (error set) on failure.
+bool ensure_device(const Network &net);
+// Grow net.dev->io to at least `bytes`.
+bool ensure_io(DeviceNet &dn, size_t bytes);
+
+// Device-side request of one sampled run (all pointers device pointers).
+struct RunDev {
+    int64_t n_traj = 0;
+    const int64_t *x0 = nullptr;
+    int64_t x0_stride = 0;
+    const double *rates = nullptr;  // nullptr: network rates
+    int64_t rate_stride = 0;
+    const uint64_t *seeds = nullptr;
+    const int64_t *in_species = nullptr;
+    const double *in_t = nullptr;
+    const uint64_t *in_rng = nullptr;
+    const double *sample_t = nullptr;
+    int64_t n_samples = 0;
+    const int32_t *save_idx = nullptr;
+    int32_t n_save = 0;
+    int64_t *out = nullptr;
+    int64_t *fin_species = nullptr;
+    double *fin_t = nullptr;
+    uint64_t *fin_rng = nullptr;
+    uint64_t *events = nullptr;
+};
+
+// Enqueue the sampled-run kernel on `stream` (scratch reset included).
+// Records ev_start/ev_stop around the kernel when `timed`.
+bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStream_t stream, bool timed,
+                    int *mapping);
+
+// Sample times t_i = tmax * i / nb_steps, i = 0..nb_steps (pyo3_gillespie.rs:202).
+std::vector<double> sample_times(double tmax, int64_t nb_steps);
+
+}  // namespace rbg

@@ -1,0 +1,85 @@
+// Kernel argument block of the SSA kernels (plain C++, shared by the CUDA
+// translation units and the host glue).  All pointers are device pointers.
+#pragma once
+
+#include <cstdint>
+
+namespace rbg {
+
+constexpr int kZigLayers = 256;            // ziggurat layers of the Exp1 sampler
+constexpr int kZigTable = kZigLayers + 1;  // abscissae x[0..256] / f(x) values
+
+struct SsaArgs {
+    // packed network (see network.hpp: Packed)
+    int32_t S, R, P, Q;
+    int32_t macro_mode;
+    const double *rate;      // [R] shared, or [n_traj][R] when rate_stride == R
+    int64_t rate_stride;     // 0 or R
+    const int32_t *fac_sp;   // [R*P]
+    const int32_t *fac_ord;  // [R*P]
+    const int32_t *jmp_sp;   // [R*Q]
+    const int64_t *jmp_d;    // [R*Q]
+
+    // trajectories
+    int64_t n_traj;
+    const int64_t *x0;       // fresh start: [S] or [n_traj][S]
+    int64_t x0_stride;       // 0 or S
+    const uint64_t *seeds;   // fresh start: [n_traj]
+    const int64_t *in_species;  // resume: [n_traj][S]   (non-null = resume mode)
+    const double *in_t;         // resume: [n_traj]
+    const uint64_t *in_rng;     // resume: [n_traj][4]
+
+    // sampling
+    const double *sample_t;  // [n_samples] advance_until targets
+    int64_t n_samples;
+    const int32_t *save_idx; // [n_save]
+    int32_t n_save;
+    int64_t *out;            // [n_samples][n_save][n_traj]
+
+    // outputs (nullable)
+    int64_t *fin_species;    // [n_traj][S]
+    double *fin_t;           // [n_traj]
+    uint64_t *fin_rng;       // [n_traj][4]
+    uint64_t *events;        // [n_traj]
+
+    // scratch: [0] trajectory ticket, [1] total accepted events
+    unsigned long long *work;
+
+    // Exp1 ziggurat tables: x[257] then f[257]
+    const double *zig;
+};
+
+// Launch the thread-per-trajectory kernel; returns a cudaError_t value.
+int launch_ssa_thread(const SsaArgs &a, int block, int grid, size_t smem, void *stream);
+size_t ssa_thread_smem(const SsaArgs &a, int block);
+int ssa_thread_max_block(const SsaArgs &a, size_t smem_limit);
+int ssa_thread_occupancy(const SsaArgs &a, int block, size_t smem);
+
+// Every-event runs (src/pyo3_gillespie.rs:209-223) and single
+// _advance_one_reaction steps (src/gillespie.rs:269-297): one thread per
+// trajectory, state in place in global memory.
+struct EventArgs {
+    int32_t S, R, P, Q;
+    int32_t macro_mode;
+    const double *rate;      // [R]
+    const int32_t *fac_sp, *fac_ord, *jmp_sp;
+    const int64_t *jmp_d;
+    int64_t n_traj;
+    int64_t *species;        // [n_traj][S] in/out
+    double *t;               // [n_traj] in/out
+    uint64_t *rng;           // [n_traj][4] in/out
+    double tmax;
+    int32_t gate;            // 1: step while t < tmax; 0: no horizon
+    int64_t max_steps;       // < 0: unlimited
+    int32_t record_initial;  // record the state before the first step
+    const int32_t *save_idx;
+    int32_t n_save;
+    int64_t cap;             // records kept per trajectory
+    double *rec_t;           // [n_traj][cap]
+    int64_t *rec_out;        // [n_traj][cap][n_save]
+    int64_t *n_rec;          // [n_traj] records produced (may exceed cap)
+    const double *zig;
+};
+int launch_ssa_events(const EventArgs &a, void *stream);
+
+}  // namespace rbg

@@ -1,0 +1,259 @@
+"""GPU parity: the engine's kernels against the oracle, bit for bit.
+
+Integer counts, event counts and reaction sequences must be identical; the
+random stream is the reference's (xoshiro256++ / ziggurat Exp1) keyed by the
+same seed on both sides.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rb():
+    import rebop_gb300
+
+    return rebop_gb300
+
+
+def _sir(rb, k1=1e-4, k2=0.01):
+    n = rb.Network(3)
+    n.add_reaction(rb.Rate.lma(k1, [1, 1, 0]), [-1, 1, 0])
+    n.add_reaction(rb.Rate.lma(k2, [0, 1, 0]), [0, -1, 1])
+    return n
+
+
+def _dimer(rb):
+    n = rb.Network(4)
+    n.add_reaction(rb.Rate.lma(25.0, [1, 0, 0, 0]), [0, 1, 0, 0])
+    n.add_reaction(rb.Rate.lma(1000.0, [0, 1, 0, 0]), [0, 0, 1, 0])
+    n.add_reaction(rb.Rate.lma(0.001, [0, 0, 2, 0]), [0, 0, -2, 1])
+    n.add_reaction(rb.Rate.lma(0.1, [0, 1, 0, 0]), [0, -1, 0, 0])
+    n.add_reaction(rb.Rate.lma(1.0, [0, 0, 1, 0]), [0, 0, -1, 0])
+    return n
+
+
+def _seeds(n, salt=0):
+    return np.random.default_rng(1234 + salt).integers(np.iinfo(np.uint64).max, size=n, dtype=np.uint64)
+
+
+def test_fixed_seed_golden_through_dropin(rb, goldens):
+    # tests/test_rebop.py:30-36 through the Python drop-in, on the GPU.
+    fs = goldens["fixed_seed"]
+    sir = rb.Gillespie()
+    sir.add_reaction(1e-4, ["S", "I"], ["I", "I"])
+    sir.add_reaction(0.01, ["I"], ["R"])
+    ds = sir.run(fs["init"], tmax=fs["tmax"], nb_steps=fs["nb_steps"], rng=fs["rng"])
+    np.testing.assert_array_equal(np.asarray(ds.time), np.arange(251))
+    assert [int(ds[s][-1]) for s in ("S", "I", "R")] == [fs["final"][s] for s in ("S", "I", "R")]
+
+
+def test_sir_ensemble_bit_exact(rb, O):
+    seeds = _seeds(1000)
+    res = _sir(rb).run_ensemble([999, 1, 0], seeds, 250.0, 250)
+    ref, ev, tot, _ = O.sir_net().run_ensemble([999, 1, 0], seeds, 250.0, 250)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+    assert res.total_events == tot
+    np.testing.assert_array_equal(res.times, np.arange(251.0))
+
+
+def test_dimer_ensemble_bit_exact(rb, O):
+    seeds = _seeds(1500, 1)
+    res = _dimer(rb).run_ensemble([1, 0, 0, 0], seeds, 1.0, 100, want_final=True)
+    ref, ev, tot, fin = O.dimer_net().run_ensemble([1, 0, 0, 0], seeds, 1.0, 100, want_final=True)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+    np.testing.assert_array_equal(res.final, fin)
+    assert res.total_events == tot > 1500 * 10_000
+
+
+def test_per_trajectory_x0_rates_and_saved_subset(rb, O):
+    n = 700
+    rng = np.random.default_rng(5)
+    x0 = np.stack([rng.integers(500, 1500, n), rng.integers(1, 20, n), np.zeros(n, np.int64)], axis=1)
+    rates = np.stack([10 ** rng.uniform(-5, -3, n), 10 ** rng.uniform(-3, -1, n)], axis=1)
+    seeds = _seeds(n, 2)
+    res = _sir(rb).run_ensemble(x0, seeds, 100.0, 37, rates=rates, save=[2, 0])
+    ref, ev, _, _ = O.sir_net().run_ensemble(x0, seeds, 100.0, 37, save_idx=[2, 0], rates=rates)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+
+
+def test_sparse_pairs_in_caller_order(rb, O):
+    # Rate::lma_sparse multiplies its pairs in the given order (gillespie.rs:79-86);
+    # a repeated index multiplies twice.
+    net = rb.Network(3)
+    net.add_reaction(rb.Rate.lma_sparse(3e-4, [(1, 1), (0, 1)]), [-1, 1, 0])
+    net.add_reaction(rb.Rate.lma_sparse(1e-6, [(1, 1), (1, 1)]), [0, -1, 1])
+    net.add_reaction(rb.Rate.lma(0.02, [0, 1, 0]), [0, -1, 1])
+    o = (O.OracleNet(3).add_lma_sparse(3e-4, [(1, 1), (0, 1)], [-1, 1, 0])
+         .add_lma_sparse(1e-6, [(1, 1), (1, 1)], [0, -1, 1]).add_lma(0.02, [0, 1, 0], [0, -1, 1]))
+    seeds = _seeds(300, 3)
+    res = net.run_ensemble([900, 5, 0], seeds, 60.0, 30)
+    ref, ev, _, _ = o.run_ensemble([900, 5, 0], seeds, 60.0, 30)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+
+
+DIMER_DSL = """
+    rtx rtl rdi rdm rdp;
+    Dimers { gene, mRNA, protein, dimer }
+    transcription   : gene      => gene + mRNA      @ rtx
+    translation     : mRNA      => mRNA + protein   @ rtl
+    dimerization    : 2 protein => dimer            @ rdi
+    decay_mRNA      : mRNA      =>                  @ rdm
+    decay_prot      : protein   =>                  @ rdp
+"""
+
+
+def test_define_system_bit_exact(rb, O):
+    D = rb.define_system(DIMER_DSL)
+    d = D.with_parameters(25.0, 1000.0, 0.001, 0.1, 1.0)
+    d.gene = 1
+    seeds = _seeds(400, 4)
+    res = d.run_ensemble(seeds, 1.0, 20)
+    o = (O.OracleNet(4, macro=True).add_macro(25.0, [(0, 1)], [0, 1, 0, 0])
+         .add_macro(1000.0, [(1, 1)], [0, 0, 1, 0]).add_macro(0.001, [(2, 2)], [0, 0, -2, 1])
+         .add_macro(0.1, [(1, 1)], [0, -1, 0, 0]).add_macro(1.0, [(2, 1)], [0, 0, -1, 0]))
+    ref, ev, _, _ = o.run_ensemble([1, 0, 0, 0], seeds, 1.0, 20)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+    # the struct API: seed + advance_until, gillespie_macro.rs:192-208
+    d2 = D.with_parameters(25.0, 1000.0, 0.001, 0.1, 1.0)
+    d2.gene = 1
+    d2.seed(int(seeds[0]))
+    d2.advance_until(1.0)
+    assert d2.t == 1.0 and d2.gene == 1 and 1000 < d2.dimer < 10000
+
+
+def test_define_system_forgotten_parameter_and_no_reactions(rb):
+    BD = rb.define_system("r_birth r_death; BirthDeath { A } birth: => A @ r_birth death: A => @ r_death")
+    bd = BD.new()
+    bd.r_birth = 10.0
+    bd.advance_until(100.0)  # r_death is NaN: no reaction (gillespie_macro.rs:225-238)
+    assert bd.t == 100.0 and bd.A == 0
+    F = rb.define_system("; FooBarBuz { Foo, Bar, Buz }")
+    f = F.new()
+    f.Foo, f.Bar = 42, 1337
+    f.advance_until(1e20)
+    assert f.t == 1e20 and (f.Foo, f.Bar, f.Buz) == (42, 1337, 0)
+
+
+def test_rust_api_stateful_trajectory(rb, O):
+    # Gillespie::new_with_seed + repeated advance_until (gillespie.rs:301-344).
+    g = rb.api.Gillespie.new_with_seed([1, 0, 0, 0], False, 777)
+    g.add_reaction(rb.Rate.lma(25.0, [1, 0, 0, 0]), [0, 1, 0, 0])
+    g.add_reaction(rb.Rate.lma(1000.0, [0, 1, 0, 0]), [0, 0, 1, 0])
+    g.add_reaction(rb.Rate.lma(0.001, [0, 0, 2, 0]), [0, 0, -2, 1])
+    g.add_reaction(rb.Rate.lma(0.1, [0, 1, 0, 0]), [0, -1, 0, 0])
+    g.add_reaction(rb.Rate.lma(1.0, [0, 0, 1, 0]), [0, 0, -1, 0])
+    assert g.get_time() == 0.0 and g.get_species(3) == 0
+    net = O.dimer_net()
+    sp, t, st = [1, 0, 0, 0], 0.0, O.seed_state(777)
+    for tm in (0.1, 0.25, 0.25, 0.7, 1.0):
+        g.advance_until(tm)
+        sp, t, st, _, _, _ = net.advance_until(sp, t, st, tm)
+        assert g.get_time() == t == tm
+        assert [g.get_species(s) for s in range(4)] == sp.tolist()
+    # set_species / set_time then continue
+    g.set_species([1, 5, 5, 5])
+    g.set_time(2.0)
+    g.advance_until(2.5)
+    sp, t, st, _, _, _ = net.advance_until([1, 5, 5, 5], 2.0, st, 2.5)
+    assert [g.get_species(s) for s in range(4)] == sp.tolist()
+    with pytest.raises(ValueError):
+        g.get_species(4)
+
+
+def test_advance_one_reaction_and_every_event_mode(rb, O):
+    net = _sir(rb)
+    for seed in (3, 11, 2024):
+        times, out = net.run_all_events([999, 1, 0], seed, 250.0)
+        rt, ro = O.sir_net().run_all_events([999, 1, 0], seed, 250.0)
+        np.testing.assert_array_equal(times, rt)
+        np.testing.assert_array_equal(out, ro)
+    # absorbing state: the last record has t = +inf (tests/test_rebop.py:47-48)
+    dead = rb.Network(1)
+    dead.add_reaction(rb.Rate.lma(1.0, [1]), [-1])
+    times, out = dead.run_all_events([3], 5, 1e9)
+    assert np.isinf(times[-1]) and out[-1, 0] == 0 and len(times) == 5
+    g = rb.api.Gillespie.new_with_seed([999, 1, 0], False, 3)
+    g.add_reaction(rb.Rate.lma(1e-4, [1, 1, 0]), [-1, 1, 0])
+    g.add_reaction(rb.Rate.lma(0.01, [0, 1, 0]), [0, -1, 1])
+    for k in range(1, 6):
+        g.advance_one_reaction()
+        assert g.get_time() == rt[k]
+        assert [g.get_species(s) for s in range(3)] == ro[k].tolist()
+
+
+def test_dropin_every_event_and_var_names(rb, O):
+    sir = rb.Gillespie()
+    sir.add_reaction(1e-4, ["S", "I"], ["I", "I"])
+    sir.add_reaction(0.01, ["I"], ["R"])
+    ds = sir.run({"S": 999, "I": 1}, tmax=250, nb_steps=0, rng=4)
+    rt, ro = O.sir_net().run_all_events([999, 1, 0], O.numpy_seed(4), 250.0)
+    np.testing.assert_array_equal(np.asarray(ds.time), rt)
+    np.testing.assert_array_equal(np.asarray(ds.R), ro[:, 2])
+    full = sir.run({"S": 999, "I": 1}, tmax=250, nb_steps=250, rng=0)
+    sub = sir.run({"S": 999, "I": 1}, tmax=250, nb_steps=250, rng=0, var_names=["S", "I"])
+    assert "R" not in sub and "S" in sub
+    np.testing.assert_array_equal(np.asarray(full.S), np.asarray(sub.S))
+    ens = sir.run_ensemble({"S": 999, "I": 1}, 250, 250, 64, rng=0)
+    np.testing.assert_array_equal(np.asarray(ens.S)[0], np.asarray(full.S))
+
+
+def test_edge_cases(rb, O):
+    # no reactions: counts constant; the clock jumps to each sample time
+    empty = rb.Network(2)
+    res = empty.run_ensemble([3, 4], _seeds(33), 10.0, 10)
+    assert np.all(res.counts[:, 0] == 3) and np.all(res.counts[:, 1] == 4) and res.total_events == 0
+    # no species at all (tests/test_rebop.py:148-152)
+    none = rb.Gillespie()
+    ds = none.run({}, tmax=10, nb_steps=10)
+    assert len(ds) == 0
+    np.testing.assert_array_equal(np.asarray(ds.time), np.linspace(0, 10, 11))
+    # NaN and negative rates: !(0 < total) absorbs, as the reference does
+    nan = rb.Network(1)
+    nan.add_reaction(rb.Rate.lma(math.nan, [1]), [-1])
+    assert np.all(nan.run_ensemble([5], _seeds(3), 1.0, 4).counts == 5)
+    neg = rb.Network(1)
+    neg.add_reaction(rb.Rate.lma(-1.0, [1]), [-1])
+    assert np.all(neg.run_ensemble([5], _seeds(3), 1.0, 4).counts == 5)
+    # zero trajectories
+    z = _sir(rb).run_ensemble([999, 1, 0], np.zeros(0, np.uint64), 1.0, 3)
+    assert z.counts.shape == (4, 3, 0)
+    # trajectory counts that are not a multiple of the block size, large counts
+    big = rb.Network(2)
+    big.add_reaction(rb.Rate.lma(1e-9, [2, 0]), [-2, 1])
+    big.add_reaction(rb.Rate.lma(1e3, [0, 0]), [1, 0])
+    ob = O.OracleNet(2).add_lma(1e-9, [2, 0], [-2, 1]).add_lma(1e3, [0, 0], [1, 0])
+    seeds = _seeds(129, 9)
+    res = big.run_ensemble([3_000_000_000, 0], seeds, 0.5, 5)
+    ref, ev, _, _ = ob.run_ensemble([3_000_000_000, 0], seeds, 0.5, 5)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+
+
+def test_device_entry_point_matches_host_entry_point(rb, O):
+    torch = pytest.importorskip("torch")
+    net = _dimer(rb)
+    n = 777
+    seeds = _seeds(n, 6)
+    d_seeds = torch.from_numpy(seeds.view(np.int64)).cuda()
+    d_x0 = torch.tensor([1, 0, 0, 0], dtype=torch.int64, device="cuda")
+    d_out = torch.empty((11, 4, n), dtype=torch.int64, device="cuda")
+    d_ev = torch.empty(n, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    net.run_ensemble_device(n, d_x0.data_ptr(), False, d_seeds.data_ptr(), 0.5, 10, d_out.data_ptr(),
+                            events_ptr=d_ev.data_ptr(), stream=stream)
+    total = net.last_events()
+    torch.cuda.synchronize()
+    ref, ev, tot, _ = O.dimer_net().run_ensemble([1, 0, 0, 0], seeds, 0.5, 10)
+    np.testing.assert_array_equal(d_out.cpu().numpy(), ref)
+    np.testing.assert_array_equal(d_ev.cpu().numpy().view(np.uint64), ev)
+    assert total == tot

@@ -1,0 +1,181 @@
+"""Host-side logic and the C ABI surface, on the CPU (no kernel runs here)."""
+
+import ctypes
+import re
+import warnings
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def rb():
+    import rebop_gb300
+
+    return rebop_gb300
+
+
+def _header_symbols():
+    text = (ROOT / "include" / "rebop_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rb_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_header_symbol(rb):
+    from rebop_gb300 import build
+
+    lib = ctypes.CDLL(str(build.LIB))
+    syms = _header_symbols()
+    assert len(syms) >= 30
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_version_and_error_channel(rb):
+    from rebop_gb300._lib import last_error, lib
+
+    assert re.match(r"\d+\.\d+\.\d+", lib.rb_version().decode())
+    h = ctypes.c_void_p()
+    assert lib.rb_network_create(-1, ctypes.byref(h)) == 1
+    assert "negative" in last_error()
+
+
+def test_add_reaction_shape_asserts(rb):
+    # src/gillespie.rs:227-237: exponent and difference vectors need S entries.
+    n = rb.Network(3)
+    with pytest.raises(ValueError, match="assertion failed"):
+        n.add_reaction(rb.Rate.lma(1.0, [1, 0]), [0, 0, 0])
+    with pytest.raises(ValueError, match="assertion failed"):
+        n.add_reaction(rb.Rate.lma(1.0, [1, 0, 0]), [0, 0])
+    n.add_reaction(rb.Rate.lma(1.0, [1, 0, 0]), [-1, 0, 1])
+    assert n.nb_reactions == 1 and n.nb_species == 3
+
+
+def test_issue85_out_of_range_sparse_index(rb):
+    # src/gillespie.rs:496-502: the reference panics; the ABI returns RB_ERR_INVALID.
+    g = rb.api.Gillespie.new_with_seed([1], True, 0)
+    with pytest.raises(ValueError, match="assertion failed"):
+        g.add_reaction(rb.Rate.lma_sparse(1.0, [(10, 1)]), [0])
+    assert g.nb_reactions() == 0
+
+
+def test_rate_and_jump_conversions(rb, goldens):
+    # src/gillespie.rs:421-446 and :474-482
+    Rate, Jump = rb.api.Rate, rb.api.Jump
+    for case in goldens["rate_sparse"]:
+        r = Rate.lma(case["rate"], case["dense"])
+        assert r.sparse() == Rate.lma_sparse(case["rate"], [tuple(p) for p in case["sparse"]])
+    r = Rate.lma(2.0, [3])
+    assert r.dense() == r and r.sparse().dense() == r
+    r = Rate.lma_sparse(2.0, [(0, 1), (3, 2)])
+    assert r.dense() == Rate.lma(2.0, [1, 0, 0, 2]) and r.dense().sparse() == r
+    dj, sj = Jump.new([-1, 0, 3, -2]), Jump.new_sparse([(0, -1), (2, 3), (3, -2)])
+    assert dj.sparse() == sj and sj.dense() == dj and dj.dense() == dj and sj.sparse() == sj
+
+
+VILAR = """
+    αA αpA αR αpR βA βR δMA δMR δA δR γA γR γC θA θR;
+    Vilar { Da, Dr, Dpa, Dpr, Ma, Mr, A, R, C }
+    r_activation_a      : Da + A    => Dpa      @ γA
+    r_activation_r      : Dr + A    => Dpr      @ γR
+    r_deactivation_a    : Dpa       => Da + A   @ θA
+    r_deactivation_r    : Dpr       => Dr + A   @ θR
+    r_transcription_a   : Da        => Da + Ma  @ αA
+    r_transcription_r   : Dr        => Dr + Mr  @ αR
+    r_transcription_p_a : Dpa       => Dpa + Ma @ αpA
+    r_transcription_p_r : Dpr       => Dpr + Mr @ αpR
+    r_translation_a     : Ma        => Ma + A   @ βA
+    r_translation_r     : Mr        => Mr + R   @ βR
+    r_complexation      : A + R     => C        @ γC
+    r_decomplexation    : C         => R        @ δA
+    r_decay_mRNA_a      : Ma        =>          @ δMA
+    r_decay_mRNA_r      : Mr        =>          @ δMR
+    r_decay_prot_a      : A         =>          @ δA
+    r_decay_prot_r      : R         =>          @ δR
+"""
+
+
+def test_dsl_lowering(rb):
+    # benchmarks/benches/vilar/vilar.rs:6-25 (Greek identifiers included)
+    net = rb.Network.from_dsl(VILAR)
+    assert net.name == "Vilar" and net.nb_species == 9 and net.nb_reactions == 16
+    assert net.params[0] == "αA" and net.species[-1] == "C"
+    assert np.isnan(net.reaction_rate(0))  # parameters start as NaN
+    net.set_param("γA", 1.0)
+    assert net.reaction_rate(0) == 1.0
+    n2 = rb.Network.from_dsl("k; X { A } r: 2 A => A @ k * 0.5 / 2")
+    n2.set_param("k", 8.0)
+    assert n2.reaction_rate(0) == 2.0
+    for bad in ("k; X { A } r: B => A @ k", "k; X { A } r: 0 A => A @ k", "k; X { A } r: A => A @ q",
+                "X { A }", "k; X { A } r: A => A @ A"):
+        with pytest.raises(ValueError):
+            rb.Network.from_dsl(bad)
+
+
+def test_expr_parser_goldens(rb, goldens):
+    from rebop_gb300 import expr
+
+    for case in goldens["expr_eval"]:
+        e = expr.parse(case["expr"]).to_expr(case["species_index"], {})
+        assert e.eval(case["species"]) == case["expected"], case["where"]
+    for bad in ("+", "1+", " 1", "1 ", "2e", "a^b^c", "max(1)", "(1"):
+        with pytest.raises(expr.ParseError):
+            expr.parse(bad)
+    assert str(expr.parse("V * A / (Km + A)")) == "((V * A) / (Km + A))"
+    assert str(expr.parse("1e-5*x")) == "(0.00001 * x)"
+    assert expr.parse("maximum").op == "var" and expr.parse("inf").op == "var"
+
+
+def test_dropin_python_errors_and_text(rb):
+    # tests/test_rebop.py:92-97 and :155-159; pyo3_gillespie.rs:239-252
+    s = rb.Gillespie()
+    with pytest.raises(ValueError, match="Rate expression not understood"):
+        s.add_reaction("+", [], ["A"])
+    with pytest.raises(ValueError, match="Rate expression not understood"):
+        s.add_reaction("1+", [], ["A"])
+    s = rb.Gillespie()
+    s.add_reaction(4, ["A"], ["B"])
+    with pytest.raises(ValueError, match="Species B cannot also be a parameter"):
+        s.run({}, 10, 10, params={"B": 4.2})
+    s = rb.Gillespie()
+    s.add_reaction(0.1, ["A", "B"], ["C"], 0.01)
+    s.add_reaction(14, [], ["A"])
+    assert s.nb_reactions() == 3 and s.nb_species() == 3
+    assert str(s) == ("3 species and 3 reactions\nA + B --> C @ LMA(0.1)\nC --> A + B @ LMA(0.01)\n"
+                      " --> A @ LMA(14)\n")
+
+
+def test_dropin_set_init_warning_adds_species(rb):
+    s = rb.Gillespie()
+    s.add_reaction(1.0, [], ["A"])
+    assert s.set_init({"B": 1}) is True
+    assert s.nb_species() == 2
+
+
+def test_partition_independence_of_seeds():
+    # Trajectory j's stream depends only on its own seed, so any split of the
+    # trajectory range across ranks reproduces the unsplit ensemble.
+    from oracle import oracle as O
+
+    net = O.sir_net()
+    seeds = np.random.default_rng(0).integers(np.iinfo(np.uint64).max, size=40, dtype=np.uint64)
+    full = net.run_ensemble([999, 1, 0], seeds, 50.0, 10)[0]
+    parts = [net.run_ensemble([999, 1, 0], seeds[a:b], 50.0, 10)[0] for a, b in ((0, 13), (13, 27), (27, 40))]
+    assert np.array_equal(np.concatenate(parts, axis=2), full)
+
+
+def test_product_zig_tables_equal_oracle(rb, O):
+    x, f = rb.api.zig_tables()
+    ox, of = O.zig_tables()
+    assert np.array_equal(x.view(np.uint64), ox.view(np.uint64))
+    assert np.array_equal(f.view(np.uint64), of.view(np.uint64))
+
+
+def test_no_oracle_import_in_product():
+    for p in (ROOT / "rebop_gb300").rglob("*"):
+        if p.suffix in (".py", ".cpp", ".cu", ".cuh", ".hpp", ".h"):
+            text = p.read_text(encoding="utf-8")
+            assert "oracle" not in text.lower() or p.name == "build.py", p
