@@ -37,7 +37,9 @@ extern "C" {
 #define RB_ERR_NOMEM 3       /* host or device allocation failed */
 #define RB_ERR_PARSE 4       /* define_system! text not understood */
 #define RB_ERR_UNSUPPORTED 5 /* network shape outside every kernel's range */
-#define RB_ERR_TIMEOUT 6     /* a kernel hit its event budget (see rb_run_stats) */
+#define RB_ERR_TIMEOUT 6     /* a kernel ran out of its wall-clock budget
+                              * (RB_KERNEL_BUDGET_S seconds, default 120);
+                              * results of that call are incomplete */
 
 /* Library version string ("<major>.<minor>.<patch>"). */
 const char *rb_version(void);
@@ -135,7 +137,8 @@ int rb_ensemble_run_device(const rb_network *net, int64_t n_traj, const int64_t 
                            uint64_t *d_events, int64_t *d_final_species, void *stream);
 
 /* Sum of accepted events of the last rb_ensemble_run_device on this network
- * (synchronises with that run's stream). */
+ * (synchronises with that run's stream); RB_ERR_TIMEOUT if that run ran out
+ * of its time budget. */
 int rb_ensemble_last_events(const rb_network *net, uint64_t *events);
 
 /* Every-event run of one trajectory, src/pyo3_gillespie.rs:209-223: records

@@ -116,10 +116,13 @@ int single_advance(const rbg::Network &net, int64_t *species, double *t, uint64_
     r.fin_t = reinterpret_cast<double *>(b + o_ft);
     r.fin_rng = reinterpret_cast<uint64_t *>(b + o_frng);
     if (!rbg::launch_sampled(net, dn, r, dn.stream, false, nullptr)) return RB_ERR_CUDA;
+    unsigned long long flag = 0;
     if (!cuda_check(cudaMemcpyAsync(h.data() + o_fsp, b + o_fsp, c.off - o_fsp, cudaMemcpyDeviceToHost, dn.stream),
                     "cudaMemcpyAsync") ||
+        !cuda_check(cudaMemcpyAsync(&flag, dn.scratch + 2, 8, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync") ||
         !cuda_check(cudaStreamSynchronize(dn.stream), "ssa_thread_kernel"))
         return RB_ERR_CUDA;
+    if (flag) return fail(RB_ERR_TIMEOUT, "advance_until ran out of its time budget (RB_KERNEL_BUDGET_S)");
     if (S) std::memcpy(species, h.data() + o_fsp, S * 8);
     std::memcpy(t, h.data() + o_ft, 8);
     std::memcpy(rng, h.data() + o_frng, 32);
@@ -176,14 +179,21 @@ int events_run(const rbg::Network &net, int64_t *species, double *t, uint64_t *r
     a.rec_out = reinterpret_cast<int64_t *>(b + o_ro);
     a.n_rec = reinterpret_cast<int64_t *>(b + o_n);
     a.zig = ctx->zig;
+    a.flag = dn.scratch + 2;
+    a.budget_ns = rbg::kernel_budget_ns();
+    if (!cuda_check(cudaMemsetAsync(dn.scratch, 0, 4 * sizeof(unsigned long long), dn.stream), "cudaMemsetAsync"))
+        return RB_ERR_CUDA;
     int err = rbg::launch_ssa_events(a, dn.stream);
     if (err) return cuda_check((cudaError_t)err, "ssa_events_kernel launch") ? RB_OK : RB_ERR_CUDA;
     int64_t n = 0;
+    unsigned long long flag = 0;
     std::vector<unsigned char> st(o_save, 0);
     if (!cuda_check(cudaMemcpyAsync(st.data(), b, o_save, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync") ||
         !cuda_check(cudaMemcpyAsync(&n, b + o_n, 8, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync") ||
+        !cuda_check(cudaMemcpyAsync(&flag, dn.scratch + 2, 8, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync") ||
         !cuda_check(cudaStreamSynchronize(dn.stream), "ssa_events_kernel"))
         return RB_ERR_CUDA;
+    if (flag) return fail(RB_ERR_TIMEOUT, "every-event run ran out of its time budget (RB_KERNEL_BUDGET_S)");
     int64_t kept = std::min<int64_t>(n, (int64_t)K);
     if (kept > 0 && times &&
         !cuda_check(cudaMemcpy(times, b + o_rt, (size_t)kept * 8, cudaMemcpyDeviceToHost), "cudaMemcpy"))
@@ -364,21 +374,22 @@ int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, i
         d2h += bytes;
         return cuda_check(cudaMemcpyAsync(dst, b + off, bytes, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync");
     };
-    uint64_t total_events = 0;
+    unsigned long long sc[2] = {0, 0};  // total events, timeout flag
     if (!d2h_copy(out, o_out, NT * NS * N * 8) || !d2h_copy(events, o_ev, N * 8) ||
         !d2h_copy(final_species, o_fin, final_species ? N * S * 8 : 0) ||
-        !cuda_check(cudaMemcpyAsync(&total_events, dn.scratch + 1, 8, cudaMemcpyDeviceToHost, dn.stream),
-                    "cudaMemcpyAsync") ||
+        !cuda_check(cudaMemcpyAsync(sc, dn.scratch + 1, 16, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync") ||
         !cuda_check(cudaStreamSynchronize(dn.stream), "ssa_thread_kernel"))
         return RB_ERR_CUDA;
+    if (sc[1]) return fail(RB_ERR_TIMEOUT, "ensemble run ran out of its time budget (RB_KERNEL_BUDGET_S)");
+    const uint64_t total_events = sc[0];
     if (stats) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, dn.ev_start, dn.ev_stop);
+        if (N) cudaEventElapsedTime(&ms, dn.ev_start, dn.ev_stop);
         stats->events = total_events;
         stats->kernel_ms = ms;
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
         stats->h2d_bytes = h2d;
-        stats->d2h_bytes = d2h + 8;
+        stats->d2h_bytes = d2h + 16;
         stats->kernel_launches = N ? 1 : 0;
         stats->mapping = mapping;
     }
@@ -442,9 +453,12 @@ int rb_ensemble_last_events(const rb_network *netp, uint64_t *events) {
     std::lock_guard<std::mutex> lk(net.mu);
     if (!net.dev) return fail(RB_ERR_INVALID, "no run on this network yet");
     rbg::DeviceNet &dn = *net.dev;
+    unsigned long long sc[2] = {0, 0};
     if (!cuda_check(cudaStreamSynchronize(dn.last_stream), "cudaStreamSynchronize") ||
-        !cuda_check(cudaMemcpy(events, dn.scratch + 1, 8, cudaMemcpyDeviceToHost), "cudaMemcpy"))
+        !cuda_check(cudaMemcpy(sc, dn.scratch + 1, 16, cudaMemcpyDeviceToHost), "cudaMemcpy"))
         return RB_ERR_CUDA;
+    *events = sc[0];
+    if (sc[1]) return fail(RB_ERR_TIMEOUT, "ensemble run ran out of its time budget (RB_KERNEL_BUDGET_S)");
     return RB_OK;
 }
 

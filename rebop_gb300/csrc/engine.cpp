@@ -2,6 +2,7 @@
 #include "engine.hpp"
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -89,7 +90,7 @@ bool ensure_device(const Network &net) {
         if (!cuda_ok(cudaStreamCreateWithFlags(&dn->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
             !cuda_ok(cudaEventCreate(&dn->ev_start), "cudaEventCreate") ||
             !cuda_ok(cudaEventCreate(&dn->ev_stop), "cudaEventCreate") ||
-            !cuda_ok(cudaMalloc(&dn->scratch, 2 * sizeof(unsigned long long)), "cudaMalloc(scratch)"))
+            !cuda_ok(cudaMalloc(&dn->scratch, 4 * sizeof(unsigned long long)), "cudaMalloc(scratch)"))
             return false;
         net.dev = std::move(dn);
     }
@@ -143,6 +144,13 @@ bool ensure_io(DeviceNet &dn, size_t bytes) {
     return true;
 }
 
+int64_t kernel_budget_ns() {
+    const char *env = std::getenv("RB_KERNEL_BUDGET_S");
+    double sec = env ? std::atof(env) : 120.0;
+    if (!(sec > 0)) sec = 120.0;
+    return (int64_t)(sec * 1e9);
+}
+
 std::vector<double> sample_times(double tmax, int64_t nb_steps) {
     std::vector<double> t((size_t)nb_steps + 1);
     for (int64_t i = 0; i <= nb_steps; i++) t[(size_t)i] = tmax * (double)i / (double)nb_steps;
@@ -184,7 +192,8 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     a.events = r.events;
     a.work = dn.scratch;
     a.zig = ctx->zig;
-    if (!cuda_ok(cudaMemsetAsync(dn.scratch, 0, 2 * sizeof(unsigned long long), stream), "cudaMemsetAsync"))
+    a.budget_ns = kernel_budget_ns();
+    if (!cuda_ok(cudaMemsetAsync(dn.scratch, 0, 4 * sizeof(unsigned long long), stream), "cudaMemsetAsync"))
         return false;
     if (r.n_traj == 0) return true;
     int block = ssa_thread_max_block(a, ctx->smem_optin);

@@ -38,7 +38,7 @@ struct DeviceNet {
     double *rate = nullptr;
     int64_t *jmp_d = nullptr;
     int32_t *fac_sp = nullptr, *fac_ord = nullptr, *jmp_sp = nullptr;
-    unsigned long long *scratch = nullptr;  // [2]: trajectory ticket, event total
+    unsigned long long *scratch = nullptr;  // [4]: trajectory ticket, event total, timeout flag
     void *io = nullptr;                 // staging for rb_ensemble_run & friends
     size_t io_bytes = 0;
     cudaStream_t stream = nullptr;      // library stream of host-pointer calls
@@ -79,6 +79,9 @@ struct RunDev {
 // Records ev_start/ev_stop around the kernel when `timed`.
 bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStream_t stream, bool timed,
                     int *mapping);
+
+// Per-launch wall-clock budget of the SSA kernels (RB_KERNEL_BUDGET_S, default 120 s).
+int64_t kernel_budget_ns();
 
 // Sample times t_i = tmax * i / nb_steps, i = 0..nb_steps (pyo3_gillespie.rs:202).
 std::vector<double> sample_times(double tmax, int64_t nb_steps);

@@ -61,6 +61,13 @@ __device__ __forceinline__ double uniform53(uint64_t bits) {
 
 __device__ __forceinline__ double xo_uniform(Xoshiro &g) { return uniform53(xo_next(g)); }
 
+// Nanosecond wall clock of the GPU.
+__device__ __forceinline__ int64_t global_ns() {
+    int64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
 constexpr double kZigR = 7.69711747013104972;  // start of the exponential tail
 
 // zx/zf: the 257-entry abscissa and density tables (shared memory).

@@ -42,11 +42,17 @@ struct SsaArgs {
     uint64_t *fin_rng;       // [n_traj][4]
     uint64_t *events;        // [n_traj]
 
-    // scratch: [0] trajectory ticket, [1] total accepted events
+    // scratch: [0] trajectory ticket, [1] total accepted events,
+    // [2] set to 1 when the time budget ran out
     unsigned long long *work;
 
     // Exp1 ziggurat tables: x[257] then f[257]
     const double *zig;
+
+    // Wall-clock budget per launch (ns of %globaltimer from each block's
+    // start).  A clock increment below one ulp of t never reaches the next
+    // sample time; the budget turns that endless loop into RB_ERR_TIMEOUT.
+    int64_t budget_ns;
 };
 
 // Launch the thread-per-trajectory kernel; returns a cudaError_t value.
@@ -79,6 +85,8 @@ struct EventArgs {
     int64_t *rec_out;        // [n_traj][cap][n_save]
     int64_t *n_rec;          // [n_traj] records produced (may exceed cap)
     const double *zig;
+    unsigned long long *flag;  // set to 1 when the time budget ran out
+    int64_t budget_ns;
 };
 int launch_ssa_events(const EventArgs &a, void *stream);
 

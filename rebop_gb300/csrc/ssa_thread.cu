@@ -86,6 +86,9 @@ __global__ void __launch_bounds__(256) ssa_thread_kernel(const __grid_constant__
     int64_t *const sp = m.sp + tid;    // species s of this lane: sp[s * BD]
     double *const cum = m.cum + tid;   // cumulative propensity r: cum[r * BD]
     unsigned long long lane_events = 0;
+    const int64_t t_start = global_ns();
+    bool out_of_time = false;
+    unsigned int tick = 0;
 
     long long traj = (long long)atomicAdd(a.work, 1ull);
     while (traj < a.n_traj) {
@@ -112,6 +115,10 @@ __global__ void __launch_bounds__(256) ssa_thread_kernel(const __grid_constant__
         double total = 0.0;
 
         for (;;) {
+            if ((++tick & 1023u) == 0 && global_ns() - t_start > a.budget_ns) {
+                out_of_time = true;
+                break;
+            }
             if (stale) {
                 // make_cumrates with the LMA (or macro) propensity of every reaction
                 total = 0.0;
@@ -179,6 +186,10 @@ __global__ void __launch_bounds__(256) ssa_thread_kernel(const __grid_constant__
         }
         if (a.events) a.events[traj] = ev;
         lane_events += ev;
+        if (out_of_time) {
+            atomicExch(a.work + 2, 1ull);
+            break;
+        }
         traj = (long long)atomicAdd(a.work, 1ull);
     }
 
@@ -268,7 +279,12 @@ __global__ void __launch_bounds__(128) ssa_events_kernel(const __grid_constant__
     };
     if (a.record_initial) record();
     long long steps = 0;
+    const int64_t t_start = global_ns();
     while ((!a.gate || t < a.tmax) && (a.max_steps < 0 || steps < a.max_steps)) {
+        if ((steps & 1023) == 1023 && global_ns() - t_start > a.budget_ns) {
+            atomicExch(a.flag, 1ull);
+            break;
+        }
         double total = 0.0;
         for (int r = 0; r < a.R; ++r) total = __dadd_rn(total, event_propensity<MACRO>(a, sp, r));
         if (!(0.0 < total)) {

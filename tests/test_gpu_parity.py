@@ -229,9 +229,9 @@ def test_edge_cases(rb, O):
     assert z.counts.shape == (4, 3, 0)
     # trajectory counts that are not a multiple of the block size, large counts
     big = rb.Network(2)
-    big.add_reaction(rb.Rate.lma(1e-9, [2, 0]), [-2, 1])
+    big.add_reaction(rb.Rate.lma(1e-18, [2, 0]), [-2, 1])
     big.add_reaction(rb.Rate.lma(1e3, [0, 0]), [1, 0])
-    ob = O.OracleNet(2).add_lma(1e-9, [2, 0], [-2, 1]).add_lma(1e3, [0, 0], [1, 0])
+    ob = O.OracleNet(2).add_lma(1e-18, [2, 0], [-2, 1]).add_lma(1e3, [0, 0], [1, 0])
     seeds = _seeds(129, 9)
     res = big.run_ensemble([3_000_000_000, 0], seeds, 0.5, 5)
     ref, ev, _, _ = ob.run_ensemble([3_000_000_000, 0], seeds, 0.5, 5)
