@@ -182,6 +182,7 @@ def test_advance_one_reaction_and_every_event_mode(rb, O):
     dead.add_reaction(rb.Rate.lma(1.0, [1]), [-1])
     times, out = dead.run_all_events([3], 5, 1e9)
     assert np.isinf(times[-1]) and out[-1, 0] == 0 and len(times) == 5
+    rt, ro = O.sir_net().run_all_events([999, 1, 0], 3, 250.0)
     g = rb.api.Gillespie.new_with_seed([999, 1, 0], False, 3)
     g.add_reaction(rb.Rate.lma(1e-4, [1, 1, 0]), [-1, 1, 0])
     g.add_reaction(rb.Rate.lma(0.01, [0, 1, 0]), [0, -1, 1])
