@@ -136,6 +136,32 @@ int rb_ensemble_run_device(const rb_network *net, int64_t n_traj, const int64_t 
                            const int32_t *save_idx, int32_t n_save, int64_t *d_out,
                            uint64_t *d_events, int64_t *d_final_species, void *stream);
 
+/* rb_ensemble_run_device for callers that cannot let a library allocate device
+ * memory -- hosts whose own pool allocator owns all GPU memory, or
+ * latency-critical callers that cannot take cudaMalloc's implicit device
+ * synchronisation.  No counterpart in the reference, which runs on the CPU and
+ * never allocates device memory.
+ *
+ * The call allocates nothing: the engine's own device data (counters, Exp1
+ * tables, packed descriptor, sample times, saved list) goes into one fixed
+ * 64 KiB array compiled into the library, which every GPU that loads the
+ * library keeps until the process exits.  A network and sampling grid that
+ * do not fit return RB_ERR_INVALID with the needed size in the message.
+ * The first call on a device looks up that array's device address (with the
+ * device current); make that first call before any stream capture.  Arguments
+ * are those of rb_ensemble_run_device (device buffers, host save_idx), plus
+ * d_status: NULL or a device pointer to 2 uint64 receiving the run's event
+ * total and its time-budget flag (1 = ran out, results incomplete).  Work is
+ * enqueued on `stream` and the call returns.  All calls share the one array
+ * and each rewrites it, so calls whose work overlaps on the GPU (e.g. on two
+ * streams) race; issue them on one stream or wait between them. */
+int rb_ensemble_run_device_noalloc(const rb_network *net, int64_t n_traj, const int64_t *d_x0,
+                                   int32_t x0_per_traj, const double *d_rates,
+                                   int32_t rates_per_traj, const uint64_t *d_seeds, double tmax,
+                                   int64_t nb_steps, const int32_t *save_idx, int32_t n_save,
+                                   int64_t *d_out, uint64_t *d_events, uint64_t *d_status,
+                                   void *stream);
+
 /* Sum of accepted events of the last rb_ensemble_run_device on this network
  * (synchronises with that run's stream); RB_ERR_TIMEOUT if that run ran out
  * of its time budget. */

@@ -72,6 +72,8 @@ _SIGS = {
                          P(_i64), P(_f64), P(_u64), P(_i64), P(RunStats)], C.c_int),
     "rb_ensemble_run_device": ([_vp, _i64, _vp, _i32, _vp, _i32, _vp, _f64, _i64, P(_i32), _i32, _vp, _vp,
                                 _vp, _vp], C.c_int),
+    "rb_ensemble_run_device_noalloc": ([_vp, _i64, _vp, _i32, _vp, _i32, _vp, _f64, _i64, P(_i32), _i32, _vp,
+                                        _vp, _vp, _vp], C.c_int),
     "rb_ensemble_last_events": ([_vp, P(_u64)], C.c_int),
     "rb_run_all_events": ([_vp, P(_i64), _u64, _f64, P(_i32), _i32, P(_f64), P(_i64), _i64, P(_i64)],
                           C.c_int),

@@ -447,6 +447,19 @@ int rb_ensemble_run_device(const rb_network *netp, int64_t n_traj, const int64_t
     return RB_OK;
 }
 
+int rb_ensemble_run_device_noalloc(const rb_network *netp, int64_t n_traj, const int64_t *d_x0, int32_t x0_per_traj,
+                                   const double *d_rates, int32_t rates_per_traj, const uint64_t *d_seeds,
+                                   double tmax, int64_t nb_steps, const int32_t *save_idx, int32_t n_save,
+                                   int64_t *d_out, uint64_t *d_events, uint64_t *d_status, void *stream) {
+    if (!netp) return fail(RB_ERR_INVALID, "null network");
+    std::lock_guard<std::mutex> lk(netp->net.mu);
+    std::string err;
+    int rc = rbg::noalloc_ensemble_run(netp->net, n_traj, d_x0, x0_per_traj, d_rates, rates_per_traj, d_seeds, tmax,
+                                       nb_steps, save_idx, n_save, d_out, d_events, d_status, stream, err);
+    if (rc == 0) return RB_OK;
+    return fail(rc == 1 ? RB_ERR_INVALID : rc == 5 ? RB_ERR_UNSUPPORTED : RB_ERR_CUDA, err);
+}
+
 int rb_ensemble_last_events(const rb_network *netp, uint64_t *events) {
     if (!netp || !events) return fail(RB_ERR_INVALID, "null argument");
     const rbg::Network &net = netp->net;

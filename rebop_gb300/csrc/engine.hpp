@@ -80,6 +80,14 @@ struct RunDev {
 bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStream_t stream, bool timed,
                     int *mapping);
 
+// Ensemble run whose engine-side device data lives in a fixed array compiled
+// into the library (ssa_thread.cu); returns 0, or 1 (invalid), 2 (CUDA),
+// 5 (unsupported) with `err` set.
+int noalloc_ensemble_run(const Network &net, int64_t n_traj, const int64_t *d_x0, int32_t x0_per_traj,
+                         const double *d_rates, int32_t rates_per_traj, const uint64_t *d_seeds, double tmax,
+                         int64_t nb_steps, const int32_t *save_idx, int32_t n_save, int64_t *d_out,
+                         uint64_t *d_events, uint64_t *d_status, void *stream, std::string &err);
+
 // Per-launch wall-clock budget of the SSA kernels (RB_KERNEL_BUDGET_S, default 120 s).
 int64_t kernel_budget_ns();
 

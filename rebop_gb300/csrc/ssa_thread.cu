@@ -329,3 +329,180 @@ int launch_ssa_events(const EventArgs &a, void *stream) {
 }
 
 }  // namespace rbg
+
+// ---------------------------------------------------------------------------
+// Ensemble run without device allocation.
+//
+// Some hosts cannot let a library call cudaMalloc: an application whose own
+// pool allocator owns all GPU memory and forbids allocations outside it after
+// start-up, or a latency-critical caller that cannot take cudaMalloc's implicit
+// device-wide synchronisation in the middle of its work.  For them the run
+// below keeps everything the engine itself needs on the device -- the counters
+// the kernel updates, the Exp1 tables, the packed reaction descriptor, the
+// sample times and the saved-species list -- in one fixed array compiled into
+// this library, so no device memory is allocated by the call.  The caller
+// still owns and passes every input and output buffer.
+//
+// The array is kNoAllocScratchBytes (64 KiB) per GPU; every GPU that loads
+// the library keeps it until the process exits.  A run whose descriptor,
+// sample grid and saved list do not fit is rejected with RB_ERR_INVALID.
+// All calls share the one array: each call clears the counters and rewrites
+// the rest before its kernel starts, and two calls whose work overlaps on the
+// GPU (for instance on two streams) overwrite each other's data and race.
+// ---------------------------------------------------------------------------
+
+#include <cstring>
+#include <mutex>
+
+#include "engine.hpp"
+#include "network.hpp"
+
+namespace rbg {
+
+constexpr size_t kNoAllocScratchBytes = 64 * 1024;
+constexpr size_t kNoAllocCounterBytes = 256;  // [0] ticket, [1] events, [2] timeout flag
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+std::mutex g_na_mu;
+unsigned char *g_na_dev[kNoAllocMaxDevices];      // device address of the array, per device
+alignas(16) unsigned char g_na_host[kNoAllocScratchBytes];  // host image, built under g_na_mu
+
+size_t na_align(size_t v) { return (v + 15) & ~(size_t)15; }
+
+}  // namespace
+
+int noalloc_ensemble_run(const Network &net, int64_t n_traj, const int64_t *d_x0, int32_t x0_per_traj,
+                         const double *d_rates, int32_t rates_per_traj, const uint64_t *d_seeds, double tmax,
+                         int64_t nb_steps, const int32_t *save_idx, int32_t n_save, int64_t *d_out,
+                         uint64_t *d_events, uint64_t *d_status, void *stream, std::string &err) {
+    const int64_t S = net.n_species, R = (int64_t)net.reactions.size();
+    if (n_traj < 0) return err = "negative number of trajectories", 1;
+    if (nb_steps < 1) return err = "nb_steps must be >= 1", 1;
+    if (nb_steps >= (int64_t)(kNoAllocScratchBytes / 8))
+        return err = "the no-allocation scratch holds " + std::to_string(kNoAllocScratchBytes) +
+                     " bytes, too few for " + std::to_string(nb_steps + 1) + " sample times",
+               1;
+    const int64_t NS = (n_save < 0 || !save_idx) ? S : n_save;
+    for (int64_t k = 0; k < NS && n_save >= 0 && save_idx; k++)
+        if (save_idx[k] < 0 || save_idx[k] >= S) return err = "save index out of range", 1;
+    if (n_traj && S && !d_x0) return err = "null x0", 1;
+    if (n_traj && !d_seeds) return err = "null seeds", 1;
+    if (n_traj && NS && !d_out) return err = "null out", 1;
+    int64_t P = 1, Q = 1;
+    for (const Reaction &r : net.reactions) {
+        P = std::max<int64_t>(P, (int64_t)r.factors.size());
+        Q = std::max<int64_t>(Q, (int64_t)r.jump.size());
+    }
+    // Layout of the array: counters | Exp1 tables | descriptor | sample times | saved list.
+    const size_t o_zig = kNoAllocCounterBytes;
+    const size_t o_rate = na_align(o_zig + sizeof(double) * 2 * kZigTable);
+    const size_t o_jd = na_align(o_rate + 8 * (size_t)std::max<int64_t>(R, 1));
+    const size_t o_fsp = na_align(o_jd + 8 * (size_t)std::max<int64_t>(R * Q, 1));
+    const size_t o_ford = na_align(o_fsp + 4 * (size_t)std::max<int64_t>(R * P, 1));
+    const size_t o_jsp = na_align(o_ford + 4 * (size_t)std::max<int64_t>(R * P, 1));
+    const size_t o_st = na_align(o_jsp + 4 * (size_t)std::max<int64_t>(R * Q, 1));
+    const size_t o_save = na_align(o_st + 8 * (size_t)(nb_steps + 1));
+    const size_t used = na_align(o_save + 4 * (size_t)std::max<int64_t>(NS, 1));
+    if (used > kNoAllocScratchBytes)
+        return err = "the no-allocation scratch holds " + std::to_string(kNoAllocScratchBytes) +
+                     " bytes; this network (" + std::to_string(R) + " reactions) with " +
+                     std::to_string(nb_steps + 1) + " sample times and " + std::to_string(NS) +
+                     " saved species needs " + std::to_string(used),
+               1;
+
+    int dev = 0, sms = 0, smem_optin = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) return err = std::string("cudaGetDevice: ") + cudaGetErrorString(ce), 2;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return err = "device ordinal out of range", 1;
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_dev[dev]) {
+        // Once per device, with that device current: the host-side name of
+        // the array is not a device address; ask the runtime for it.
+        void *p = nullptr;
+        ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (ce != cudaSuccess) return err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(ce), 2;
+        g_na_dev[dev] = static_cast<unsigned char *>(p);
+    }
+    unsigned char *dbase = g_na_dev[dev];
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+
+    unsigned char *h = g_na_host;
+    zig_tables_host(reinterpret_cast<double *>(h + o_zig), reinterpret_cast<double *>(h + o_zig) + kZigTable);
+    double *rate = reinterpret_cast<double *>(h + o_rate);
+    int64_t *jd = reinterpret_cast<int64_t *>(h + o_jd);
+    int32_t *fsp = reinterpret_cast<int32_t *>(h + o_fsp), *ford = reinterpret_cast<int32_t *>(h + o_ford);
+    int32_t *jsp = reinterpret_cast<int32_t *>(h + o_jsp);
+    std::memset(h + o_rate, 0, o_st - o_rate);
+    int32_t max_order = 0;
+    for (int64_t i = 0; i < R; i++) {
+        const Reaction &r = net.reactions[i];
+        rate[i] = r.rate;
+        for (size_t k = 0; k < r.factors.size(); k++) {
+            fsp[i * P + k] = r.factors[k].species;
+            ford[i * P + k] = r.factors[k].order;
+            max_order = std::max(max_order, r.factors[k].order);
+        }
+        for (size_t k = 0; k < r.jump.size(); k++) {
+            jsp[i * Q + k] = r.jump[k].species;
+            jd[i * Q + k] = r.jump[k].delta;
+        }
+    }
+    double *st = reinterpret_cast<double *>(h + o_st);
+    for (int64_t i = 0; i <= nb_steps; i++) st[i] = tmax * (double)i / (double)nb_steps;
+    int32_t *sv = reinterpret_cast<int32_t *>(h + o_save);
+    for (int64_t k = 0; k < NS; k++) sv[k] = (n_save < 0 || !save_idx) ? (int32_t)k : save_idx[k];
+
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ce = cudaMemsetAsync(dbase, 0, kNoAllocCounterBytes, s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(dbase + o_zig, h + o_zig, used - o_zig, cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) return err = std::string("staging copy: ") + cudaGetErrorString(ce), 2;
+
+    SsaArgs a{};
+    a.S = (int32_t)S;
+    a.R = (int32_t)R;
+    a.P = (int32_t)P;
+    a.Q = (int32_t)Q;
+    a.macro_mode = net.macro_mode ? 1 : 0;
+    a.rate = d_rates ? d_rates : reinterpret_cast<const double *>(dbase + o_rate);
+    a.rate_stride = d_rates && rates_per_traj ? R : 0;
+    a.fac_sp = reinterpret_cast<const int32_t *>(dbase + o_fsp);
+    a.fac_ord = reinterpret_cast<const int32_t *>(dbase + o_ford);
+    a.jmp_sp = reinterpret_cast<const int32_t *>(dbase + o_jsp);
+    a.jmp_d = reinterpret_cast<const int64_t *>(dbase + o_jd);
+    a.n_traj = n_traj;
+    a.x0 = d_x0;
+    a.x0_stride = x0_per_traj ? S : 0;
+    a.seeds = d_seeds;
+    a.sample_t = reinterpret_cast<const double *>(dbase + o_st);
+    a.n_samples = nb_steps + 1;
+    a.save_idx = reinterpret_cast<const int32_t *>(dbase + o_save);
+    a.n_save = (int32_t)NS;
+    a.out = d_out;
+    a.events = d_events;
+    a.work = reinterpret_cast<unsigned long long *>(dbase);
+    a.zig = reinterpret_cast<const double *>(dbase + o_zig);
+    a.budget_ns = kernel_budget_ns();
+    (void)max_order;
+    if (n_traj > 0) {
+        const int block = ssa_thread_max_block(a, (size_t)smem_optin);
+        if (block == 0) return err = "network too large for the thread-per-trajectory kernel", 5;
+        const size_t smem = ssa_thread_smem(a, block);
+        int per_sm = std::max(1, ssa_thread_occupancy(a, block, smem));
+        const int64_t want = (n_traj + block - 1) / block;
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * per_sm));
+        int le = launch_ssa_thread(a, block, grid, smem, stream);
+        if (le != 0) return err = std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)le), 2;
+    }
+    if (d_status) {
+        ce = cudaMemcpyAsync(d_status, dbase + 8, 16, cudaMemcpyDeviceToDevice, s);
+        if (ce != cudaSuccess) return err = std::string("status copy: ") + cudaGetErrorString(ce), 2;
+    }
+    return 0;
+}
+
+}  // namespace rbg
