@@ -32,6 +32,25 @@ void zig_tables_host(double *x, double *f) {
     for (int i = 0; i < kZigTable; i++) f[i] = std::exp(-x[i]);
 }
 
+// Fast-path companions of the tables.  Layer i draws u = (2k+1) 2^-53 from a
+// 52-bit k and accepts x = RN(u * x[i]) when x < x[i+1].  RN(u * x[i]) is
+// non-decreasing in k, so the accepted k form a prefix [0, K_i): K_i replaces
+// the comparison with an integer one.  d[i] = RN(f[i] - f[i+1]) is the
+// wedge test's difference, computed once here exactly as the draw would.
+void zig_fast_tables_host(const double *x, const double *f, uint64_t *K, double *d) {
+    for (int i = 0; i < kZigLayers; i++) {
+        uint64_t lo = 0, hi = 1ull << 52;  // first k in [lo, hi] with !(x < x[i+1])
+        while (lo < hi) {
+            const uint64_t mid = lo + (hi - lo) / 2;
+            const double u = (double)(2 * mid + 1) * 0x1p-53;
+            if (u * x[i] < x[i + 1]) lo = mid + 1;
+            else hi = mid;
+        }
+        K[i] = lo;
+        d[i] = f[i] - f[i + 1];
+    }
+}
+
 static std::mutex g_ctx_mu;
 static std::map<int, DeviceCtx *> g_ctx;
 
@@ -55,10 +74,12 @@ DeviceCtx *device_ctx() {
     }
     c->sm_count = prop.multiProcessorCount;
     c->smem_optin = prop.sharedMemPerBlockOptin;
-    std::vector<double> tab(2 * kZigTable);
-    zig_tables_host(tab.data(), tab.data() + kZigTable);
-    if (!cuda_ok(cudaMalloc(&c->zig, sizeof(double) * 2 * kZigTable), "cudaMalloc(zig)") ||
-        !cuda_ok(cudaMemcpy(c->zig, tab.data(), sizeof(double) * 2 * kZigTable, cudaMemcpyHostToDevice),
+    std::vector<double> tab(kZigWords);
+    zig_tables_host(tab.data(), tab.data() + kZigOffF);
+    zig_fast_tables_host(tab.data(), tab.data() + kZigOffF, reinterpret_cast<uint64_t *>(tab.data() + kZigOffK),
+                         tab.data() + kZigOffD);
+    if (!cuda_ok(cudaMalloc(&c->zig, sizeof(double) * kZigWords), "cudaMalloc(zig)") ||
+        !cuda_ok(cudaMemcpy(c->zig, tab.data(), sizeof(double) * kZigWords, cudaMemcpyHostToDevice),
                  "cudaMemcpy(zig)")) {
         delete c;
         return nullptr;
@@ -196,23 +217,41 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     if (!cuda_ok(cudaMemsetAsync(dn.scratch, 0, 4 * sizeof(unsigned long long), stream), "cudaMemsetAsync"))
         return false;
     if (r.n_traj == 0) return true;
-    int block = ssa_thread_max_block(a, ctx->smem_optin);
-    if (block == 0) {
-        set_error("network too large for the thread-per-trajectory kernel (" + std::to_string(p.S) +
-                  " species, " + std::to_string(p.R) + " reactions)");
+    // Kernel choice: the lockstep integer-binary64 kernel when it applies
+    // (RB_SSA_KERNEL=generic|fast overrides), else the generic kernel.
+    const char *pref = std::getenv("RB_SSA_KERNEL");
+    const bool want_generic = pref && std::strcmp(pref, "generic") == 0;
+    const bool fast = !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
+                      ssa_fast_smem(a, 128) <= ctx->smem_optin;
+    if (pref && std::strcmp(pref, "fast") == 0 && !fast) {
+        set_error("RB_SSA_KERNEL=fast but the fast kernel does not cover this network or sample grid");
         return false;
     }
-    size_t smem = ssa_thread_smem(a, block);
-    int per_sm = ssa_thread_occupancy(a, block, smem);
+    int block, per_sm;
+    size_t smem;
+    if (fast) {
+        block = 128;
+        smem = ssa_fast_smem(a, block);
+        per_sm = ssa_fast_occupancy(a, block, smem);
+    } else {
+        block = ssa_thread_max_block(a, ctx->smem_optin);
+        if (block == 0) {
+            set_error("network too large for the thread-per-trajectory kernel (" + std::to_string(p.S) +
+                      " species, " + std::to_string(p.R) + " reactions)");
+            return false;
+        }
+        smem = ssa_thread_smem(a, block);
+        per_sm = ssa_thread_occupancy(a, block, smem);
+    }
     if (per_sm < 1) per_sm = 1;
     int64_t want = (r.n_traj + block - 1) / block;
     int64_t cap = (int64_t)ctx->sm_count * per_sm;
     int grid = (int)std::max<int64_t>(1, std::min(want, cap));
     if (timed && !cuda_ok(cudaEventRecord(dn.ev_start, stream), "cudaEventRecord")) return false;
-    int err = launch_ssa_thread(a, block, grid, smem, stream);
-    if (err != 0) return cuda_ok((cudaError_t)err, "ssa_thread_kernel launch");
+    int err = fast ? launch_ssa_fast(a, block, grid, smem, stream) : launch_ssa_thread(a, block, grid, smem, stream);
+    if (err != 0) return cuda_ok((cudaError_t)err, fast ? "ssa_fast_kernel launch" : "ssa_thread_kernel launch");
     if (timed && !cuda_ok(cudaEventRecord(dn.ev_stop, stream), "cudaEventRecord")) return false;
-    if (mapping) *mapping = 0;
+    if (mapping) *mapping = fast ? 2 : 0;
     return true;
 }
 

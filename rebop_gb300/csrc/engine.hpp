@@ -27,6 +27,8 @@ struct DeviceCtx {
 DeviceCtx *device_ctx();
 // Host copy of the Exp1 ziggurat tables (x[257], f[257]).
 void zig_tables_host(double *x, double *f);
+// Acceptance thresholds K[256] and wedge differences d[256] of those tables.
+void zig_fast_tables_host(const double *x, const double *f, uint64_t *K, double *d);
 
 // Device copy of one network's packed descriptor, its scratch words and the
 // staging buffers of host-pointer calls.
@@ -73,6 +75,7 @@ struct RunDev {
     double *fin_t = nullptr;
     uint64_t *fin_rng = nullptr;
     uint64_t *events = nullptr;
+    bool times_ok = false;  // every sample time finite and >= 0 (lets the fast kernel run)
 };
 
 // Enqueue the sampled-run kernel on `stream` (scratch reset included).

@@ -8,6 +8,13 @@ namespace rbg {
 
 constexpr int kZigLayers = 256;            // ziggurat layers of the Exp1 sampler
 constexpr int kZigTable = kZigLayers + 1;  // abscissae x[0..256] / f(x) values
+// Device table layout (doubles / u64 words): x[257] | f[257] | k[256] | d[256]
+// where k[i] is the number of 52-bit fractions u accepted without the wedge
+// test in layer i and d[i] = f[i] - f[i+1] (see zig_fast_tables_host).
+constexpr int kZigOffF = kZigTable;
+constexpr int kZigOffK = 2 * kZigTable;
+constexpr int kZigOffD = 2 * kZigTable + kZigLayers;
+constexpr int kZigWords = 2 * kZigTable + 2 * kZigLayers;
 
 struct SsaArgs {
     // packed network (see network.hpp: Packed)
@@ -60,6 +67,13 @@ int launch_ssa_thread(const SsaArgs &a, int block, int grid, size_t smem, void *
 size_t ssa_thread_smem(const SsaArgs &a, int block);
 int ssa_thread_max_block(const SsaArgs &a, size_t smem_limit);
 int ssa_thread_occupancy(const SsaArgs &a, int block, size_t smem);
+
+// Lockstep kernel with integer binary64 (ssa_fast.cu): networks with at most
+// 32 reactions, reactant orders below 2^15 and finite non-negative sample times.
+bool ssa_fast_supported(const SsaArgs &a, int max_order);
+size_t ssa_fast_smem(const SsaArgs &a, int block);
+int ssa_fast_occupancy(const SsaArgs &a, int block, size_t smem);
+int launch_ssa_fast(const SsaArgs &a, int block, int grid, size_t smem, void *stream);
 
 // Every-event runs (src/pyo3_gillespie.rs:209-223) and single
 // _advance_one_reaction steps (src/gillespie.rs:269-297): one thread per

@@ -258,3 +258,79 @@ def test_device_entry_point_matches_host_entry_point(rb, O):
     np.testing.assert_array_equal(d_out.cpu().numpy(), ref)
     np.testing.assert_array_equal(d_ev.cpu().numpy().view(np.uint64), ev)
     assert total == tot
+
+
+def _with_kernel(kind, fn):
+    import os
+
+    old = os.environ.get("RB_SSA_KERNEL")
+    os.environ["RB_SSA_KERNEL"] = kind
+    try:
+        return fn()
+    finally:
+        if old is None:
+            del os.environ["RB_SSA_KERNEL"]
+        else:
+            os.environ["RB_SSA_KERNEL"] = old
+
+
+def test_fast_and_generic_kernels_match_oracle(rb, O):
+    # The lockstep integer-binary64 kernel and the generic kernel against the oracle.
+    cases = []
+    cases.append((_dimer(rb), O.dimer_net(), [1, 0, 0, 0], 0.5, 25, None))
+    cases.append((_sir(rb), O.sir_net(), [999, 1, 0], 250.0, 50, None))
+    n = 300
+    rng = np.random.default_rng(11)
+    rates = np.stack([10 ** rng.uniform(-5, -3, n), 10 ** rng.uniform(-3, -1, n)], axis=1)
+    cases.append((_sir(rb), O.sir_net(), [999, 1, 0], 100.0, 20, rates))
+    for net, onet, x0, tmax, nb, r in cases:
+        seeds = _seeds(n, 21)
+        fast = _with_kernel("fast", lambda: net.run_ensemble(x0, seeds, tmax, nb, rates=r))
+        gen = _with_kernel("generic", lambda: net.run_ensemble(x0, seeds, tmax, nb, rates=r))
+        ref, ev, _, _ = onet.run_ensemble(x0, seeds, tmax, nb, rates=r)
+        assert fast.stats["mapping"] == 2 and gen.stats["mapping"] == 0
+        np.testing.assert_array_equal(fast.counts, ref)
+        np.testing.assert_array_equal(gen.counts, ref)
+        np.testing.assert_array_equal(fast.events, ev)
+
+
+def test_fast_kernel_native_fallback_paths(rb, O):
+    # Steps outside the integer emulation's domain are redone in native binary64.
+    seeds = _seeds(200, 31)
+    # NaN / negative rate constants for some trajectories (per-trajectory rates)
+    rates = np.tile([1e-4, 0.01], (200, 1))
+    rates[::7, 1] = np.nan
+    rates[::11, 0] = -1e-4
+    net, onet = _sir(rb), O.sir_net()
+    fast = _with_kernel("fast", lambda: net.run_ensemble([999, 1, 0], seeds, 100.0, 10, rates=rates))
+    ref, ev, _, _ = onet.run_ensemble([999, 1, 0], seeds, 100.0, 10, rates=rates)
+    np.testing.assert_array_equal(fast.counts, ref)
+    np.testing.assert_array_equal(fast.events, ev)
+    # counts that go negative: A is consumed at a rate set by B, and A is a reactant too
+    net = rb.Network(2)
+    net.add_reaction(rb.Rate.lma(1.0, [0, 1]), [-1, 0])
+    net.add_reaction(rb.Rate.lma(0.5, [1, 0]), [0, 1])
+    onet = O.OracleNet(2).add_lma(1.0, [0, 1], [-1, 0]).add_lma(0.5, [1, 0], [0, 1])
+    fast = _with_kernel("fast", lambda: net.run_ensemble([3, 5], seeds, 3.0, 6))
+    ref, ev, _, _ = onet.run_ensemble([3, 5], seeds, 3.0, 6)
+    np.testing.assert_array_equal(fast.counts, ref)
+    np.testing.assert_array_equal(fast.events, ev)
+    # counts at and beyond 2^53 (the reference's `as f64` rounds them)
+    net = rb.Network(2)
+    net.add_reaction(rb.Rate.lma(1e-16, [1, 0]), [-1, 1])
+    onet = O.OracleNet(2).add_lma(1e-16, [1, 0], [-1, 1])
+    x0 = [2 ** 53 + 7, 0]
+    fast = _with_kernel("fast", lambda: net.run_ensemble(x0, seeds[:50], 0.02, 4))
+    ref, ev, _, _ = onet.run_ensemble(x0, seeds[:50], 0.02, 4)
+    np.testing.assert_array_equal(fast.counts, ref)
+    np.testing.assert_array_equal(fast.events, ev)
+    # macro arithmetic through the fast kernel
+    D = rb.define_system(DIMER_DSL)
+    d = D.with_parameters(25.0, 1000.0, 0.001, 0.1, 1.0)
+    d.gene = 1
+    res = _with_kernel("fast", lambda: d.run_ensemble(seeds, 0.3, 5))
+    o = (O.OracleNet(4, macro=True).add_macro(25.0, [(0, 1)], [0, 1, 0, 0])
+         .add_macro(1000.0, [(1, 1)], [0, 0, 1, 0]).add_macro(0.001, [(2, 2)], [0, 0, -2, 1])
+         .add_macro(0.1, [(1, 1)], [0, -1, 0, 0]).add_macro(1.0, [(2, 1)], [0, 0, -1, 0]))
+    ref, ev, _, _ = o.run_ensemble([1, 0, 0, 0], seeds, 0.3, 5)
+    np.testing.assert_array_equal(res.counts, ref)
