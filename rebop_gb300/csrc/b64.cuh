@@ -93,6 +93,75 @@ B64_HD uint64_t mul_int(uint64_t a, uint64_t n, int down, bool &bad) {
     return pack(ea + 75 - s - down, m, bad);
 }
 
+// Branch-free forms for the kernels' hot loop (no data-dependent branches, so
+// the lanes of a warp stay converged; 32-bit limbs where the operands allow).
+
+// RN(a * n) for a non-negative double a (normal or +0) and 0 <= n < 2^32.
+// The 85-bit product is formed from two 32x32 -> 64 multiplies.
+B64_HD uint64_t mul_u32(uint64_t a, uint32_t n, bool &bad) {
+    const int ea = (int)(a >> 52);
+    const uint32_t ml = (uint32_t)a, mh = ((uint32_t)(a >> 32) & 0xFFFFFu) | 0x100000u;
+    const uint64_t lo = (uint64_t)ml * n;
+    const uint64_t hi = (uint64_t)mh * n + (lo >> 32);  // product = hi * 2^32 + (uint32)lo
+    const uint32_t w0 = (uint32_t)lo;
+    const int z = clz64(hi | 1);                        // in [10, 43] when n > 0
+    const uint64_t top = z < 32 ? (hi << z) | ((uint64_t)w0 >> (32 - z)) : (hi << z) | ((uint64_t)w0 << (z - 32));
+    const uint32_t rest = z < 32 ? (w0 << z) : 0u;
+    uint64_t m = top >> 11;
+    m += ((top >> 10) & (((top & 0x3FF) | rest) != 0 || (m & 1))) ? 1 : 0;
+    const int E = ea + 43 - z;
+    const bool zero = (a == 0) | (n == 0);
+    bad |= !zero && (ea == 0 || ea >= 2047 || E < 1 || E + (int)(m >> 53) > 2046);
+    return zero ? 0 : ((uint64_t)(E - 1) << 52) + m;
+}
+
+// RN(a * n * 2^-down) for a non-negative double a (normal or +0) and
+// 0 <= n < 2^63; branch-free 128-bit normalisation.
+B64_HD uint64_t mul_u64(uint64_t a, uint64_t n, int down, bool &bad) {
+    const int ea = (int)(a >> 52);
+    uint64_t hi, lo;
+    mul64((a & kMant) | kHidden, n, hi, lo);
+    const bool big = hi != 0;
+    const int s = big ? clz64(hi) : 64 + clz64(lo | 1);
+    const int sl = s & 63;
+    const uint64_t H = big ? (sl ? (hi << sl) | (lo >> (64 - sl)) : hi) : (lo << sl);
+    const uint64_t L = big ? (lo << sl) : 0;
+    uint64_t m = H >> 11;
+    const uint64_t rest = H & 0x7FF;
+    m += ((rest >> 10) & ((rest & 0x3FF) != 0 || L != 0 || (m & 1))) ? 1 : 0;
+    const int E = ea + 75 - s - down;
+    const bool zero = (a == 0) | (n == 0);
+    bad |= !zero && (ea == 0 || ea >= 2047 || E < 1 || E + (int)(m >> 53) > 2046);
+    return zero ? 0 : ((uint64_t)(E - 1) << 52) + m;
+}
+
+// RN(a + b) for non-negative doubles a, b (normal or +0), branch-free.
+B64_HD uint64_t add_bf(uint64_t a, uint64_t b, bool &bad) {
+    const uint64_t x = a > b ? a : b, y = a > b ? b : a;  // x >= y
+    const int ex = (int)(x >> 52), ey = (int)(y >> 52);
+    const uint64_t A = ((x & kMant) | kHidden) << 10;
+    const uint64_t B = ((y & kMant) | kHidden) << 10;
+    const int d = ex - ey;
+    const int dd = d < 63 ? d : 63;
+    const uint64_t Bs = B >> dd;
+    uint64_t sticky = (B & ((1ull << dd) - 1)) != 0;
+    uint64_t S = A + Bs;
+    const uint64_t carry = S >> 63;
+    sticky |= S & carry;
+    S >>= carry;
+    uint64_t m = S >> 10;
+    const uint64_t r = S & 0x3FF;
+    m += (r > 0x200 || (r == 0x200 && (sticky || (m & 1)))) ? 1 : 0;
+    const int E = ex + (int)carry;
+    const bool trivial = y == 0;  // x + 0 = x (also covers 0 + 0)
+    bad |= !trivial && (ey == 0 || ex >= 2047 || E + (int)(m >> 53) > 2046);
+    return trivial ? x : ((uint64_t)(E - 1) << 52) + m;
+}
+
+// RN(a / b) for a >= 0 (normal or +0) and b > 0 normal, branch-free; same
+// radix-2^11 long division as div() below.
+B64_HD uint64_t div_bf(uint64_t a, uint64_t b, bool &bad);
+
 // RN(a + b) for non-negative doubles a, b (normal or +0).
 B64_HD uint64_t add(uint64_t a, uint64_t b, bool &bad) {
     if (a == 0) return b;
@@ -223,6 +292,36 @@ B64_HD uint64_t div(uint64_t a, uint64_t b, bool &bad) {
     const bool sticky = (g & (half - 1)) != 0 || R != 0;
     m += ((g & half) && (sticky || (m & 1))) ? 1 : 0;
     return pack(E, m, bad);
+}
+
+// Branch-free RN(a / b); see the declaration above.
+B64_HD uint64_t div_bf(uint64_t a, uint64_t b, bool &bad) {
+    const int ea = (int)(a >> 52), eb = (int)(b >> 52);
+    const uint64_t ma = (a & kMant) | kHidden, mb = (b & kMant) | kHidden;
+    const uint32_t inv = recip_estimate(mb);
+    const uint32_t mb_lo = (uint32_t)mb, mb_hi = (uint32_t)(mb >> 32);
+    uint64_t R = ma, Q = 0;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int j = 0; j < 5; ++j) {
+        R <<= 11;
+        const uint32_t q = (uint32_t)(((R >> 32) * (uint64_t)inv) >> 51);
+        R -= (uint64_t)mb_lo * q + ((uint64_t)(mb_hi * q) << 32);
+        const uint32_t c = R >= mb ? 1u : 0u;
+        R -= c ? mb : 0;
+        Q = (Q << 11) | (q + c);
+    }
+    const uint64_t top = Q >> 55;  // 1 when ma >= mb
+    const uint64_t m0 = Q >> (2 + top);
+    const uint64_t g = Q & ((4ull << top) - 1);
+    const uint64_t half = 2ull << top;
+    const bool sticky = (g & (half - 1)) != 0 || R != 0;
+    const uint64_t m = m0 + (((g & half) != 0 && (sticky || (m0 & 1))) ? 1 : 0);
+    const int E = ea - eb + 1022 + (int)top;
+    const bool zero = a == 0;
+    bad |= !zero && (ea == 0 || ea >= 2047 || eb == 0 || eb >= 2047 || E < 1 || E + (int)(m >> 53) > 2046);
+    return zero ? 0 : ((uint64_t)(E - 1) << 52) + m;
 }
 
 }  // namespace b64

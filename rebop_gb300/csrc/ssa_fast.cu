@@ -23,6 +23,9 @@
 //   and redone with native binary64 instructions from the committed state.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+#include <cstring>
+
 #include "b64.cuh"
 #include "rng.cuh"
 #include "ssa_args.hpp"
@@ -88,7 +91,7 @@ __device__ __forceinline__ uint64_t exp1_emul(Xoshiro &g, const FastSmem &m, boo
         const int i = (int)(b & 0xff);
         const uint64_t k = b >> 12;
         const ulonglong2 e = m.zxk[i];
-        const uint64_t x = b64::mul_int(e.x, 2 * k + 1, 53, bad);
+        const uint64_t x = b64::mul_u64(e.x, 2 * k + 1, 53, bad);
         if (k < e.y) return x;
         if (i == 0) {  // tail: R - ln U in binary64
             const double u = xo_uniform(g);
@@ -96,7 +99,7 @@ __device__ __forceinline__ uint64_t exp1_emul(Xoshiro &g, const FastSmem &m, boo
         }
         // wedge: f[i+1] + (f[i] - f[i+1]) U < exp(-x), with f[i] < f[i+1]
         const uint64_t mu = xo_next(g) >> 11;
-        const uint64_t w = b64::sub(m.zf[i + 1], b64::mul_int(m.zd[i], mu, 53, bad), bad);
+        const uint64_t w = b64::sub(m.zf[i + 1], b64::mul_u64(m.zd[i], mu, 53, bad), bad);
         const float wf = f32_rz(w), ef = expf(-f32_rz(x));
         // |wf - w| and |ef - exp(-x)| are below 1.5e-6 relative; the margin is 7.6e-6.
         bool accept;
@@ -159,8 +162,17 @@ __device__ __noinline__ bool native_step(const SsaArgs &a, Xoshiro &g, const int
 
 }  // namespace
 
-template <int MAXR, bool MACRO>
-__global__ void __launch_bounds__(128) ssa_fast_kernel(const __grid_constant__ SsaArgs a) {
+// Exact binary64 a + b of the hot loop: on the FP64 pipe (ADD_NATIVE), or on
+// the integer pipes.  Either way the bits are the FPU's.
+template <bool ADD_NATIVE>
+__device__ __forceinline__ uint64_t hot_add(uint64_t a, uint64_t b, bool &bad) {
+    if (ADD_NATIVE) return (uint64_t)__double_as_longlong(__dadd_rn(__longlong_as_double((long long)a),
+                                                                     __longlong_as_double((long long)b)));
+    return b64::add_bf(a, b, bad);
+}
+
+template <int MAXR, bool MACRO, bool ADD_NATIVE>
+__global__ void __launch_bounds__(128, 6) ssa_fast_kernel(const __grid_constant__ SsaArgs a) {
     const int BD = blockDim.x, tid = threadIdx.x;
     const int S = a.S, R = a.R, P = a.P, Q = a.Q;
     const FastSmem m = fast_layout(S, R, P, Q, BD);
@@ -183,45 +195,43 @@ __global__ void __launch_bounds__(128) ssa_fast_kernel(const __grid_constant__ S
     const int64_t t_start = global_ns();
     unsigned int tick = 0;
     unsigned long long lane_events = 0;
-    bool out_of_time = false;
 
-    Xoshiro g;
+    Xoshiro g{0, 0, 0, 0};
     uint64_t t = 0, T = 0;
-    long long i = 0, traj;
+    long long i = 0, traj = -1;
     unsigned long long ev = 0;
     bool nat = false;
 
-    auto start = [&](long long j) {
-        if (a.in_species) {
-            for (int s = 0; s < S; ++s) sp[s * BD] = a.in_species[j * S + s];
-            t = (uint64_t)__double_as_longlong(a.in_t[j]);
-            g.s0 = a.in_rng[j * 4 + 0];
-            g.s1 = a.in_rng[j * 4 + 1];
-            g.s2 = a.in_rng[j * 4 + 2];
-            g.s3 = a.in_rng[j * 4 + 3];
-        } else {
-            for (int s = 0; s < S; ++s) sp[s * BD] = a.x0[j * a.x0_stride + s];
-            t = 0;
-            xo_seed(g, a.seeds[j]);
+    for (;;) {
+        if (traj < 0) {
+            // ---- take the next trajectory (fresh, or resumed from a state)
+            traj = (long long)atomicAdd(a.work, 1ull);
+            if (traj >= a.n_traj) break;
+            if (a.in_species) {
+                for (int s = 0; s < S; ++s) sp[s * BD] = a.in_species[traj * S + s];
+                t = (uint64_t)__double_as_longlong(a.in_t[traj]);
+                g.s0 = a.in_rng[traj * 4 + 0];
+                g.s1 = a.in_rng[traj * 4 + 1];
+                g.s2 = a.in_rng[traj * 4 + 2];
+                g.s3 = a.in_rng[traj * 4 + 3];
+            } else {
+                for (int s = 0; s < S; ++s) sp[s * BD] = a.x0[traj * a.x0_stride + s];
+                t = 0;
+                xo_seed(g, a.seeds[traj]);
+            }
+            nat = !emul_domain(t);
+            for (int r = 0; r < R; ++r) {
+                const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[traj * a.rate_stride + r]);
+                rl[r * BD] = rb;
+                nat |= !emul_domain(rb);
+            }
+            i = 0;
+            ev = 0;
+            T = (uint64_t)__double_as_longlong(a.sample_t[0]);
         }
-        nat = !emul_domain(t);
-        for (int r = 0; r < R; ++r) {
-            const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[j * a.rate_stride + r]);
-            rl[r * BD] = rb;
-            nat |= !emul_domain(rb);
-        }
-        i = 0;
-        ev = 0;
-        T = (uint64_t)__double_as_longlong(a.sample_t[0]);
-    };
-
-    traj = (long long)atomicAdd(a.work, 1ull);
-    bool active = traj < a.n_traj;
-    if (active) start(traj);
-
-    while (active) {
         if ((++tick & 1023u) == 0 && global_ns() - t_start > a.budget_ns) {
-            out_of_time = true;
+            lane_events += ev;
+            atomicExch(a.work + 2, 1ull);
             break;
         }
         // ---- propensities and their running sum
@@ -240,30 +250,32 @@ __global__ void __launch_bounds__(128) ssa_fast_kernel(const __grid_constant__ S
                     if (MACRO) {
                         int64_t ff = n;
                         for (int j = 1; j < o; ++j) ff *= n - j;
-                        bad |= (uint64_t)ff >= kLimit53;
-                        acc = b64::mul_int(acc, (uint64_t)ff, 0, bad);
+                        bad |= (uint64_t)ff >= 0x100000000ull;
+                        acc = b64::mul_u32(acc, (uint32_t)ff, bad);
                     } else {
                         for (int j = o - 1; j >= 0; --j) {
                             const int64_t x = n - j;
-                            bad |= (uint64_t)x >= kLimit53;
-                            acc = b64::mul_int(acc, (uint64_t)x, 0, bad);
+                            bad |= (uint64_t)x >= 0x100000000ull;
+                            acc = b64::mul_u32(acc, (uint32_t)x, bad);
                         }
                     }
                 }
-                tot = b64::add(tot, acc, bad);
+                tot = hot_add<ADD_NATIVE>(tot, acc, bad);
                 cum[r] = tot;
             }
         }
+        bad |= !emul_domain(tot);
         // ---- Exp1 draw, candidate clock, choice (on copies of the generator)
         const bool pos = tot != 0;
         Xoshiro g2 = g;
         bool bad_t = false, bad_c = false;
         const uint64_t x = exp1_emul(g2, m, bad_t);
-        const uint64_t q = b64::div(x, pos ? tot : kOneBits, bad_t);
-        uint64_t tn = b64::add(t, q, bad_t);
+        const uint64_t q = b64::div_bf(x, pos ? tot : kOneBits, bad_t);
+        uint64_t tn = hot_add<ADD_NATIVE>(t, q, bad_t);
+        bad_t |= !emul_domain(tn);
         bool fire = pos && tn <= T;
         Xoshiro g3 = g2;
-        const uint64_t chosen = b64::mul_int(tot, xo_next(g3) >> 11, 53, bad_c);
+        const uint64_t chosen = b64::mul_u64(tot, xo_next(g3) >> 11, 53, bad_c);
         int idx;
         if (MACRO) {
             idx = R;
@@ -279,10 +291,8 @@ __global__ void __launch_bounds__(128) ssa_fast_kernel(const __grid_constant__ S
         bad = bad || (pos && bad_t) || (fire && bad_c);
         if (bad) {
             fire = native_step<MAXR, MACRO>(a, g, sp, rl, BD, t, T, idx, tn, m);
-        } else if (fire) {
-            g = g3;
-        } else if (pos) {
-            g = g2;
+        } else {
+            g = fire ? g3 : (pos ? g2 : g);
         }
         // ---- fire the reaction, or record the sample and move to the next
         if (fire) {
@@ -308,15 +318,9 @@ __global__ void __launch_bounds__(128) ssa_fast_kernel(const __grid_constant__ S
                 }
                 if (a.events) a.events[traj] = ev;
                 lane_events += ev;
-                traj = (long long)atomicAdd(a.work, 1ull);
-                active = traj < a.n_traj;
-                if (active) start(traj);
+                traj = -1;
             }
         }
-    }
-    if (out_of_time) {
-        lane_events += ev;
-        atomicExch(a.work + 2, 1ull);
     }
     for (int off = 16; off > 0; off >>= 1) lane_events += __shfl_down_sync(0xffffffffu, lane_events, off);
     if ((tid & 31) == 0 && lane_events) atomicAdd(a.work + 1, lane_events);
@@ -326,20 +330,34 @@ __global__ void __launch_bounds__(128) ssa_fast_kernel(const __grid_constant__ S
 
 namespace {
 
+// Placement of the hot loop's binary64 adds: the FP64 pipe (default) or the
+// integer pipes (RB_FAST_ADD=int); both give the same bits.
+bool add_native() {
+    const char *v = std::getenv("RB_FAST_ADD");
+    return !(v && std::strcmp(v, "int") == 0);
+}
+
+template <int MAXR, bool MACRO, bool ADDN>
+int fast_launch_v(const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st) {
+    auto kern = ssa_fast_kernel<MAXR, MACRO, ADDN>;
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return (int)err;
+    kern<<<grid, block, smem, st>>>(a);
+    return (int)cudaGetLastError();
+}
+
 template <int MAXR, bool MACRO>
 int fast_launch(const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st) {
-    cudaError_t err = cudaFuncSetAttribute(ssa_fast_kernel<MAXR, MACRO>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return (int)err;
-    ssa_fast_kernel<MAXR, MACRO><<<grid, block, smem, st>>>(a);
-    return (int)cudaGetLastError();
+    return add_native() ? fast_launch_v<MAXR, MACRO, true>(a, block, grid, smem, st)
+                        : fast_launch_v<MAXR, MACRO, false>(a, block, grid, smem, st);
 }
 
 template <int MAXR, bool MACRO>
 int fast_occupancy(int block, size_t smem) {
     int n = 0;
-    cudaFuncSetAttribute(ssa_fast_kernel<MAXR, MACRO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_fast_kernel<MAXR, MACRO>, block, smem);
+    auto kern = add_native() ? ssa_fast_kernel<MAXR, MACRO, true> : ssa_fast_kernel<MAXR, MACRO, false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, block, smem);
     return n;
 }
 

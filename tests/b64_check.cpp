@@ -90,6 +90,35 @@ int main(int argc, char **argv) {
     }
     std::printf("mul_int %ld %ld %ld\n", N, fail, bad);
 
+    // mul_u32 (counts) and mul_u64 (53-bit integers, optional 2^-53 scale), branch-free
+    long f32 = 0, b32 = 0, f64 = 0, b64c = 0;
+    for (long i = 0; i < N; i++) {
+        const uint64_t a = (i % 17 == 0) ? 0 : rnd_double(i % 5 == 0 ? 1 : 600, i % 7 == 0 ? 2046 : 1400);
+        const uint32_t n32 = (uint32_t)(rnd_int() & 0xFFFFFFFFull);
+        bool b = false;
+        uint64_t got = mul_u32(a, n32, b);
+        double ref = dbl(a) * (double)n32;
+        if (b) {
+            b32++;
+            if (!refusal_ok(ref)) f32++;
+        } else if (got != bits(ref)) {
+            f32++;
+        }
+        const uint64_t n = rnd_int() & ((1ull << 53) - 1);
+        const int down = (i & 1) ? 53 : 0;
+        b = false;
+        got = mul_u64(a, n, down, b);
+        ref = dbl(a) * ((double)n * (down ? 0x1p-53 : 1.0));
+        if (b) {
+            b64c++;
+            if (!refusal_ok(ref)) f64++;
+        } else if (got != bits(ref)) {
+            f64++;
+        }
+    }
+    std::printf("mul_u32 %ld %ld %ld\n", N, f32, b32);
+    std::printf("mul_u64 %ld %ld %ld\n", N, f64, b64c);
+
     // add
     fail = bad = 0;
     for (long i = 0; i < N; i++) {
@@ -109,6 +138,13 @@ int main(int argc, char **argv) {
             bad++;
             if (!refusal_ok(ref)) fail++;
         } else if (got != bits(ref)) {
+            fail++;
+        }
+        bool bb2 = false;
+        const uint64_t got2 = add_bf(a, b, bb2);
+        if (bb2) {
+            if (!refusal_ok(ref)) fail++;
+        } else if (got2 != bits(ref)) {
             fail++;
         }
     }
@@ -159,6 +195,13 @@ int main(int argc, char **argv) {
             bad++;
             if (!refusal_ok(ref)) fail++;
         } else if (got != bits(ref)) {
+            fail++;
+        }
+        bool bb2 = false;
+        const uint64_t got2 = div_bf(a, b, bb2);
+        if (bb2) {
+            if (!refusal_ok(ref)) fail++;
+        } else if (got2 != bits(ref)) {
             fail++;
         }
     }

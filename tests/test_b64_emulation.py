@@ -20,7 +20,7 @@ def test_b64_primitives_match_host_fpu(tmp_path, n):
                     str(ROOT / "tests" / "b64_check.cpp"), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe), str(n)], check=True, capture_output=True, text=True).stdout
     rows = {line.split()[0]: [int(x) for x in line.split()[1:]] for line in out.strip().splitlines()}
-    assert set(rows) == {"from_u53", "mul_int", "add", "sub", "div", "div_exact"}
+    assert set(rows) == {"from_u53", "mul_int", "mul_u32", "mul_u64", "add", "sub", "div", "div_exact"}
     for op, (cases, mismatches, refused) in rows.items():
         assert cases > 0 and mismatches == 0, f"{op}: {mismatches} mismatches in {cases}"
         assert refused < cases // 20, f"{op}: refused {refused} of {cases}"
