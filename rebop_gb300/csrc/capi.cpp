@@ -116,6 +116,7 @@ int single_advance(const rbg::Network &net, int64_t *species, double *t, uint64_
     r.fin_t = reinterpret_cast<double *>(b + o_ft);
     r.fin_rng = reinterpret_cast<uint64_t *>(b + o_frng);
     r.times_ok = std::isfinite(tmax) && tmax >= 0;
+    r.t_last = tmax;
     if (!rbg::launch_sampled(net, dn, r, dn.stream, false, nullptr)) return RB_ERR_CUDA;
     unsigned long long flag = 0;
     if (!cuda_check(cudaMemcpyAsync(h.data() + o_fsp, b + o_fsp, c.off - o_fsp, cudaMemcpyDeviceToHost, dn.stream),
@@ -369,6 +370,7 @@ int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, i
     r.events = reinterpret_cast<uint64_t *>(b + o_ev);
     r.fin_species = final_species ? reinterpret_cast<int64_t *>(b + o_fin) : nullptr;
     r.times_ok = std::isfinite(tmax) && tmax >= 0;
+    r.t_last = tmax;
     int mapping = 0;
     if (!rbg::launch_sampled(net, dn, r, dn.stream, true, &mapping)) return RB_ERR_CUDA;
     auto d2h_copy = [&](void *dst, size_t off, size_t bytes) {
@@ -445,6 +447,7 @@ int rb_ensemble_run_device(const rb_network *netp, int64_t n_traj, const int64_t
     r.events = d_events;
     r.fin_species = d_final_species;
     r.times_ok = std::isfinite(tmax) && tmax >= 0;
+    r.t_last = tmax;
     if (!rbg::launch_sampled(net, dn, r, s, false, nullptr)) return RB_ERR_CUDA;
     dn.last_stream = s;
     return RB_OK;

@@ -78,6 +78,12 @@ DeviceCtx *device_ctx() {
     zig_tables_host(tab.data(), tab.data() + kZigOffF);
     zig_fast_tables_host(tab.data(), tab.data() + kZigOffF, reinterpret_cast<uint64_t *>(tab.data() + kZigOffK),
                          tab.data() + kZigOffD);
+    for (int i = 0; i < kZigLayers; i++) {
+        float pair[2];
+        pair[0] = (float)tab[i];
+        pair[1] = (float)(tab[i] - (double)pair[0]);
+        std::memcpy(&tab[kZigOffXdf + i], pair, sizeof pair);
+    }
     if (!cuda_ok(cudaMalloc(&c->zig, sizeof(double) * kZigWords), "cudaMalloc(zig)") ||
         !cuda_ok(cudaMemcpy(c->zig, tab.data(), sizeof(double) * kZigWords, cudaMemcpyHostToDevice),
                  "cudaMemcpy(zig)")) {
@@ -217,19 +223,36 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     if (!cuda_ok(cudaMemsetAsync(dn.scratch, 0, 4 * sizeof(unsigned long long), stream), "cudaMemsetAsync"))
         return false;
     if (r.n_traj == 0) return true;
-    // Kernel choice: the lockstep integer-binary64 kernel when it applies
-    // (RB_SSA_KERNEL=generic|fast overrides), else the generic kernel.
+    // Kernel choice (RB_SSA_KERNEL=spec|fast|generic overrides): the
+    // speculative float-pair kernel, else the lockstep exact kernel, else
+    // the generic shared-memory kernel.
+    {
+        int mm = 0;
+        for (int32_t rr = 0; rr < p.R; rr++) {
+            int s = 0;
+            for (int32_t k = 0; k < p.P; k++) s += p.fac_ord[(size_t)rr * p.P + k];
+            mm = std::max(mm, s);
+        }
+        a.max_mults = mm;
+    }
     const char *pref = std::getenv("RB_SSA_KERNEL");
     const bool want_generic = pref && std::strcmp(pref, "generic") == 0;
-    const bool fast = !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
+    const bool want_fast = pref && std::strcmp(pref, "fast") == 0;
+    const bool spec = !want_generic && !want_fast && r.times_ok && r.t_last < 0x1p60 &&
+                      ssa_spec_supported(a, p.max_order) && ssa_spec_smem(a, 128) <= ctx->smem_optin;
+    const bool fast = !spec && !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
                       ssa_fast_smem(a, 128) <= ctx->smem_optin;
-    if (pref && std::strcmp(pref, "fast") == 0 && !fast) {
-        set_error("RB_SSA_KERNEL=fast but the fast kernel does not cover this network or sample grid");
+    if (pref && ((want_fast && !fast) || (std::strcmp(pref, "spec") == 0 && !spec))) {
+        set_error(std::string("RB_SSA_KERNEL=") + pref + " does not cover this network or sample grid");
         return false;
     }
     int block, per_sm;
     size_t smem;
-    if (fast) {
+    if (spec) {
+        block = 128;
+        smem = ssa_spec_smem(a, block);
+        per_sm = ssa_spec_occupancy(a, block, smem);
+    } else if (fast) {
         block = 128;
         smem = ssa_fast_smem(a, block);
         per_sm = ssa_fast_occupancy(a, block, smem);
@@ -248,10 +271,12 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     int64_t cap = (int64_t)ctx->sm_count * per_sm;
     int grid = (int)std::max<int64_t>(1, std::min(want, cap));
     if (timed && !cuda_ok(cudaEventRecord(dn.ev_start, stream), "cudaEventRecord")) return false;
-    int err = fast ? launch_ssa_fast(a, block, grid, smem, stream) : launch_ssa_thread(a, block, grid, smem, stream);
-    if (err != 0) return cuda_ok((cudaError_t)err, fast ? "ssa_fast_kernel launch" : "ssa_thread_kernel launch");
+    int err = spec   ? launch_ssa_spec(a, block, grid, smem, stream)
+              : fast ? launch_ssa_fast(a, block, grid, smem, stream)
+                     : launch_ssa_thread(a, block, grid, smem, stream);
+    if (err != 0) return cuda_ok((cudaError_t)err, "SSA kernel launch");
     if (timed && !cuda_ok(cudaEventRecord(dn.ev_stop, stream), "cudaEventRecord")) return false;
-    if (mapping) *mapping = fast ? 2 : 0;
+    if (mapping) *mapping = spec ? 3 : fast ? 2 : 0;
     return true;
 }
 

@@ -75,7 +75,8 @@ struct RunDev {
     double *fin_t = nullptr;
     uint64_t *fin_rng = nullptr;
     uint64_t *events = nullptr;
-    bool times_ok = false;  // every sample time finite and >= 0 (lets the fast kernel run)
+    bool times_ok = false;  // every sample time finite and >= 0 (lets the fast kernels run)
+    double t_last = 0.0;    // largest sample time
 };
 
 // Enqueue the sampled-run kernel on `stream` (scratch reset included).

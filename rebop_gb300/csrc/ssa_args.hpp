@@ -11,10 +11,13 @@ constexpr int kZigTable = kZigLayers + 1;  // abscissae x[0..256] / f(x) values
 // Device table layout (doubles / u64 words): x[257] | f[257] | k[256] | d[256]
 // where k[i] is the number of 52-bit fractions u accepted without the wedge
 // test in layer i and d[i] = f[i] - f[i+1] (see zig_fast_tables_host).
+// The last block, xdf[256], holds each x[i] as a float pair (hi, lo) with
+// hi + lo = x[i] to 2^-48, for the float-pair approximation of a draw.
 constexpr int kZigOffF = kZigTable;
 constexpr int kZigOffK = 2 * kZigTable;
 constexpr int kZigOffD = 2 * kZigTable + kZigLayers;
-constexpr int kZigWords = 2 * kZigTable + 2 * kZigLayers;
+constexpr int kZigOffXdf = 2 * kZigTable + 2 * kZigLayers;
+constexpr int kZigWords = 2 * kZigTable + 3 * kZigLayers;
 
 struct SsaArgs {
     // packed network (see network.hpp: Packed)
@@ -60,6 +63,9 @@ struct SsaArgs {
     // start).  A clock increment below one ulp of t never reaches the next
     // sample time; the budget turns that endless loop into RB_ERR_TIMEOUT.
     int64_t budget_ns;
+
+    // Largest sum of reactant orders over the reactions (float-pair error bound).
+    int32_t max_mults;
 };
 
 // Launch the thread-per-trajectory kernel; returns a cudaError_t value.
@@ -74,6 +80,13 @@ bool ssa_fast_supported(const SsaArgs &a, int max_order);
 size_t ssa_fast_smem(const SsaArgs &a, int block);
 int ssa_fast_occupancy(const SsaArgs &a, int block, size_t smem);
 int launch_ssa_fast(const SsaArgs &a, int block, int grid, size_t smem, void *stream);
+
+// Speculative float-pair kernel with exact interval re-runs (ssa_spec.cu):
+// networks with at most 16 reactions and finite sample times in [0, 2^60).
+bool ssa_spec_supported(const SsaArgs &a, int max_order);
+size_t ssa_spec_smem(const SsaArgs &a, int block);
+int ssa_spec_occupancy(const SsaArgs &a, int block, size_t smem);
+int launch_ssa_spec(const SsaArgs &a, int block, int grid, size_t smem, void *stream);
 
 // Every-event runs (src/pyo3_gillespie.rs:209-223) and single
 // _advance_one_reaction steps (src/gillespie.rs:269-297): one thread per

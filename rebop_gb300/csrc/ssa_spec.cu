@@ -1,0 +1,452 @@
+// Speculative thread-per-trajectory SSA kernel: float-pair arithmetic with
+// rigorous error bounds, exact re-run of undecidable sample intervals.
+//
+// What an SSA trajectory records depends on its binary64 arithmetic only
+// through decisions: which reaction fires (#{r : cum_r < total * U}) and
+// whether the next event falls before the sample time (t + Exp1/total <= T).
+// The random stream consumed follows from those decisions too.  And at every
+// sample time the clock is reset to T exactly (gillespie.rs:328-330).
+//
+// So each step here evaluates propensities, their running sum, the Exp1
+// abscissa, Exp1/total, the clock and total*U in float pairs (hi + lo,
+// about 46 bits) on the FP32 pipe -- the widest pipe of the SM -- together
+// with a bound on the distance of every quantity from the value rebop's
+// binary64 arithmetic produces.  A decision whose operands lie farther apart
+// than their bounds is the reference's decision.  When a decision falls inside
+// the margin (or a value leaves the float-pair range), the lane restores the
+// state it saved at the start of the sample interval and re-runs that interval
+// with the exact step of ssa_exact.cuh, so every recorded count, event count
+// and random draw equals rebop's bit for bit.  Intervals of trajectories whose
+// rates are outside the float-pair range always run exactly.
+//
+// Error model: every float-pair operation (including the reference's own
+// binary64 rounding of the same operation) moves a value by at most
+// gamma = 2^-44 relative (the float-pair errors are near 2^-46, binary64's
+// 2^-53).  With M reactant factors per reaction at most and R reactions,
+// running sums are within G = (M + R + 2) gamma of the reference, the clock
+// increment within (G + 6 gamma) q plus the Exp1 abscissa's absolute error
+// over total, and each clock add adds 2 gamma t.
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <cstring>
+
+#include "ssa_exact.cuh"
+
+namespace rbg {
+
+extern __shared__ __align__(16) unsigned char g_spec_smem[];
+
+namespace {
+
+constexpr float kGamma = 0x1p-44f;
+
+struct DF {
+    float h, l;
+};
+
+__device__ __forceinline__ DF fast2sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// a * f for a float pair a and an exact float f >= 0.
+__device__ __forceinline__ DF df_mul_f(DF a, float f) {
+    const float p = __fmul_rn(a.h, f);
+    const float e = __fmaf_rn(a.h, f, -p);
+    return fast2sum(p, __fmaf_rn(a.l, f, e));
+}
+
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return fast2sum(p, e);
+}
+
+// a + b for non-negative float pairs.
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const float s = __fadd_rn(a.h, b.h);
+    const float bb = __fsub_rn(s, a.h);
+    float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    return fast2sum(s, e);
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// a / b for b > 0: one reciprocal estimate, one residual correction.
+__device__ __forceinline__ DF df_div(DF a, DF b, float r) {
+    const float q1 = __fmul_rn(a.h, r);
+    const float p = __fmul_rn(q1, b.h);
+    const float pe = __fmaf_rn(q1, b.h, -p);
+    float res = __fsub_rn(__fsub_rn(a.h, p), pe);
+    res = __fadd_rn(res, a.l);
+    res = __fmaf_rn(-q1, b.l, res);
+    return fast2sum(q1, __fmul_rn(res, r));
+}
+
+// Exact float of an integer 0 <= x < 2^23.
+__device__ __forceinline__ float f23(uint32_t x) { return __fsub_rn(__uint_as_float(0x4B000000u | x), 8388608.0f); }
+
+// u * 2^-53 for 0 <= u < 2^53, keeping the top 46 bits of u (absolute error < 2^-46).
+__device__ __forceinline__ DF df_u53(uint64_t u) {
+    return DF{__fmul_rn(f23((uint32_t)(u >> 30)), 0x1p-23f),
+              __fmul_rn(f23((uint32_t)(u >> 7) & 0x7FFFFFu), 0x1p-46f)};
+}
+
+// Float pair of a double (rare paths: interval starts, rates, the Exp1 tail).
+__device__ __forceinline__ DF df_from_double(double v) {
+    const float h = __double2float_rz(v);
+    return DF{h, __double2float_rn(__dsub_rn(v, (double)h))};
+}
+
+// Exp1 draw as a float pair, consuming the stream exactly as the reference
+// does (the wedge test is decided exactly, see wedge_accept).  xerr bounds
+// |x - rebop's binary64 draw|.
+__device__ __forceinline__ DF exp1_df(Xoshiro &g, const ExactTables &ex, const float2 *xdf, float &xerr) {
+    for (;;) {
+        const uint64_t b = xo_next(g);
+        const int i = (int)(b & 0xff);
+        const uint64_t k = b >> 12;
+        const ulonglong2 e = ex.zxk[i];
+        const float2 X = xdf[i];
+        if (k < e.y) {
+            xerr = kGamma * X.x;
+            return df_mul(df_u53(2 * k + 1), DF{X.x, X.y});
+        }
+        if (i == 0) {
+            const double xd = __dsub_rn(kZigR, log(xo_uniform(g)));
+            const DF x = df_from_double(xd);
+            xerr = kGamma * x.h;
+            return x;
+        }
+        bool bad = false;
+        const uint64_t xb = b64::mul_u64(e.x, 2 * k + 1, 53, bad);
+        if (wedge_accept(ex, i, xb, xo_next(g) >> 11, bad)) {
+            xerr = kGamma * X.x;
+            return df_from_double(__longlong_as_double((long long)xb));
+        }
+    }
+}
+
+// Rate in the float-pair range (0, or 2^-60 .. 2^60), also inside the exact
+// engine's integer domain.
+__device__ __forceinline__ bool spec_rate_ok(uint64_t v) {
+    const uint64_t e = v >> 52;
+    return v == 0 || (e >= 1023 - 60 && e <= 1023 + 60);
+}
+
+struct SpecSmem {
+    ExactTables ex;
+    const float2 *xdf;  // [256] x[i] as float pairs
+    uint64_t *rate;     // [R][block] exact rate bits
+    float2 *rdf;        // [R][block] rates as float pairs
+    int64_t *sp;        // [S][block] counts
+    int64_t *sps;       // [S][block] counts at the start of the interval
+    uint64_t *gsv;      // [4][block] generator state at the start of the interval
+};
+
+__host__ __device__ inline size_t spec_smem_bytes(int S, int R, int P, int Q, int block) {
+    size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;
+    b += 8 * (size_t)R * Q;
+    b += 16 * (size_t)R * block;
+    b += 16 * (size_t)S * block;
+    b += 32 * (size_t)block;
+    b += 4 * ((size_t)R * P + (size_t)R * Q);
+    return (b + 15) & ~(size_t)15;
+}
+
+// Exact re-run of one sample interval from its saved start (counts in sps,
+// generator in gsv, event count ev0, clock t0) up to the step that records
+// the sample at T.  Kept out of line so the float-pair loop keeps its
+// registers; the generator state after the interval goes back to gsv.
+// Returns the event count, or ~0 if the time budget ran out.
+template <int MAXR, bool MACRO>
+__device__ __noinline__ unsigned long long replay_interval(const SsaArgs &a, const ExactTables &ex, int64_t *sp,
+                                                           const int64_t *sps, uint64_t *gsv, const uint64_t *rl,
+                                                           int BD, uint64_t t0, uint64_t T, bool nat,
+                                                           unsigned long long ev0, int64_t t_start) {
+    for (int s = 0; s < a.S; ++s) sp[s * BD] = sps[s * BD];
+    Xoshiro h{gsv[0], gsv[BD], gsv[2 * BD], gsv[3 * BD]};
+    unsigned long long e = ev0;
+    uint64_t t = t0;
+    for (unsigned int n = 1;; ++n) {
+        if ((n & 255u) == 0 && global_ns() - t_start > a.budget_ns) return ~0ull;
+        int ix;
+        uint64_t tx;
+        if (!exact_step<MAXR, MACRO, true>(a, ex, sp, rl, BD, h, t, T, nat, ix, tx)) break;
+        t = tx;
+        ++e;
+        if (ix < a.R)
+            for (int k = 0; k < a.Q; ++k) sp[ex.jsp[ix * a.Q + k] * BD] += ex.jd[ix * a.Q + k];
+    }
+    gsv[0] = h.s0;
+    gsv[BD] = h.s1;
+    gsv[2 * BD] = h.s2;
+    gsv[3 * BD] = h.s3;
+    return e;
+}
+
+}  // namespace
+
+template <int MAXR, bool MACRO>
+__global__ void __launch_bounds__(128, 6) ssa_spec_kernel(const __grid_constant__ SsaArgs a) {
+    const int BD = blockDim.x, tid = threadIdx.x;
+    const int S = a.S, R = a.R, P = a.P, Q = a.Q;
+
+    // ---- shared memory: block tables, then per-lane columns
+    ulonglong2 *zxk = reinterpret_cast<ulonglong2 *>(g_spec_smem);
+    uint64_t *zf = reinterpret_cast<uint64_t *>(zxk + 256);
+    uint64_t *zd = zf + 257;
+    float2 *xdf = reinterpret_cast<float2 *>(zd + 256);
+    int64_t *jd = reinterpret_cast<int64_t *>(xdf + 256);
+    uint64_t *rate = reinterpret_cast<uint64_t *>(jd + (size_t)R * Q);
+    float2 *rdf = reinterpret_cast<float2 *>(rate + (size_t)R * BD);
+    int64_t *spa = reinterpret_cast<int64_t *>(rdf + (size_t)R * BD);
+    int64_t *spsa = spa + (size_t)S * BD;
+    uint64_t *gsva = reinterpret_cast<uint64_t *>(spsa + (size_t)S * BD);
+    int32_t *fac = reinterpret_cast<int32_t *>(gsva + 4 * (size_t)BD);
+    int32_t *jsp = fac + (size_t)R * P;
+    load_exact_tables(a, zxk, zf, zd, fac, jsp, jd);
+    for (int k = tid; k < 256; k += BD) {
+        const double v = a.zig[kZigOffXdf + k];
+        xdf[k] = *reinterpret_cast<const float2 *>(&v);
+    }
+    __syncthreads();
+    const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
+
+    int64_t *const sp = spa + tid;      // counts: sp[s * BD]
+    int64_t *const sps = spsa + tid;    // counts at interval start
+    uint64_t *const gsv = gsva + tid;   // generator at interval start: gsv[w * BD]
+    uint64_t *const rl = rate + tid;    // exact rate bits: rl[r * BD]
+    float2 *const rf = rdf + tid;       // float-pair rates: rf[r * BD]
+
+    const float G = (float)(a.max_mults + R + 2) * kGamma;  // running-sum bound
+    const float c_q = G + 6.0f * kGamma;                     // relative bound of Exp1/total
+    const float c_sel = 2.0f * G + 8.0f * kGamma;            // choice margin / total
+
+    const int64_t t_start = global_ns();
+    unsigned int tick = 0;
+    unsigned long long lane_events = 0;
+    bool out_of_time = false;
+
+    Xoshiro g{0, 0, 0, 0};
+    uint64_t t0 = 0, T = 0;  // exact clock at interval start, sample time
+    DF Tdf{0.f, 0.f}, tdf{0.f, 0.f};
+    float err_t = 0.f;
+    long long i = 0, traj = -1;
+    unsigned long long ev = 0, ev0 = 0;
+    bool nat = false, exact_traj = false, begin = false;
+
+    for (;;) {
+        if (traj < 0) {
+            // ---- take the next trajectory (fresh, or resumed from a state)
+            traj = (long long)atomicAdd(a.work, 1ull);
+            if (traj >= a.n_traj) break;
+            if (a.in_species) {
+                for (int s = 0; s < S; ++s) sp[s * BD] = a.in_species[traj * S + s];
+                t0 = (uint64_t)__double_as_longlong(a.in_t[traj]);
+                g.s0 = a.in_rng[traj * 4 + 0];
+                g.s1 = a.in_rng[traj * 4 + 1];
+                g.s2 = a.in_rng[traj * 4 + 2];
+                g.s3 = a.in_rng[traj * 4 + 3];
+            } else {
+                for (int s = 0; s < S; ++s) sp[s * BD] = a.x0[traj * a.x0_stride + s];
+                t0 = 0;
+                xo_seed(g, a.seeds[traj]);
+            }
+            nat = !emul_domain(t0);
+            exact_traj = nat || (t0 >> 52) > 1023 + 60;
+            for (int r = 0; r < R; ++r) {
+                const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[traj * a.rate_stride + r]);
+                rl[r * BD] = rb;
+                nat |= !emul_domain(rb);
+                exact_traj |= !spec_rate_ok(rb);
+                const DF d = df_from_double(__longlong_as_double((long long)rb));
+                rf[r * BD] = make_float2(d.h, d.l);
+            }
+            exact_traj |= nat;
+            i = 0;
+            ev = 0;
+            begin = true;
+        }
+        if (begin) {
+            // ---- a sample interval starts at t0: save what a re-run needs
+            T = (uint64_t)__double_as_longlong(a.sample_t[i]);
+            Tdf = df_from_double(__longlong_as_double((long long)T));
+            tdf = df_from_double(__longlong_as_double((long long)t0));
+            err_t = kGamma * tdf.h;
+            for (int s = 0; s < S; ++s) sps[s * BD] = sp[s * BD];
+            gsv[0] = g.s0;
+            gsv[BD] = g.s1;
+            gsv[2 * BD] = g.s2;
+            gsv[3 * BD] = g.s3;
+            ev0 = ev;
+            begin = false;
+        }
+        if ((++tick & 1023u) == 0 && global_ns() - t_start > a.budget_ns) {
+            out_of_time = true;
+            break;
+        }
+
+        bool fire = false, replay = exact_traj;
+        int idx = 0;
+        if (!replay) {
+            // ---- float-pair step; the generator advances in place because
+            // each draw happens only when the reference makes it (Exp1 when
+            // total > 0, the uniform when the reaction fires); an undecided
+            // step re-runs the interval from its saved generator state.
+            DF cum[MAXR];
+            DF tot{0.f, 0.f};
+            bool amb = false;
+#pragma unroll
+            for (int r = 0; r < MAXR; ++r) {
+                if (r < R) {
+                    const float2 k = rf[r * BD];
+                    DF acc{k.x, k.y};
+                    for (int p = 0; p < P; ++p) {
+                        const int f = fac[r * P + p];
+                        const int o = f >> 16;
+                        if (o == 0) continue;
+                        const int64_t n = sp[(f & 0xFFFF) * BD];
+                        for (int j = 0; j < o; ++j) {
+                            const int64_t x = n - j;
+                            amb |= (uint64_t)x >= (1ull << 23);
+                            acc = df_mul_f(acc, f23((uint32_t)x & 0x7FFFFFu));
+                        }
+                    }
+                    tot = df_add(tot, acc);
+                    cum[r] = tot;
+                }
+            }
+            if (tot.h > 0.0f) {
+                amb |= tot.h < 0x1p-90f || tot.h > 0x1p90f;
+                float xerr;
+                const DF x = exp1_df(g, ex, xdf, xerr);
+                const float r = rcp_approx(tot.h);
+                const DF q = df_div(x, tot, r);
+                const DF tn = df_add(tdf, q);
+                const float err_tn = err_t + 1.001f * xerr * r + c_q * q.h + 2.0f * kGamma * tn.h;
+                const float d = __fadd_rn(__fsub_rn(Tdf.h, tn.h), __fsub_rn(Tdf.l, tn.l));
+                const float mt = err_tn + 4.0f * kGamma * Tdf.h;
+                fire = d > mt;
+                amb |= !(fire || d < -mt) || !(err_tn < 3.0e38f);
+                if (fire && !amb) {
+                    const DF ch = df_mul(tot, df_u53(xo_next(g) >> 11));
+                    const float msel = c_sel * tot.h;
+#pragma unroll
+                    for (int rr = 0; rr < MAXR; ++rr) {
+                        if (rr < R) {
+                            const float dr = __fadd_rn(__fsub_rn(cum[rr].h, ch.h), __fsub_rn(cum[rr].l, ch.l));
+                            idx += dr < 0.0f ? 1 : 0;
+                            amb |= fabsf(dr) <= msel;
+                        }
+                    }
+                    tdf = tn;
+                    err_t = err_tn;
+                }
+            }
+            replay = amb;
+        }
+        if (replay) {
+            ev = replay_interval<MAXR, MACRO>(a, ex, sp, sps, gsv, rl, BD, t0, T, nat, ev0, t_start);
+            if (ev == ~0ull) {
+                ev = ev0;
+                out_of_time = true;
+                break;
+            }
+            g = Xoshiro{gsv[0], gsv[BD], gsv[2 * BD], gsv[3 * BD]};
+            fire = false;
+        }
+        if (fire) {
+            ++ev;
+            if (idx < R)
+                for (int k = 0; k < Q; ++k) sp[jsp[idx * Q + k] * BD] += jd[idx * Q + k];
+        } else {
+            // ---- record sample i at t = T
+            int64_t *o = a.out + (size_t)i * a.n_save * a.n_traj + traj;
+            for (int k = 0; k < a.n_save; ++k) o[(size_t)k * a.n_traj] = sp[a.save_idx[k] * BD];
+            if (++i < a.n_samples) {
+                t0 = T;
+                begin = true;
+            } else {
+                if (a.fin_species)
+                    for (int s = 0; s < S; ++s) a.fin_species[traj * S + s] = sp[s * BD];
+                if (a.fin_t) a.fin_t[traj] = __longlong_as_double((long long)T);
+                if (a.fin_rng) {
+                    a.fin_rng[traj * 4 + 0] = g.s0;
+                    a.fin_rng[traj * 4 + 1] = g.s1;
+                    a.fin_rng[traj * 4 + 2] = g.s2;
+                    a.fin_rng[traj * 4 + 3] = g.s3;
+                }
+                if (a.events) a.events[traj] = ev;
+                lane_events += ev;
+                traj = -1;
+            }
+        }
+    }
+    if (out_of_time) {
+        lane_events += ev;
+        atomicExch(a.work + 2, 1ull);
+    }
+    for (int off = 16; off > 0; off >>= 1) lane_events += __shfl_down_sync(0xffffffffu, lane_events, off);
+    if ((tid & 31) == 0 && lane_events) atomicAdd(a.work + 1, lane_events);
+}
+
+// ------------------------------------------------------------------ host side
+
+namespace {
+
+template <int MAXR, bool MACRO>
+int spec_launch(const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st) {
+    auto kern = ssa_spec_kernel<MAXR, MACRO>;
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return (int)err;
+    kern<<<grid, block, smem, st>>>(a);
+    return (int)cudaGetLastError();
+}
+
+template <int MAXR, bool MACRO>
+int spec_occupancy(int block, size_t smem) {
+    int n = 0;
+    auto kern = ssa_spec_kernel<MAXR, MACRO>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, block, smem);
+    return n;
+}
+
+template <bool MACRO>
+int spec_dispatch(const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st, int *occ) {
+    if (a.R <= 8) return occ ? (*occ = spec_occupancy<8, MACRO>(block, smem), 0)
+                             : spec_launch<8, MACRO>(a, block, grid, smem, st);
+    return occ ? (*occ = spec_occupancy<16, MACRO>(block, smem), 0) : spec_launch<16, MACRO>(a, block, grid, smem, st);
+}
+
+}  // namespace
+
+bool ssa_spec_supported(const SsaArgs &a, int max_order) {
+    return a.R <= 16 && a.S < 65536 && max_order < 32768;
+}
+
+size_t ssa_spec_smem(const SsaArgs &a, int block) { return spec_smem_bytes(a.S, a.R, a.P, a.Q, block); }
+
+int ssa_spec_occupancy(const SsaArgs &a, int block, size_t smem) {
+    int occ = 0;
+    if (a.macro_mode) spec_dispatch<true>(a, block, 0, smem, nullptr, &occ);
+    else spec_dispatch<false>(a, block, 0, smem, nullptr, &occ);
+    return occ;
+}
+
+int launch_ssa_spec(const SsaArgs &a, int block, int grid, size_t smem, void *stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return a.macro_mode ? spec_dispatch<true>(a, block, grid, smem, st, nullptr)
+                        : spec_dispatch<false>(a, block, grid, smem, st, nullptr);
+}
+
+}  // namespace rbg
