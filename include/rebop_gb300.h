@@ -56,7 +56,11 @@ typedef struct {
     uint64_t h2d_bytes;    /* host->device bytes copied by the call         */
     uint64_t d2h_bytes;    /* device->host bytes copied by the call         */
     int32_t kernel_launches;
-    int32_t mapping;       /* 0 = thread per trajectory, 1 = warp per trajectory */
+    int32_t mapping;       /* kernel that ran: 0 generic thread-per-trajectory,
+                            * 2 lockstep exact, 3 speculative float-pair */
+    uint64_t exact_reruns; /* sample intervals the speculative kernel re-ran
+                            * exactly because a decision fell inside its
+                            * error margin */
 } rb_run_stats;
 
 /* ------------------------------------------------- reaction network -----

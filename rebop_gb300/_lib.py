@@ -29,6 +29,7 @@ class RunStats(C.Structure):
         ("d2h_bytes", C.c_uint64),
         ("kernel_launches", C.c_int32),
         ("mapping", C.c_int32),
+        ("exact_reruns", C.c_uint64),
     ]
 
 

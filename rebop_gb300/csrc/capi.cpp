@@ -378,10 +378,10 @@ int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, i
         d2h += bytes;
         return cuda_check(cudaMemcpyAsync(dst, b + off, bytes, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync");
     };
-    unsigned long long sc[2] = {0, 0};  // total events, timeout flag
+    unsigned long long sc[3] = {0, 0, 0};  // total events, timeout flag, exact re-runs
     if (!d2h_copy(out, o_out, NT * NS * N * 8) || !d2h_copy(events, o_ev, N * 8) ||
         !d2h_copy(final_species, o_fin, final_species ? N * S * 8 : 0) ||
-        !cuda_check(cudaMemcpyAsync(sc, dn.scratch + 1, 16, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync") ||
+        !cuda_check(cudaMemcpyAsync(sc, dn.scratch + 1, 24, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync") ||
         !cuda_check(cudaStreamSynchronize(dn.stream), "ssa_thread_kernel"))
         return RB_ERR_CUDA;
     if (sc[1]) return fail(RB_ERR_TIMEOUT, "ensemble run ran out of its time budget (RB_KERNEL_BUDGET_S)");
@@ -393,7 +393,8 @@ int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, i
         stats->kernel_ms = ms;
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
         stats->h2d_bytes = h2d;
-        stats->d2h_bytes = d2h + 16;
+        stats->d2h_bytes = d2h + 24;
+        stats->exact_reruns = sc[2];
         stats->kernel_launches = N ? 1 : 0;
         stats->mapping = mapping;
     }

@@ -355,6 +355,7 @@ __global__ void __launch_bounds__(128, 6) ssa_spec_kernel(const __grid_constant_
             replay = amb;
         }
         if (replay) {
+            if (!exact_traj) atomicAdd(a.work + 3, 1ull);  // speculation undecided: count the re-run
             ev = replay_interval<MAXR, MACRO>(a, ex, sp, sps, gsv, rl, BD, t0, T, nat, ev0, t_start);
             if (ev == ~0ull) {
                 ev = ev0;

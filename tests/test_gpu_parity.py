@@ -285,13 +285,42 @@ def test_fast_and_generic_kernels_match_oracle(rb, O):
     cases.append((_sir(rb), O.sir_net(), [999, 1, 0], 100.0, 20, rates))
     for net, onet, x0, tmax, nb, r in cases:
         seeds = _seeds(n, 21)
+        spec = _with_kernel("spec", lambda: net.run_ensemble(x0, seeds, tmax, nb, rates=r))
         fast = _with_kernel("fast", lambda: net.run_ensemble(x0, seeds, tmax, nb, rates=r))
         gen = _with_kernel("generic", lambda: net.run_ensemble(x0, seeds, tmax, nb, rates=r))
         ref, ev, _, _ = onet.run_ensemble(x0, seeds, tmax, nb, rates=r)
-        assert fast.stats["mapping"] == 2 and gen.stats["mapping"] == 0
+        assert spec.stats["mapping"] == 3 and fast.stats["mapping"] == 2 and gen.stats["mapping"] == 0
+        np.testing.assert_array_equal(spec.counts, ref)
         np.testing.assert_array_equal(fast.counts, ref)
         np.testing.assert_array_equal(gen.counts, ref)
+        np.testing.assert_array_equal(spec.events, ev)
         np.testing.assert_array_equal(fast.events, ev)
+
+
+def test_spec_kernel_stress_against_oracle(rb, O):
+    # Speculative float-pair kernel: bit-exact counts and event numbers over
+    # many trajectories, including long sample intervals (the clock's error
+    # bound grows with the events of an interval) and order-2 reactions.
+    seeds = _seeds(4000, 41)
+    res = _with_kernel("spec", lambda: _dimer(rb).run_ensemble([1, 0, 0, 0], seeds, 1.0, 25))
+    ref, ev, _, _ = O.dimer_net().run_ensemble([1, 0, 0, 0], seeds, 1.0, 25)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+    assert res.stats["exact_reruns"] < 4000 * 26 // 100
+    # dimers2 (benchmarks/benches/my_benchmark.rs:74-105): 2A <-> A_A -> AA with 1e5 A
+    net = rb.Network(3)
+    for k, e, d in [(1.0, [1, 0, 0], [-1, 0, 0]), (1 / 500, [2, 0, 0], [-2, 1, 0]),
+                    (0.5, [0, 1, 0], [2, -1, 0]), (1 / 25, [0, 1, 0], [0, -1, 1])]:
+        net.add_reaction(rb.Rate.lma(k, e), d)
+    onet = O.OracleNet(3)
+    for k, e, d in [(1.0, [1, 0, 0], [-1, 0, 0]), (1 / 500, [2, 0, 0], [-2, 1, 0]),
+                    (0.5, [0, 1, 0], [2, -1, 0]), (1 / 25, [0, 1, 0], [0, -1, 1])]:
+        onet.add_lma(k, e, d)
+    seeds = _seeds(256, 42)
+    res = _with_kernel("spec", lambda: net.run_ensemble([5000, 0, 0], seeds, 2.0, 4))
+    ref, ev, _, _ = onet.run_ensemble([5000, 0, 0], seeds, 2.0, 4)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
 
 
 def test_fast_kernel_native_fallback_paths(rb, O):
