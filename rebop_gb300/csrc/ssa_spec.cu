@@ -315,9 +315,13 @@ __global__ void __launch_bounds__(128, 6) ssa_spec_kernel(const __grid_constant_
                         const int o = f >> 16;
                         if (o == 0) continue;
                         const int64_t n = sp[(f & 0xFFFF) * BD];
+                        // Counts must be in [0, 2^23).  For n < o the factors
+                        // n, n-1, ... reach 0 before going negative, so the
+                        // product is 0 (the reference's is +-0, which leaves
+                        // every running sum unchanged): clamp at 0.
+                        amb |= (uint64_t)n >= (1ull << 23);
                         for (int j = 0; j < o; ++j) {
-                            const int64_t x = n - j;
-                            amb |= (uint64_t)x >= (1ull << 23);
+                            const int64_t x = n - j > 0 ? n - j : 0;
                             acc = df_mul_f(acc, f23((uint32_t)x & 0x7FFFFFu));
                         }
                     }
