@@ -239,7 +239,7 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     const bool want_generic = pref && std::strcmp(pref, "generic") == 0;
     const bool want_fast = pref && std::strcmp(pref, "fast") == 0;
     const bool spec = !want_generic && !want_fast && r.times_ok && r.t_last < 0x1p60 &&
-                      ssa_spec_supported(a, p.max_order) && ssa_spec_smem(a, 128) <= ctx->smem_optin;
+                      ssa_spec_supported(a, p.max_order) && ssa_spec_smem(a, ssa_spec_block()) <= ctx->smem_optin;
     const bool fast = !spec && !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
                       ssa_fast_smem(a, 128) <= ctx->smem_optin;
     if (pref && ((want_fast && !fast) || (std::strcmp(pref, "spec") == 0 && !spec))) {
@@ -249,7 +249,7 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     int block, per_sm;
     size_t smem;
     if (spec) {
-        block = 128;
+        block = ssa_spec_block();
         smem = ssa_spec_smem(a, block);
         per_sm = ssa_spec_occupancy(a, block, smem);
     } else if (fast) {

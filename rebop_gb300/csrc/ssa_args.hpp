@@ -84,6 +84,7 @@ int launch_ssa_fast(const SsaArgs &a, int block, int grid, size_t smem, void *st
 // Speculative float-pair kernel with exact interval re-runs (ssa_spec.cu):
 // networks with at most 16 reactions and finite sample times in [0, 2^60).
 bool ssa_spec_supported(const SsaArgs &a, int max_order);
+int ssa_spec_block();
 size_t ssa_spec_smem(const SsaArgs &a, int block);
 int ssa_spec_occupancy(const SsaArgs &a, int block, size_t smem);
 int launch_ssa_spec(const SsaArgs &a, int block, int grid, size_t smem, void *stream);

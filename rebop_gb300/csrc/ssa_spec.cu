@@ -142,23 +142,22 @@ __device__ __forceinline__ bool spec_rate_ok(uint64_t v) {
     return v == 0 || (e >= 1023 - 60 && e <= 1023 + 60);
 }
 
-struct SpecSmem {
-    ExactTables ex;
-    const float2 *xdf;  // [256] x[i] as float pairs
-    uint64_t *rate;     // [R][block] exact rate bits
-    float2 *rdf;        // [R][block] rates as float pairs
-    int64_t *sp;        // [S][block] counts
-    int64_t *sps;       // [S][block] counts at the start of the interval
-    uint64_t *gsv;      // [4][block] generator state at the start of the interval
-};
+constexpr int kSpecBlock = 512;   // slots = lanes per block; one block per SM
+constexpr int kSpecPhase = 128;   // steps between two compactions of the block
 
+// Shared memory: block tables, then per-slot columns [field][block].  A slot
+// holds one trajectory's whole state between phases; a lane works on the
+// slot the last compaction gave it.
 __host__ __device__ inline size_t spec_smem_bytes(int S, int R, int P, int Q, int block) {
-    size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;
-    b += 8 * (size_t)R * Q;
-    b += 16 * (size_t)R * block;
-    b += 16 * (size_t)S * block;
-    b += 32 * (size_t)block;
-    b += 4 * ((size_t)R * P + (size_t)R * Q);
+    size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;  // zxk, zf, zd, xdf
+    b += 8 * (size_t)R * Q;                             // jd
+    b += 16 * (size_t)R * block;                        // exact rate bits, float-pair rates
+    b += 16 * (size_t)S * block;                        // counts, counts at interval start
+    b += 32 * (size_t)block;                            // generator at interval start
+    b += 80 * (size_t)block;                            // 10 state words
+    b += 24 * (size_t)block;                            // 5 float state words, flags
+    b += 4 * (size_t)block + 128;                       // slot list, block counters
+    b += 4 * ((size_t)R * P + (size_t)R * Q);           // fac, jsp
     return (b + 15) & ~(size_t)15;
 }
 
@@ -195,12 +194,15 @@ __device__ __noinline__ unsigned long long replay_interval(const SsaArgs &a, con
 
 }  // namespace
 
+// Slot flags.
+constexpr uint32_t kLive = 1, kNat = 2, kExactTraj = 4, kBegin = 8;
+
 template <int MAXR, bool MACRO>
-__global__ void __launch_bounds__(128, 6) ssa_spec_kernel(const __grid_constant__ SsaArgs a) {
+__global__ void __launch_bounds__(kSpecBlock, 1) ssa_spec_kernel(const __grid_constant__ SsaArgs a) {
     const int BD = blockDim.x, tid = threadIdx.x;
     const int S = a.S, R = a.R, P = a.P, Q = a.Q;
 
-    // ---- shared memory: block tables, then per-lane columns
+    // ---- shared memory: block tables, then per-slot columns
     ulonglong2 *zxk = reinterpret_cast<ulonglong2 *>(g_spec_smem);
     uint64_t *zf = reinterpret_cast<uint64_t *>(zxk + 256);
     uint64_t *zd = zf + 257;
@@ -211,194 +213,267 @@ __global__ void __launch_bounds__(128, 6) ssa_spec_kernel(const __grid_constant_
     int64_t *spa = reinterpret_cast<int64_t *>(rdf + (size_t)R * BD);
     int64_t *spsa = spa + (size_t)S * BD;
     uint64_t *gsva = reinterpret_cast<uint64_t *>(spsa + (size_t)S * BD);
-    int32_t *fac = reinterpret_cast<int32_t *>(gsva + 4 * (size_t)BD);
+    uint64_t *stw = gsva + 4 * (size_t)BD;                         // [10][BD]
+    float *stf = reinterpret_cast<float *>(stw + 10 * (size_t)BD);  // [5][BD]
+    uint32_t *stflag = reinterpret_cast<uint32_t *>(stf + 5 * (size_t)BD);
+    int32_t *slot_list = reinterpret_cast<int32_t *>(stflag + BD);
+    int32_t *ctr = slot_list + BD;  // [0] live slots, [1] abort, [2..] warp totals
+    int32_t *fac = ctr + 32;
     int32_t *jsp = fac + (size_t)R * P;
     load_exact_tables(a, zxk, zf, zd, fac, jsp, jd);
     for (int k = tid; k < 256; k += BD) {
         const double v = a.zig[kZigOffXdf + k];
         xdf[k] = *reinterpret_cast<const float2 *>(&v);
     }
+    stflag[tid] = 0;
+    if (tid < 32) ctr[tid] = 0;
     __syncthreads();
     const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
-
-    int64_t *const sp = spa + tid;      // counts: sp[s * BD]
-    int64_t *const sps = spsa + tid;    // counts at interval start
-    uint64_t *const gsv = gsva + tid;   // generator at interval start: gsv[w * BD]
-    uint64_t *const rl = rate + tid;    // exact rate bits: rl[r * BD]
-    float2 *const rf = rdf + tid;       // float-pair rates: rf[r * BD]
 
     const float G = (float)(a.max_mults + R + 2) * kGamma;  // running-sum bound
     const float c_q = G + 6.0f * kGamma;                     // relative bound of Exp1/total
     const float c_sel = 2.0f * G + 8.0f * kGamma;            // choice margin / total
-
     const int64_t t_start = global_ns();
     unsigned int tick = 0;
     unsigned long long lane_events = 0;
-    bool out_of_time = false;
 
+    // ---- this lane's slot and its state, cached in registers during a phase
+    int slot = tid;
     Xoshiro g{0, 0, 0, 0};
-    uint64_t t0 = 0, T = 0;  // exact clock at interval start, sample time
+    uint64_t t0 = 0, T = 0;
     DF Tdf{0.f, 0.f}, tdf{0.f, 0.f};
     float err_t = 0.f;
     long long i = 0, traj = -1;
     unsigned long long ev = 0, ev0 = 0;
-    bool nat = false, exact_traj = false, begin = false;
+    bool live = true, nat = false, exact_traj = false, begin = false, abort_run = false;
 
     for (;;) {
-        if (traj < 0) {
-            // ---- take the next trajectory (fresh, or resumed from a state)
-            traj = (long long)atomicAdd(a.work, 1ull);
-            if (traj >= a.n_traj) break;
-            if (a.in_species) {
-                for (int s = 0; s < S; ++s) sp[s * BD] = a.in_species[traj * S + s];
-                t0 = (uint64_t)__double_as_longlong(a.in_t[traj]);
-                g.s0 = a.in_rng[traj * 4 + 0];
-                g.s1 = a.in_rng[traj * 4 + 1];
-                g.s2 = a.in_rng[traj * 4 + 2];
-                g.s3 = a.in_rng[traj * 4 + 3];
-            } else {
-                for (int s = 0; s < S; ++s) sp[s * BD] = a.x0[traj * a.x0_stride + s];
-                t0 = 0;
-                xo_seed(g, a.seeds[traj]);
+        // ---------------------------------------------------------- phase
+        if (slot >= 0) {
+            int64_t *const sp = spa + slot;
+            int64_t *const sps = spsa + slot;
+            uint64_t *const gsv = gsva + slot;
+            uint64_t *const rl = rate + slot;
+            float2 *const rf = rdf + slot;
+            for (int step = 0; step < kSpecPhase && live; ++step) {
+                if (traj < 0) {
+                    // take the next trajectory into this slot
+                    traj = (long long)atomicAdd(a.work, 1ull);
+                    if (traj >= a.n_traj) {
+                        live = false;
+                        break;
+                    }
+                    if (a.in_species) {
+                        for (int s = 0; s < S; ++s) sp[s * BD] = a.in_species[traj * S + s];
+                        t0 = (uint64_t)__double_as_longlong(a.in_t[traj]);
+                        g.s0 = a.in_rng[traj * 4 + 0];
+                        g.s1 = a.in_rng[traj * 4 + 1];
+                        g.s2 = a.in_rng[traj * 4 + 2];
+                        g.s3 = a.in_rng[traj * 4 + 3];
+                    } else {
+                        for (int s = 0; s < S; ++s) sp[s * BD] = a.x0[traj * a.x0_stride + s];
+                        t0 = 0;
+                        xo_seed(g, a.seeds[traj]);
+                    }
+                    nat = !emul_domain(t0);
+                    exact_traj = (t0 >> 52) > 1023 + 60;
+                    for (int r = 0; r < R; ++r) {
+                        const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[traj * a.rate_stride + r]);
+                        rl[r * BD] = rb;
+                        nat |= !emul_domain(rb);
+                        exact_traj |= !spec_rate_ok(rb);
+                        const DF d = df_from_double(__longlong_as_double((long long)rb));
+                        rf[r * BD] = make_float2(d.h, d.l);
+                    }
+                    exact_traj |= nat;
+                    i = 0;
+                    ev = 0;
+                    begin = true;
+                }
+                if (begin) {
+                    // a sample interval starts at t0: save what a re-run needs
+                    T = (uint64_t)__double_as_longlong(a.sample_t[i]);
+                    Tdf = df_from_double(__longlong_as_double((long long)T));
+                    tdf = df_from_double(__longlong_as_double((long long)t0));
+                    err_t = kGamma * tdf.h;
+                    for (int s = 0; s < S; ++s) sps[s * BD] = sp[s * BD];
+                    gsv[0] = g.s0;
+                    gsv[BD] = g.s1;
+                    gsv[2 * BD] = g.s2;
+                    gsv[3 * BD] = g.s3;
+                    ev0 = ev;
+                    begin = false;
+                }
+                if ((++tick & 1023u) == 0 && global_ns() - t_start > a.budget_ns) {
+                    abort_run = true;
+                    break;
+                }
+
+                bool fire = false, replay = exact_traj;
+                int idx = 0;
+                if (!replay) {
+                    // float-pair step; the generator advances in place since
+                    // each draw happens only when the reference makes it (Exp1
+                    // when total > 0, the uniform when the reaction fires); an
+                    // undecided step re-runs the interval from its saved state.
+                    DF cum[MAXR];
+                    DF tot{0.f, 0.f};
+                    bool amb = false;
+#pragma unroll
+                    for (int r = 0; r < MAXR; ++r) {
+                        if (r < R) {
+                            const float2 k = rf[r * BD];
+                            DF acc{k.x, k.y};
+                            for (int p = 0; p < P; ++p) {
+                                const int f = fac[r * P + p];
+                                const int o = f >> 16;
+                                if (o == 0) continue;
+                                const int64_t n = sp[(f & 0xFFFF) * BD];
+                                // counts in [0, 2^23); for n < o the factors
+                                // n, n-1, ... reach 0 before going negative, so
+                                // the product is 0 (the reference's +-0 leaves
+                                // every running sum unchanged): clamp at 0.
+                                amb |= (uint64_t)n >= (1ull << 23);
+                                for (int j = 0; j < o; ++j) {
+                                    const int64_t x = n - j > 0 ? n - j : 0;
+                                    acc = df_mul_f(acc, f23((uint32_t)x & 0x7FFFFFu));
+                                }
+                            }
+                            tot = df_add(tot, acc);
+                            cum[r] = tot;
+                        }
+                    }
+                    if (tot.h > 0.0f) {
+                        amb |= tot.h < 0x1p-90f || tot.h > 0x1p90f;
+                        float xerr;
+                        const DF x = exp1_df(g, ex, xdf, xerr);
+                        const float r = rcp_approx(tot.h);
+                        const DF q = df_div(x, tot, r);
+                        const DF tn = df_add(tdf, q);
+                        const float err_tn = err_t + 1.001f * xerr * r + c_q * q.h + 2.0f * kGamma * tn.h;
+                        const float d = __fadd_rn(__fsub_rn(Tdf.h, tn.h), __fsub_rn(Tdf.l, tn.l));
+                        const float mt = err_tn + 4.0f * kGamma * Tdf.h;
+                        fire = d > mt;
+                        amb |= !(fire || d < -mt) || !(err_tn < 3.0e38f);
+                        if (fire && !amb) {
+                            const DF ch = df_mul(tot, df_u53(xo_next(g) >> 11));
+                            const float msel = c_sel * tot.h;
+#pragma unroll
+                            for (int rr = 0; rr < MAXR; ++rr) {
+                                if (rr < R) {
+                                    const float dr =
+                                        __fadd_rn(__fsub_rn(cum[rr].h, ch.h), __fsub_rn(cum[rr].l, ch.l));
+                                    idx += dr < 0.0f ? 1 : 0;
+                                    amb |= fabsf(dr) <= msel;
+                                }
+                            }
+                            tdf = tn;
+                            err_t = err_tn;
+                        }
+                    }
+                    replay = amb;
+                }
+                if (replay) {
+                    if (!exact_traj) atomicAdd(a.work + 3, 1ull);  // speculation undecided
+                    ev = replay_interval<MAXR, MACRO>(a, ex, sp, sps, gsv, rl, BD, t0, T, nat, ev0, t_start);
+                    if (ev == ~0ull) {
+                        ev = ev0;
+                        abort_run = true;
+                        break;
+                    }
+                    g = Xoshiro{gsv[0], gsv[BD], gsv[2 * BD], gsv[3 * BD]};
+                    fire = false;
+                }
+                if (fire) {
+                    ++ev;
+                    if (idx < R)
+                        for (int k = 0; k < Q; ++k) sp[jsp[idx * Q + k] * BD] += jd[idx * Q + k];
+                } else {
+                    // record sample i at t = T
+                    int64_t *o = a.out + (size_t)i * a.n_save * a.n_traj + traj;
+                    for (int k = 0; k < a.n_save; ++k) o[(size_t)k * a.n_traj] = sp[a.save_idx[k] * BD];
+                    if (++i < a.n_samples) {
+                        t0 = T;
+                        begin = true;
+                    } else {
+                        if (a.fin_species)
+                            for (int s = 0; s < S; ++s) a.fin_species[traj * S + s] = sp[s * BD];
+                        if (a.fin_t) a.fin_t[traj] = __longlong_as_double((long long)T);
+                        if (a.fin_rng) {
+                            a.fin_rng[traj * 4 + 0] = g.s0;
+                            a.fin_rng[traj * 4 + 1] = g.s1;
+                            a.fin_rng[traj * 4 + 2] = g.s2;
+                            a.fin_rng[traj * 4 + 3] = g.s3;
+                        }
+                        if (a.events) a.events[traj] = ev;
+                        lane_events += ev;
+                        traj = -1;
+                    }
+                }
             }
-            nat = !emul_domain(t0);
-            exact_traj = nat || (t0 >> 52) > 1023 + 60;
-            for (int r = 0; r < R; ++r) {
-                const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[traj * a.rate_stride + r]);
-                rl[r * BD] = rb;
-                nat |= !emul_domain(rb);
-                exact_traj |= !spec_rate_ok(rb);
-                const DF d = df_from_double(__longlong_as_double((long long)rb));
-                rf[r * BD] = make_float2(d.h, d.l);
+            // ---- park the slot's state
+            if (live) {
+                stw[0 * BD + slot] = g.s0;
+                stw[1 * BD + slot] = g.s1;
+                stw[2 * BD + slot] = g.s2;
+                stw[3 * BD + slot] = g.s3;
+                stw[4 * BD + slot] = t0;
+                stw[5 * BD + slot] = T;
+                stw[6 * BD + slot] = (uint64_t)traj;
+                stw[7 * BD + slot] = ev;
+                stw[8 * BD + slot] = ev0;
+                stw[9 * BD + slot] = (uint64_t)i;
+                stf[0 * BD + slot] = tdf.h;
+                stf[1 * BD + slot] = tdf.l;
+                stf[2 * BD + slot] = err_t;
+                stf[3 * BD + slot] = Tdf.h;
+                stf[4 * BD + slot] = Tdf.l;
             }
-            exact_traj |= nat;
-            i = 0;
-            ev = 0;
-            begin = true;
+            stflag[slot] = (live ? kLive : 0u) | (nat ? kNat : 0u) | (exact_traj ? kExactTraj : 0u) |
+                           (begin ? kBegin : 0u);
+            if (abort_run) ctr[1] = 1;
         }
-        if (begin) {
-            // ---- a sample interval starts at t0: save what a re-run needs
-            T = (uint64_t)__double_as_longlong(a.sample_t[i]);
-            Tdf = df_from_double(__longlong_as_double((long long)T));
-            tdf = df_from_double(__longlong_as_double((long long)t0));
-            err_t = kGamma * tdf.h;
-            for (int s = 0; s < S; ++s) sps[s * BD] = sp[s * BD];
-            gsv[0] = g.s0;
-            gsv[BD] = g.s1;
-            gsv[2 * BD] = g.s2;
-            gsv[3 * BD] = g.s3;
-            ev0 = ev;
-            begin = false;
+        __syncthreads();
+        // ---------------------------------------------------------- compaction
+        // Live slots, in slot order, go to lanes 0 .. n-1: warps stay full
+        // while trajectories end at different times.
+        const bool alive = (stflag[tid] & kLive) != 0;
+        const unsigned int bal = __ballot_sync(0xffffffffu, alive);
+        const int warp = tid >> 5, lane = tid & 31;
+        if (lane == 0) ctr[2 + warp] = __popc(bal);
+        __syncthreads();
+        int base = 0, n_live = 0;
+        for (int w = 0; w < (BD >> 5); ++w) {
+            const int c = ctr[2 + w];
+            base += w < warp ? c : 0;
+            n_live += c;
         }
-        if ((++tick & 1023u) == 0 && global_ns() - t_start > a.budget_ns) {
-            out_of_time = true;
+        if (alive) slot_list[base + __popc(bal & ((1u << lane) - 1u))] = tid;
+        const bool stop = n_live == 0 || ctr[1] != 0;
+        __syncthreads();
+        if (stop) {
+            if (ctr[1] != 0 && tid == 0) atomicExch(a.work + 2, 1ull);
             break;
         }
-
-        bool fire = false, replay = exact_traj;
-        int idx = 0;
-        if (!replay) {
-            // ---- float-pair step; the generator advances in place because
-            // each draw happens only when the reference makes it (Exp1 when
-            // total > 0, the uniform when the reaction fires); an undecided
-            // step re-runs the interval from its saved generator state.
-            DF cum[MAXR];
-            DF tot{0.f, 0.f};
-            bool amb = false;
-#pragma unroll
-            for (int r = 0; r < MAXR; ++r) {
-                if (r < R) {
-                    const float2 k = rf[r * BD];
-                    DF acc{k.x, k.y};
-                    for (int p = 0; p < P; ++p) {
-                        const int f = fac[r * P + p];
-                        const int o = f >> 16;
-                        if (o == 0) continue;
-                        const int64_t n = sp[(f & 0xFFFF) * BD];
-                        // Counts must be in [0, 2^23).  For n < o the factors
-                        // n, n-1, ... reach 0 before going negative, so the
-                        // product is 0 (the reference's is +-0, which leaves
-                        // every running sum unchanged): clamp at 0.
-                        amb |= (uint64_t)n >= (1ull << 23);
-                        for (int j = 0; j < o; ++j) {
-                            const int64_t x = n - j > 0 ? n - j : 0;
-                            acc = df_mul_f(acc, f23((uint32_t)x & 0x7FFFFFu));
-                        }
-                    }
-                    tot = df_add(tot, acc);
-                    cum[r] = tot;
-                }
-            }
-            if (tot.h > 0.0f) {
-                amb |= tot.h < 0x1p-90f || tot.h > 0x1p90f;
-                float xerr;
-                const DF x = exp1_df(g, ex, xdf, xerr);
-                const float r = rcp_approx(tot.h);
-                const DF q = df_div(x, tot, r);
-                const DF tn = df_add(tdf, q);
-                const float err_tn = err_t + 1.001f * xerr * r + c_q * q.h + 2.0f * kGamma * tn.h;
-                const float d = __fadd_rn(__fsub_rn(Tdf.h, tn.h), __fsub_rn(Tdf.l, tn.l));
-                const float mt = err_tn + 4.0f * kGamma * Tdf.h;
-                fire = d > mt;
-                amb |= !(fire || d < -mt) || !(err_tn < 3.0e38f);
-                if (fire && !amb) {
-                    const DF ch = df_mul(tot, df_u53(xo_next(g) >> 11));
-                    const float msel = c_sel * tot.h;
-#pragma unroll
-                    for (int rr = 0; rr < MAXR; ++rr) {
-                        if (rr < R) {
-                            const float dr = __fadd_rn(__fsub_rn(cum[rr].h, ch.h), __fsub_rn(cum[rr].l, ch.l));
-                            idx += dr < 0.0f ? 1 : 0;
-                            amb |= fabsf(dr) <= msel;
-                        }
-                    }
-                    tdf = tn;
-                    err_t = err_tn;
-                }
-            }
-            replay = amb;
+        slot = tid < n_live ? slot_list[tid] : -1;
+        live = slot >= 0;
+        if (live) {
+            g = Xoshiro{stw[0 * BD + slot], stw[1 * BD + slot], stw[2 * BD + slot], stw[3 * BD + slot]};
+            t0 = stw[4 * BD + slot];
+            T = stw[5 * BD + slot];
+            traj = (long long)stw[6 * BD + slot];
+            ev = stw[7 * BD + slot];
+            ev0 = stw[8 * BD + slot];
+            i = (long long)stw[9 * BD + slot];
+            tdf = DF{stf[0 * BD + slot], stf[1 * BD + slot]};
+            err_t = stf[2 * BD + slot];
+            Tdf = DF{stf[3 * BD + slot], stf[4 * BD + slot]};
+            const uint32_t fl = stflag[slot];
+            nat = (fl & kNat) != 0;
+            exact_traj = (fl & kExactTraj) != 0;
+            begin = (fl & kBegin) != 0;
         }
-        if (replay) {
-            if (!exact_traj) atomicAdd(a.work + 3, 1ull);  // speculation undecided: count the re-run
-            ev = replay_interval<MAXR, MACRO>(a, ex, sp, sps, gsv, rl, BD, t0, T, nat, ev0, t_start);
-            if (ev == ~0ull) {
-                ev = ev0;
-                out_of_time = true;
-                break;
-            }
-            g = Xoshiro{gsv[0], gsv[BD], gsv[2 * BD], gsv[3 * BD]};
-            fire = false;
-        }
-        if (fire) {
-            ++ev;
-            if (idx < R)
-                for (int k = 0; k < Q; ++k) sp[jsp[idx * Q + k] * BD] += jd[idx * Q + k];
-        } else {
-            // ---- record sample i at t = T
-            int64_t *o = a.out + (size_t)i * a.n_save * a.n_traj + traj;
-            for (int k = 0; k < a.n_save; ++k) o[(size_t)k * a.n_traj] = sp[a.save_idx[k] * BD];
-            if (++i < a.n_samples) {
-                t0 = T;
-                begin = true;
-            } else {
-                if (a.fin_species)
-                    for (int s = 0; s < S; ++s) a.fin_species[traj * S + s] = sp[s * BD];
-                if (a.fin_t) a.fin_t[traj] = __longlong_as_double((long long)T);
-                if (a.fin_rng) {
-                    a.fin_rng[traj * 4 + 0] = g.s0;
-                    a.fin_rng[traj * 4 + 1] = g.s1;
-                    a.fin_rng[traj * 4 + 2] = g.s2;
-                    a.fin_rng[traj * 4 + 3] = g.s3;
-                }
-                if (a.events) a.events[traj] = ev;
-                lane_events += ev;
-                traj = -1;
-            }
-        }
-    }
-    if (out_of_time) {
-        lane_events += ev;
-        atomicExch(a.work + 2, 1ull);
+        __syncthreads();  // slot flags are rewritten by the next phase
     }
     for (int off = 16; off > 0; off >>= 1) lane_events += __shfl_down_sync(0xffffffffu, lane_events, off);
     if ((tid & 31) == 0 && lane_events) atomicAdd(a.work + 1, lane_events);
@@ -434,6 +509,8 @@ int spec_dispatch(const SsaArgs &a, int block, int grid, size_t smem, cudaStream
 }
 
 }  // namespace
+
+int ssa_spec_block() { return kSpecBlock; }
 
 bool ssa_spec_supported(const SsaArgs &a, int max_order) {
     return a.R <= 16 && a.S < 65536 && max_order < 32768;
