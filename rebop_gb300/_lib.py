@@ -105,6 +105,10 @@ lib.rbg_internal_zig_tables.argtypes = [P(_f64), P(_f64)]
 lib.rbg_internal_zig_tables.restype = None
 lib.rbg_internal_fp64_fma_rate.argtypes = [_vp]
 lib.rbg_internal_fp64_fma_rate.restype = _f64
+lib.rbg_internal_jit_source.argtypes = [_vp, _cp, _sz]
+lib.rbg_internal_jit_source.restype = C.c_int
+lib.rbg_internal_jit_compile.argtypes = [_vp, P(_u64)]
+lib.rbg_internal_jit_compile.restype = C.c_int
 
 
 def last_error() -> str:

@@ -23,7 +23,10 @@ LIB = BUILD / "librebop_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["ssa_thread.cu", "ssa_fast.cu", "ssa_spec.cu", "fp64_peak.cu"]
-CXX_SOURCES = ["network.cpp", "engine.cpp", "capi.cpp"]
+CXX_SOURCES = ["network.cpp", "engine.cpp", "capi.cpp", "ssa_jit.cpp"]
+# Device headers embedded in the library for run-time network compilation.
+JIT_HEADERS = ["rtc_types.hpp", "ssa_args.hpp", "b64.cuh", "rng.cuh", "ssa_exact.cuh", "ssa_spec_body.cuh"]
+JIT_SOURCES_CPP = "jit_headers.cpp"
 
 
 def cuda_home() -> Path:
@@ -48,10 +51,28 @@ def up_to_date() -> bool:
     return all(p.stat().st_mtime <= t for p in _sources() if p.exists())
 
 
+def _write_jit_headers() -> Path:
+    """C++ file holding the device headers as string literals."""
+    out = ["// generated by rebop_gb300/build.py from csrc/ -- do not edit", "namespace rbg {",
+           "extern const char *const kJitHeaderNames[] = {"]
+    out += [f'    "{h}",' for h in JIT_HEADERS]
+    out += ["};", "extern const char *const kJitHeaderSources[] = {"]
+    for h in JIT_HEADERS:
+        text = (CSRC / h).read_text()
+        if ')RBGJIT"' in text:
+            raise RuntimeError(f"{h} holds the raw-string delimiter")
+        out.append('    R"RBGJIT(' + text + ')RBGJIT",')
+    out += ["};", f"extern const int kJitHeaderCount = {len(JIT_HEADERS)};", "}  // namespace rbg", ""]
+    path = BUILD / JIT_SOURCES_CPP
+    path.write_text("\n".join(out))
+    return path
+
+
 def build(force: bool = False, verbose: bool = False) -> Path:
     if not force and up_to_date():
         return LIB
     BUILD.mkdir(exist_ok=True)
+    jit_cpp = _write_jit_headers()
     cuda = cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
     inc = ["-I", str(ROOT / "include"), "-I", str(CSRC)]
@@ -74,11 +95,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         return r.stderr
 
+    jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-c", str(jit_cpp), "-o", str(BUILD / (JIT_SOURCES_CPP + ".o"))])
+
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         for err in ex.map(run, jobs):
             if verbose and err:
                 print(err)
-    objs = [str(BUILD / (s + ".o")) for s in CUDA_SOURCES + CXX_SOURCES]
+    objs = [str(BUILD / (s + ".o")) for s in CUDA_SOURCES + CXX_SOURCES + [JIT_SOURCES_CPP]]
     tmp = BUILD / f"librebop_gb300.{os.getpid()}.so"
     run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *objs, "-lpthread", "-ldl", "-lrt"])
     os.replace(tmp, LIB)

@@ -14,7 +14,7 @@
 // the host FPU on random and constructed operands.
 #pragma once
 
-#include <cstdint>
+#include "rtc_types.hpp"
 
 #if defined(__CUDACC__)
 #define B64_HD __host__ __device__ __forceinline__

@@ -7,6 +7,7 @@
 #include <random>
 
 #include "engine.hpp"
+#include "ssa_jit.hpp"
 #include "network.hpp"
 
 using rbg::set_error;
@@ -597,5 +598,30 @@ void rb_rng_state_from_seed(uint64_t seed, uint64_t *state) {
 // Test hook (not part of the public header): the Exp1 ziggurat tables the
 // device copy is made from.
 void rbg_internal_zig_tables(double *x, double *f) { rbg::zig_tables_host(x, f); }
+
+// Test hooks: the generated source of a network's kernel, and its compilation
+// by NVRTC (no GPU needed).  Return RB_ERR_UNSUPPORTED when the generator does
+// not cover the network.
+int rbg_internal_jit_source(const rb_network *net, char *buf, size_t len) {
+    if (!net) return fail(RB_ERR_INVALID, "null network");
+    std::lock_guard<std::mutex> lk(net->net.mu);
+    const rbg::Packed p = net->net.pack();
+    if (!rbg::jit_supported(p)) return fail(RB_ERR_UNSUPPORTED, "network not covered by the generator");
+    return copy_name(rbg::jit_net_source(p), buf, len);
+}
+
+int rbg_internal_jit_compile(const rb_network *net, uint64_t *image_bytes) {
+    if (!net) return fail(RB_ERR_INVALID, "null network");
+    rbg::Packed p;
+    {
+        std::lock_guard<std::mutex> lk(net->net.mu);
+        p = net->net.pack();
+    }
+    if (!rbg::jit_supported(p)) return fail(RB_ERR_UNSUPPORTED, "network not covered by the generator");
+    size_t n = 0;
+    if (!rbg::jit_compile(p, &n)) return RB_ERR_UNSUPPORTED;
+    if (image_bytes) *image_bytes = n;
+    return RB_OK;
+}
 
 }  // extern "C"

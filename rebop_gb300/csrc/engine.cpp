@@ -1,5 +1,6 @@
 // Host engine implementation.
 #include "engine.hpp"
+#include "ssa_jit.hpp"
 
 #include <cmath>
 #include <cstdlib>
@@ -238,8 +239,11 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     const char *pref = std::getenv("RB_SSA_KERNEL");
     const bool want_generic = pref && std::strcmp(pref, "generic") == 0;
     const bool want_fast = pref && std::strcmp(pref, "fast") == 0;
+    const int spec_grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>(ctx->sm_count, (r.n_traj + ssa_spec_block() - 1) / ssa_spec_block()));
+    const int spec_slots = ssa_spec_slots(a, spec_grid, ctx->smem_optin);
     const bool spec = !want_generic && !want_fast && r.times_ok && r.t_last < 0x1p60 &&
-                      ssa_spec_supported(a, p.max_order) && ssa_spec_smem(a, ssa_spec_block()) <= ctx->smem_optin;
+                      ssa_spec_supported(a, p.max_order) && spec_slots > 0;
     const bool fast = !spec && !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
                       ssa_fast_smem(a, 128) <= ctx->smem_optin;
     if (pref && ((want_fast && !fast) || (std::strcmp(pref, "spec") == 0 && !spec))) {
@@ -250,7 +254,8 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     size_t smem;
     if (spec) {
         block = ssa_spec_block();
-        smem = ssa_spec_smem(a, block);
+        a.n_slots = spec_slots;
+        smem = ssa_spec_smem(a, spec_slots);
         per_sm = ssa_spec_occupancy(a, block, smem);
     } else if (fast) {
         block = 128;
@@ -270,13 +275,26 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     int64_t want = (r.n_traj + block - 1) / block;
     int64_t cap = (int64_t)ctx->sm_count * per_sm;
     int grid = (int)std::max<int64_t>(1, std::min(want, cap));
+    // A network the generator covers runs on its own compiled kernel when the
+    // ensemble is large enough to repay the compilation (RB_JIT=0 never,
+    // RB_JIT=1 always); results are the same either way.
+    const void *jk = nullptr;
+    if (spec && jit_supported(p)) {
+        const char *jit = std::getenv("RB_JIT");
+        const bool want = jit ? std::strcmp(jit, "0") != 0 : r.n_traj >= 4096;
+        if (want) {
+            jk = jit_kernel(p);
+            if (!jk && jit && std::strcmp(jit, "1") == 0) return false;
+        }
+    }
     if (timed && !cuda_ok(cudaEventRecord(dn.ev_start, stream), "cudaEventRecord")) return false;
-    int err = spec   ? launch_ssa_spec(a, block, grid, smem, stream)
+    int err = jk     ? launch_ssa_jit(jk, a, block, grid, smem, stream)
+              : spec ? launch_ssa_spec(a, block, grid, smem, stream)
               : fast ? launch_ssa_fast(a, block, grid, smem, stream)
                      : launch_ssa_thread(a, block, grid, smem, stream);
     if (err != 0) return cuda_ok((cudaError_t)err, "SSA kernel launch");
     if (timed && !cuda_ok(cudaEventRecord(dn.ev_stop, stream), "cudaEventRecord")) return false;
-    if (mapping) *mapping = spec ? 3 : fast ? 2 : 0;
+    if (mapping) *mapping = jk ? 4 : spec ? 3 : fast ? 2 : 0;
     return true;
 }
 

@@ -16,7 +16,7 @@
 // compiler cannot fuse it into an FMA.
 #pragma once
 
-#include <cstdint>
+#include "rtc_types.hpp"
 
 namespace rbg {
 

@@ -2,7 +2,7 @@
 // translation units and the host glue).  All pointers are device pointers.
 #pragma once
 
-#include <cstdint>
+#include "rtc_types.hpp"
 
 namespace rbg {
 
@@ -53,7 +53,7 @@ struct SsaArgs {
     uint64_t *events;        // [n_traj]
 
     // scratch: [0] trajectory ticket, [1] total accepted events,
-    // [2] set to 1 when the time budget ran out
+    // [2] set to 1 when the time budget ran out, [3] exact interval re-runs
     unsigned long long *work;
 
     // Exp1 ziggurat tables: x[257] then f[257]
@@ -66,6 +66,10 @@ struct SsaArgs {
 
     // Largest sum of reactant orders over the reactions (float-pair error bound).
     int32_t max_mults;
+
+    // Speculative kernel: trajectory slots per block (a multiple of 32, at
+    // least the block size).
+    int32_t n_slots;
 };
 
 // Launch the thread-per-trajectory kernel; returns a cudaError_t value.
@@ -85,7 +89,11 @@ int launch_ssa_fast(const SsaArgs &a, int block, int grid, size_t smem, void *st
 // networks with at most 16 reactions and finite sample times in [0, 2^60).
 bool ssa_spec_supported(const SsaArgs &a, int max_order);
 int ssa_spec_block();
-size_t ssa_spec_smem(const SsaArgs &a, int block);
+size_t ssa_spec_smem(const SsaArgs &a, int slots);
+// Slots per block for a launch of `grid` blocks: enough for every trajectory
+// to be resident at once when shared memory allows; 0 if not even one slot
+// per lane fits in smem_limit bytes.
+int ssa_spec_slots(const SsaArgs &a, int grid, size_t smem_limit);
 int ssa_spec_occupancy(const SsaArgs &a, int block, size_t smem);
 int launch_ssa_spec(const SsaArgs &a, int block, int grid, size_t smem, void *stream);
 

@@ -13,7 +13,9 @@
 //               macro's first r with total * U < cum_r (gillespie_macro.rs:159)
 #pragma once
 
+#if !defined(__CUDACC_RTC__)
 #include <cuda_runtime.h>
+#endif
 
 #include "b64.cuh"
 #include "rng.cuh"

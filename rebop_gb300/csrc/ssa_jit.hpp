@@ -1,0 +1,26 @@
+// Run-time compiled network kernels (ssa_jit.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "network.hpp"
+#include "ssa_args.hpp"
+
+namespace rbg {
+
+// Networks the generator covers: 1..16 species, 1..32 reactions, jumps of
+// magnitude below 2^23.
+bool jit_supported(const Packed &p);
+// CUDA source of the speculative kernel specialised for the network.
+std::string jit_net_source(const Packed &p);
+// Compile (or find in the disk cache) the network's kernel image without
+// loading it; false with the error set on failure.
+bool jit_compile(const Packed &p, size_t *image_bytes);
+// The compiled kernel for the current device (compiled on first use); null
+// with the error set on failure.
+const void *jit_kernel(const Packed &p);
+int launch_ssa_jit(const void *kern, const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st);
+
+}  // namespace rbg

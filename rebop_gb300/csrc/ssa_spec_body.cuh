@@ -1,0 +1,551 @@
+// Speculative thread-per-trajectory SSA kernel: float-pair arithmetic with
+// rigorous error bounds, exact re-run of undecidable sample intervals.
+//
+// What an SSA trajectory records depends on its binary64 arithmetic only
+// through decisions: which reaction fires (#{r : cum_r < total * U}) and
+// whether the next event falls before the sample time (t + Exp1/total <= T).
+// The random stream consumed follows from those decisions too.  And at every
+// sample time the clock is reset to T exactly (gillespie.rs:328-330).
+//
+// So each step here evaluates propensities, their running sum, the Exp1
+// abscissa, Exp1/total, the clock and total*U in float pairs (hi + lo,
+// about 46 bits) on the FP32 pipe -- the widest pipe of the SM -- together
+// with a bound on the distance of every quantity from the value rebop's
+// binary64 arithmetic produces.  A decision whose operands lie farther apart
+// than their bounds is the reference's decision.  When a decision falls inside
+// the margin (or a value leaves the float-pair range), the lane restores the
+// state it saved at the start of the sample interval and re-runs that interval
+// with the exact step of ssa_exact.cuh, so every recorded count, event count
+// and random draw equals rebop's bit for bit.  Intervals of trajectories whose
+// rates are outside the float-pair range always run exactly.
+//
+// Error model: every float-pair operation (including the reference's own
+// binary64 rounding of the same operation) moves a value by at most
+// gamma = 2^-44 relative (the float-pair errors are near 2^-46, binary64's
+// 2^-53).  With M reactant factors per reaction at most and R reactions,
+// running sums are within G = (M + R + 2) gamma of the reference, the clock
+// increment within (G + 6 gamma) q plus the Exp1 abscissa's absolute error
+// over total, and each clock add adds 2 gamma t.
+// This header holds the device side, templated on the network operations of
+// the float-pair step: TableOps below walks the packed descriptor; a network
+// compiled at run time supplies the same members unrolled, with its counts in
+// registers.
+#pragma once
+
+#include "ssa_exact.cuh"
+
+namespace rbg {
+
+extern __shared__ __align__(16) unsigned char g_spec_smem[];
+
+constexpr float kGamma = 0x1p-44f;
+
+struct DF {
+    float h, l;
+};
+
+__device__ __forceinline__ DF fast2sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// a * f for a float pair a and an exact float f >= 0.
+__device__ __forceinline__ DF df_mul_f(DF a, float f) {
+    const float p = __fmul_rn(a.h, f);
+    const float e = __fmaf_rn(a.h, f, -p);
+    return fast2sum(p, __fmaf_rn(a.l, f, e));
+}
+
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return fast2sum(p, e);
+}
+
+// a + b for non-negative float pairs.
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const float s = __fadd_rn(a.h, b.h);
+    const float bb = __fsub_rn(s, a.h);
+    float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    return fast2sum(s, e);
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// a / b for b > 0: one reciprocal estimate, one residual correction.
+__device__ __forceinline__ DF df_div(DF a, DF b, float r) {
+    const float q1 = __fmul_rn(a.h, r);
+    const float p = __fmul_rn(q1, b.h);
+    const float pe = __fmaf_rn(q1, b.h, -p);
+    float res = __fsub_rn(__fsub_rn(a.h, p), pe);
+    res = __fadd_rn(res, a.l);
+    res = __fmaf_rn(-q1, b.l, res);
+    return fast2sum(q1, __fmul_rn(res, r));
+}
+
+// Exact float of an integer 0 <= x < 2^23.
+__device__ __forceinline__ float f23(uint32_t x) { return __fsub_rn(__uint_as_float(0x4B000000u | x), 8388608.0f); }
+
+// u * 2^-53 for 0 <= u < 2^53, keeping the top 46 bits of u (absolute error < 2^-46).
+__device__ __forceinline__ DF df_u53(uint64_t u) {
+    return DF{__fmul_rn(f23((uint32_t)(u >> 30)), 0x1p-23f),
+              __fmul_rn(f23((uint32_t)(u >> 7) & 0x7FFFFFu), 0x1p-46f)};
+}
+
+// Float pair of a double (rare paths: interval starts, rates, the Exp1 tail).
+__device__ __forceinline__ DF df_from_double(double v) {
+    const float h = __double2float_rz(v);
+    return DF{h, __double2float_rn(__dsub_rn(v, (double)h))};
+}
+
+// Exp1 draw as a float pair, consuming the stream exactly as the reference
+// does (the wedge test is decided exactly, see wedge_accept).  xerr bounds
+// |x - rebop's binary64 draw|.
+__device__ __forceinline__ DF exp1_df(Xoshiro &g, const ExactTables &ex, const float2 *xdf, float &xerr) {
+    for (;;) {
+        const uint64_t b = xo_next(g);
+        const int i = (int)(b & 0xff);
+        const uint64_t k = b >> 12;
+        const ulonglong2 e = ex.zxk[i];
+        const float2 X = xdf[i];
+        if (k < e.y) {
+            xerr = kGamma * X.x;
+            return df_mul(df_u53(2 * k + 1), DF{X.x, X.y});
+        }
+        if (i == 0) {
+            const double xd = __dsub_rn(kZigR, log(xo_uniform(g)));
+            const DF x = df_from_double(xd);
+            xerr = kGamma * x.h;
+            return x;
+        }
+        bool bad = false;
+        const uint64_t xb = b64::mul_u64(e.x, 2 * k + 1, 53, bad);
+        if (wedge_accept(ex, i, xb, xo_next(g) >> 11, bad)) {
+            xerr = kGamma * X.x;
+            return df_from_double(__longlong_as_double((long long)xb));
+        }
+    }
+}
+
+// Rate in the float-pair range (0, or 2^-60 .. 2^60), also inside the exact
+// engine's integer domain.
+__device__ __forceinline__ bool spec_rate_ok(uint64_t v) {
+    const uint64_t e = v >> 52;
+    return v == 0 || (e >= 1023 - 60 && e <= 1023 + 60);
+}
+
+constexpr int kSpecBlock = 512;   // lanes per block; one block per SM
+constexpr int kSpecPhase = 128;   // steps between two compactions of the block
+constexpr int kSpecMaxSlots = 2048;
+
+// Shared memory: block tables, then per-slot columns [field][slots].  A slot
+// holds one trajectory's whole state between phases; a lane works on the
+// slot the last compaction gave it.  A block may hold more slots than lanes:
+// then the lanes rotate over the live slots, so every resident trajectory
+// advances at the same pace and no second wave of late starters is left to
+// run on a nearly empty SM.
+__host__ __device__ inline size_t spec_smem_bytes(int S, int R, int P, int Q, int slots) {
+    size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;  // zxk, zf, zd, xdf
+    b += 8 * (size_t)R * Q;                             // jd
+    b += 16 * (size_t)R * slots;                        // exact rate bits, float-pair rates
+    b += 16 * (size_t)S * slots;                        // counts, counts at interval start
+    b += 32 * (size_t)slots;                            // generator at interval start
+    b += 80 * (size_t)slots;                            // 10 state words
+    b += 24 * (size_t)slots;                            // 5 float state words, flags
+    b += 4 * (size_t)slots + 512;                       // slot list, block counters
+    b += 4 * ((size_t)R * P + (size_t)R * Q);           // fac, jsp
+    return (b + 15) & ~(size_t)15;
+}
+
+// Exact re-run of one sample interval from its saved start (counts in sps,
+// generator in gsv, event count ev0, clock t0) up to the step that records
+// the sample at T.  Kept out of line so the float-pair loop keeps its
+// registers; the generator state after the interval goes back to gsv.
+// Returns the event count, or ~0 if the time budget ran out.
+template <int MAXR, bool MACRO>
+__device__ __noinline__ unsigned long long replay_interval(const SsaArgs &a, const ExactTables &ex, int64_t *sp,
+                                                           const int64_t *sps, uint64_t *gsv, const uint64_t *rl,
+                                                           int BD, uint64_t t0, uint64_t T, bool nat,
+                                                           unsigned long long ev0, int64_t t_start) {
+    for (int s = 0; s < a.S; ++s) sp[s * BD] = sps[s * BD];
+    Xoshiro h{gsv[0], gsv[BD], gsv[2 * BD], gsv[3 * BD]};
+    unsigned long long e = ev0;
+    uint64_t t = t0;
+    for (unsigned int n = 1;; ++n) {
+        if ((n & 255u) == 0 && global_ns() - t_start > a.budget_ns) return ~0ull;
+        int ix;
+        uint64_t tx;
+        if (!exact_step<MAXR, MACRO, true>(a, ex, sp, rl, BD, h, t, T, nat, ix, tx)) break;
+        t = tx;
+        ++e;
+        if (ix < a.R)
+            for (int k = 0; k < a.Q; ++k) sp[ex.jsp[ix * a.Q + k] * BD] += ex.jd[ix * a.Q + k];
+    }
+    gsv[0] = h.s0;
+    gsv[BD] = h.s1;
+    gsv[2 * BD] = h.s2;
+    gsv[3 * BD] = h.s3;
+    return e;
+}
+
+// Slot flags.
+constexpr uint32_t kLive = 1, kNat = 2, kExactTraj = 4, kBegin = 8;
+
+// Network operations of the float-pair step over a data-driven descriptor:
+// the counts stay in the slot's shared-memory column and every reaction walks
+// its (species, order) factor list.  A generated network (see ssa_jit.cpp)
+// supplies the same members with the network unrolled and the counts held in
+// registers.
+template <int MAXR, bool MACRO>
+struct TableOps {
+    static constexpr int kMaxR = MAXR;
+    static constexpr bool kMacro = MACRO;
+    struct Counts {};
+    __device__ static int nr(const SsaArgs &a) { return a.R; }
+    // registers <- column; false if a count is outside [0, 2^23)
+    __device__ static bool load(Counts &, const SsaArgs &, const int64_t *, int) { return true; }
+    // column <- registers
+    __device__ static void store(const Counts &, const SsaArgs &, int64_t *, int) {}
+    // interval-start copy of the counts
+    __device__ static void save(const Counts &, const SsaArgs &a, const int64_t *sp, int64_t *sps, int NS) {
+        for (int s = 0; s < a.S; ++s) sps[s * NS] = sp[s * NS];
+    }
+    // Float-pair propensities and running sums; true if a count leaves the
+    // float-pair range (then the step is undecided).
+    __device__ static bool props(const SsaArgs &a, const ExactTables &ex, const Counts &, const int64_t *sp,
+                                 const float2 *rf, int NS, DF *cum, DF &tot) {
+        bool amb = false;
+        tot = DF{0.f, 0.f};
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r) {
+            if (r < a.R) {
+                const float2 k = rf[r * NS];
+                DF acc{k.x, k.y};
+                for (int p = 0; p < a.P; ++p) {
+                    const int f = ex.fac[r * a.P + p];
+                    const int o = f >> 16;
+                    if (o == 0) continue;
+                    const int64_t n = sp[(f & 0xFFFF) * NS];
+                    // counts in [0, 2^23); for n < o the factors n, n-1, ...
+                    // reach 0 before going negative, so the product is 0 (the
+                    // reference's +-0 leaves every running sum unchanged):
+                    // clamp at 0.
+                    amb |= (uint64_t)n >= (1ull << 23);
+                    for (int j = 0; j < o; ++j) {
+                        const int64_t x = n - j > 0 ? n - j : 0;
+                        acc = df_mul_f(acc, f23((uint32_t)x & 0x7FFFFFu));
+                    }
+                }
+                tot = df_add(tot, acc);
+                cum[r] = tot;
+            }
+        }
+        return amb;
+    }
+    __device__ static void jump(Counts &, const SsaArgs &a, const ExactTables &ex, int64_t *sp, int NS, int idx) {
+        if (idx < a.R)
+            for (int k = 0; k < a.Q; ++k) sp[ex.jsp[idx * a.Q + k] * NS] += ex.jd[idx * a.Q + k];
+    }
+};
+
+// The kernel body: one block per SM, `a.n_slots` trajectory slots rotated
+// over the block's lanes in phases of kSpecPhase steps.
+template <class Ops>
+__device__ __forceinline__ void spec_body(const SsaArgs &a) {
+    constexpr int MAXR = Ops::kMaxR;
+    constexpr bool MACRO = Ops::kMacro;
+    const int BD = blockDim.x, tid = threadIdx.x;
+    const int NS = a.n_slots;  // slots per block, a multiple of 32, >= BD
+    const int S = a.S, R = Ops::nr(a), P = a.P, Q = a.Q;
+
+    // ---- shared memory: block tables, then per-slot columns
+    ulonglong2 *zxk = reinterpret_cast<ulonglong2 *>(g_spec_smem);
+    uint64_t *zf = reinterpret_cast<uint64_t *>(zxk + 256);
+    uint64_t *zd = zf + 257;
+    float2 *xdf = reinterpret_cast<float2 *>(zd + 256);
+    int64_t *jd = reinterpret_cast<int64_t *>(xdf + 256);
+    uint64_t *rate = reinterpret_cast<uint64_t *>(jd + (size_t)R * Q);
+    float2 *rdf = reinterpret_cast<float2 *>(rate + (size_t)R * NS);
+    int64_t *spa = reinterpret_cast<int64_t *>(rdf + (size_t)R * NS);
+    int64_t *spsa = spa + (size_t)S * NS;
+    uint64_t *gsva = reinterpret_cast<uint64_t *>(spsa + (size_t)S * NS);
+    uint64_t *stw = gsva + 4 * (size_t)NS;                         // [10][NS]
+    float *stf = reinterpret_cast<float *>(stw + 10 * (size_t)NS);  // [5][NS]
+    uint32_t *stflag = reinterpret_cast<uint32_t *>(stf + 5 * (size_t)NS);
+    int32_t *slot_list = reinterpret_cast<int32_t *>(stflag + NS);
+    int32_t *ctr = slot_list + NS;  // [1] abort, [2..] live slots per (chunk, warp)
+    int32_t *fac = ctr + 128;
+    int32_t *jsp = fac + (size_t)R * P;
+    load_exact_tables(a, zxk, zf, zd, fac, jsp, jd);
+    for (int k = tid; k < 256; k += BD) {
+        const double v = a.zig[kZigOffXdf + k];
+        xdf[k] = *reinterpret_cast<const float2 *>(&v);
+    }
+    // every slot starts live and empty (no trajectory taken yet)
+    for (int k = tid; k < NS; k += BD) {
+        stflag[k] = kLive;
+        stw[6 * (size_t)NS + k] = ~0ull;
+    }
+    if (tid < 128) ctr[tid] = 0;
+    __syncthreads();
+    const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
+
+    const float G = (float)(a.max_mults + R + 2) * kGamma;  // running-sum bound
+    const float c_q = G + 6.0f * kGamma;                     // relative bound of Exp1/total
+    const float c_sel = 2.0f * G + 8.0f * kGamma;            // choice margin / total
+    const int64_t t_start = global_ns();
+    unsigned int tick = 0, rot = 0;
+    unsigned long long lane_events = 0;
+
+    // ---- this lane's slot and its state, cached in registers during a phase
+    int slot = tid;
+    typename Ops::Counts c{};
+    Xoshiro g{0, 0, 0, 0};
+    uint64_t t0 = 0, T = 0;
+    DF Tdf{0.f, 0.f}, tdf{0.f, 0.f};
+    float err_t = 0.f;
+    long long i = 0, traj = -1;
+    unsigned long long ev = 0, ev0 = 0;
+    bool live = true, nat = false, exact_traj = false, begin = false, abort_run = false;
+
+    for (;;) {
+        // ---------------------------------------------------------- phase
+        if (slot >= 0) {
+            int64_t *const sp = spa + slot;
+            int64_t *const sps = spsa + slot;
+            uint64_t *const gsv = gsva + slot;
+            uint64_t *const rl = rate + slot;
+            float2 *const rf = rdf + slot;
+            for (int step = 0; step < kSpecPhase && live; ++step) {
+                if (traj < 0) {
+                    // take the next trajectory into this slot
+                    traj = (long long)atomicAdd(a.work, 1ull);
+                    if (traj >= a.n_traj) {
+                        live = false;
+                        break;
+                    }
+                    if (a.in_species) {
+                        for (int s = 0; s < S; ++s) sp[s * NS] = a.in_species[traj * S + s];
+                        t0 = (uint64_t)__double_as_longlong(a.in_t[traj]);
+                        g.s0 = a.in_rng[traj * 4 + 0];
+                        g.s1 = a.in_rng[traj * 4 + 1];
+                        g.s2 = a.in_rng[traj * 4 + 2];
+                        g.s3 = a.in_rng[traj * 4 + 3];
+                    } else {
+                        for (int s = 0; s < S; ++s) sp[s * NS] = a.x0[traj * a.x0_stride + s];
+                        t0 = 0;
+                        xo_seed(g, a.seeds[traj]);
+                    }
+                    nat = !emul_domain(t0);
+                    exact_traj = (t0 >> 52) > 1023 + 60;
+                    for (int r = 0; r < R; ++r) {
+                        const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[traj * a.rate_stride + r]);
+                        rl[r * NS] = rb;
+                        nat |= !emul_domain(rb);
+                        exact_traj |= !spec_rate_ok(rb);
+                        const DF d = df_from_double(__longlong_as_double((long long)rb));
+                        rf[r * NS] = make_float2(d.h, d.l);
+                    }
+                    exact_traj |= nat;
+                    exact_traj |= !Ops::load(c, a, sp, NS);
+                    i = 0;
+                    ev = 0;
+                    begin = true;
+                }
+                if (begin) {
+                    // a sample interval starts at t0: save what a re-run needs
+                    T = (uint64_t)__double_as_longlong(a.sample_t[i]);
+                    Tdf = df_from_double(__longlong_as_double((long long)T));
+                    tdf = df_from_double(__longlong_as_double((long long)t0));
+                    err_t = kGamma * tdf.h;
+                    if (exact_traj)
+                        for (int s = 0; s < S; ++s) sps[s * NS] = sp[s * NS];
+                    else
+                        Ops::save(c, a, sp, sps, NS);
+                    gsv[0] = g.s0;
+                    gsv[NS] = g.s1;
+                    gsv[2 * NS] = g.s2;
+                    gsv[3 * NS] = g.s3;
+                    ev0 = ev;
+                    begin = false;
+                }
+                if ((++tick & 1023u) == 0 && global_ns() - t_start > a.budget_ns) {
+                    abort_run = true;
+                    break;
+                }
+
+                bool fire = false, replay = exact_traj;
+                int idx = 0;
+                if (!replay) {
+                    // float-pair step; the generator advances in place since
+                    // each draw happens only when the reference makes it (Exp1
+                    // when total > 0, the uniform when the reaction fires); an
+                    // undecided step re-runs the interval from its saved state.
+                    DF cum[MAXR];
+                    DF tot;
+                    bool amb = Ops::props(a, ex, c, sp, rf, NS, cum, tot);
+                    if (tot.h > 0.0f) {
+                        amb |= tot.h < 0x1p-90f || tot.h > 0x1p90f;
+                        float xerr;
+                        const DF x = exp1_df(g, ex, xdf, xerr);
+                        const float r = rcp_approx(tot.h);
+                        const DF q = df_div(x, tot, r);
+                        const DF tn = df_add(tdf, q);
+                        const float err_tn = err_t + 1.001f * xerr * r + c_q * q.h + 2.0f * kGamma * tn.h;
+                        const float d = __fadd_rn(__fsub_rn(Tdf.h, tn.h), __fsub_rn(Tdf.l, tn.l));
+                        const float mt = err_tn + 4.0f * kGamma * Tdf.h;
+                        fire = d > mt;
+                        amb |= !(fire || d < -mt) || !(err_tn < 3.0e38f);
+                        if (fire && !amb) {
+                            const DF ch = df_mul(tot, df_u53(xo_next(g) >> 11));
+                            const float msel = c_sel * tot.h;
+#pragma unroll
+                            for (int rr = 0; rr < MAXR; ++rr) {
+                                if (rr < R) {
+                                    const float dr =
+                                        __fadd_rn(__fsub_rn(cum[rr].h, ch.h), __fsub_rn(cum[rr].l, ch.l));
+                                    idx += dr < 0.0f ? 1 : 0;
+                                    amb |= fabsf(dr) <= msel;
+                                }
+                            }
+                            tdf = tn;
+                            err_t = err_tn;
+                        }
+                    }
+                    replay = amb;
+                }
+                if (replay) {
+                    if (!exact_traj) atomicAdd(a.work + 3, 1ull);  // speculation undecided
+                    ev = replay_interval<MAXR, MACRO>(a, ex, sp, sps, gsv, rl, NS, t0, T, nat, ev0, t_start);
+                    if (ev == ~0ull) {
+                        ev = ev0;
+                        abort_run = true;
+                        break;
+                    }
+                    g = Xoshiro{gsv[0], gsv[NS], gsv[2 * NS], gsv[3 * NS]};
+                    exact_traj |= !Ops::load(c, a, sp, NS);
+                    fire = false;
+                }
+                if (fire) {
+                    ++ev;
+                    Ops::jump(c, a, ex, sp, NS, idx);
+                } else {
+                    // record sample i at t = T
+                    if (!replay) Ops::store(c, a, sp, NS);
+                    int64_t *o = a.out + (size_t)i * a.n_save * a.n_traj + traj;
+                    for (int k = 0; k < a.n_save; ++k) o[(size_t)k * a.n_traj] = sp[a.save_idx[k] * NS];
+                    if (++i < a.n_samples) {
+                        t0 = T;
+                        begin = true;
+                    } else {
+                        if (a.fin_species)
+                            for (int s = 0; s < S; ++s) a.fin_species[traj * S + s] = sp[s * NS];
+                        if (a.fin_t) a.fin_t[traj] = __longlong_as_double((long long)T);
+                        if (a.fin_rng) {
+                            a.fin_rng[traj * 4 + 0] = g.s0;
+                            a.fin_rng[traj * 4 + 1] = g.s1;
+                            a.fin_rng[traj * 4 + 2] = g.s2;
+                            a.fin_rng[traj * 4 + 3] = g.s3;
+                        }
+                        if (a.events) a.events[traj] = ev;
+                        lane_events += ev;
+                        traj = -1;
+                    }
+                }
+            }
+            // ---- park the slot's state
+            if (live) {
+                if (traj >= 0 && !exact_traj) Ops::store(c, a, sp, NS);
+                stw[0 * NS + slot] = g.s0;
+                stw[1 * NS + slot] = g.s1;
+                stw[2 * NS + slot] = g.s2;
+                stw[3 * NS + slot] = g.s3;
+                stw[4 * NS + slot] = t0;
+                stw[5 * NS + slot] = T;
+                stw[6 * NS + slot] = (uint64_t)traj;
+                stw[7 * NS + slot] = ev;
+                stw[8 * NS + slot] = ev0;
+                stw[9 * NS + slot] = (uint64_t)i;
+                stf[0 * NS + slot] = tdf.h;
+                stf[1 * NS + slot] = tdf.l;
+                stf[2 * NS + slot] = err_t;
+                stf[3 * NS + slot] = Tdf.h;
+                stf[4 * NS + slot] = Tdf.l;
+            }
+            stflag[slot] = (live ? kLive : 0u) | (nat ? kNat : 0u) | (exact_traj ? kExactTraj : 0u) |
+                           (begin ? kBegin : 0u);
+            if (abort_run) ctr[1] = 1;
+        }
+        __syncthreads();
+        // ---------------------------------------------------------- compaction
+        // Live slots, in slot order, go to a list; lanes take consecutive
+        // list entries, so warps stay full while trajectories end at
+        // different times.  With more live slots than lanes the starting
+        // entry rotates by one block of lanes per phase.
+        const int warp = tid >> 5, lane = tid & 31, nw = BD >> 5;
+        const int nch = (NS + BD - 1) / BD;
+        for (int ch = 0; ch < nch; ++ch) {
+            const int j = ch * BD + tid;
+            const unsigned int bal = __ballot_sync(0xffffffffu, j < NS && (stflag[j] & kLive) != 0);
+            if (lane == 0) ctr[2 + ch * nw + warp] = __popc(bal);
+        }
+        __syncthreads();
+        int n_live = 0;
+        for (int k = 0; k < nch * nw; ++k) n_live += ctr[2 + k];
+        for (int ch = 0, base = 0; ch < nch; ++ch) {
+            const int j = ch * BD + tid;
+            const bool alive = j < NS && (stflag[j] & kLive) != 0;
+            const unsigned int bal = __ballot_sync(0xffffffffu, alive);
+            int b = base;
+            for (int w = 0; w < warp; ++w) b += ctr[2 + ch * nw + w];
+            if (alive) slot_list[b + __popc(bal & ((1u << lane) - 1u))] = j;
+            for (int w = 0; w < nw; ++w) base += ctr[2 + ch * nw + w];
+        }
+        const bool stop = n_live == 0 || ctr[1] != 0;
+        __syncthreads();
+        if (stop) {
+            if (ctr[1] != 0 && tid == 0) atomicExch(a.work + 2, 1ull);
+            break;
+        }
+        if (n_live <= BD) {
+            slot = tid < n_live ? slot_list[tid] : -1;
+            rot = 0;
+        } else {
+            rot %= (unsigned int)n_live;
+            unsigned int k = rot + (unsigned int)tid;
+            if (k >= (unsigned int)n_live) k -= (unsigned int)n_live;
+            slot = slot_list[k];
+            rot += (unsigned int)BD;
+        }
+        live = slot >= 0;
+        if (live) {
+            g = Xoshiro{stw[0 * NS + slot], stw[1 * NS + slot], stw[2 * NS + slot], stw[3 * NS + slot]};
+            t0 = stw[4 * NS + slot];
+            T = stw[5 * NS + slot];
+            traj = (long long)stw[6 * NS + slot];
+            ev = stw[7 * NS + slot];
+            ev0 = stw[8 * NS + slot];
+            i = (long long)stw[9 * NS + slot];
+            tdf = DF{stf[0 * NS + slot], stf[1 * NS + slot]};
+            err_t = stf[2 * NS + slot];
+            Tdf = DF{stf[3 * NS + slot], stf[4 * NS + slot]};
+            const uint32_t fl = stflag[slot];
+            nat = (fl & kNat) != 0;
+            exact_traj = (fl & kExactTraj) != 0;
+            begin = (fl & kBegin) != 0;
+            if (traj >= 0 && !exact_traj) Ops::load(c, a, spa + slot, NS);
+        }
+        __syncthreads();  // slot flags are rewritten by the next phase
+    }
+    for (int off = 16; off > 0; off >>= 1) lane_events += __shfl_down_sync(0xffffffffu, lane_events, off);
+    if ((tid & 31) == 0 && lane_events) atomicAdd(a.work + 1, lane_events);
+}
+
+}  // namespace rbg

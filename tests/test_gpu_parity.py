@@ -363,3 +363,58 @@ def test_fast_kernel_native_fallback_paths(rb, O):
          .add_macro(0.1, [(1, 1)], [0, -1, 0, 0]).add_macro(1.0, [(2, 1)], [0, 0, -1, 0]))
     ref, ev, _, _ = o.run_ensemble([1, 0, 0, 0], seeds, 0.3, 5)
     np.testing.assert_array_equal(res.counts, ref)
+
+
+def _with_env(name, value, fn):
+    import os
+
+    old = os.environ.get(name)
+    os.environ[name] = value
+    try:
+        return fn()
+    finally:
+        if old is None:
+            del os.environ[name]
+        else:
+            os.environ[name] = old
+
+
+def test_generated_network_kernel_matches_oracle(rb, O):
+    # Networks compiled at run time (counts in registers, reactions unrolled)
+    # against the oracle, bit for bit, and against the descriptor kernel.
+    seeds = _seeds(3000, 51)
+    jit = _with_env("RB_JIT", "1", lambda: _dimer(rb).run_ensemble([1, 0, 0, 0], seeds, 1.0, 20))
+    ref, ev, _, _ = O.dimer_net().run_ensemble([1, 0, 0, 0], seeds, 1.0, 20)
+    assert jit.stats["mapping"] == 4
+    np.testing.assert_array_equal(jit.counts, ref)
+    np.testing.assert_array_equal(jit.events, ev)
+    # per-trajectory rates, with some outside the float-pair range (exact re-runs)
+    n = 500
+    rng = np.random.default_rng(5)
+    rates = np.stack([10 ** rng.uniform(-5, -3, n), 10 ** rng.uniform(-3, -1, n)], axis=1)
+    rates[::50, 0] = 1e-30
+    rates[::77, 1] = np.nan
+    jit = _with_env("RB_JIT", "1", lambda: _sir(rb).run_ensemble([999, 1, 0], seeds[:n], 200.0, 40, rates=rates))
+    ref, ev, _, _ = O.sir_net().run_ensemble([999, 1, 0], seeds[:n], 200.0, 40, rates=rates)
+    assert jit.stats["mapping"] == 4
+    np.testing.assert_array_equal(jit.counts, ref)
+    np.testing.assert_array_equal(jit.events, ev)
+    # counts that go negative (A consumed at a rate set by B)
+    net = rb.Network(2)
+    net.add_reaction(rb.Rate.lma(1.0, [0, 1]), [-1, 0])
+    net.add_reaction(rb.Rate.lma(0.5, [1, 0]), [0, 1])
+    onet = O.OracleNet(2).add_lma(1.0, [0, 1], [-1, 0]).add_lma(0.5, [1, 0], [0, 1])
+    jit = _with_env("RB_JIT", "1", lambda: net.run_ensemble([3, 5], seeds[:400], 3.0, 6))
+    ref, ev, _, _ = onet.run_ensemble([3, 5], seeds[:400], 3.0, 6)
+    np.testing.assert_array_equal(jit.counts, ref)
+    np.testing.assert_array_equal(jit.events, ev)
+    # macro arithmetic
+    D = rb.define_system(DIMER_DSL)
+    d = D.with_parameters(25.0, 1000.0, 0.001, 0.1, 1.0)
+    d.gene = 1
+    res = _with_env("RB_JIT", "1", lambda: d.run_ensemble(seeds[:600], 0.5, 10))
+    o = (O.OracleNet(4, macro=True).add_macro(25.0, [(0, 1)], [0, 1, 0, 0])
+         .add_macro(1000.0, [(1, 1)], [0, 0, 1, 0]).add_macro(0.001, [(2, 2)], [0, 0, -2, 1])
+         .add_macro(0.1, [(1, 1)], [0, -1, 0, 0]).add_macro(1.0, [(2, 1)], [0, 0, -1, 0]))
+    ref, ev, _, _ = o.run_ensemble([1, 0, 0, 0], seeds[:600], 0.5, 10)
+    np.testing.assert_array_equal(res.counts, ref)

@@ -179,3 +179,49 @@ def test_no_oracle_import_in_product():
         if p.suffix in (".py", ".cpp", ".cu", ".cuh", ".hpp", ".h"):
             text = p.read_text(encoding="utf-8")
             assert "oracle" not in text.lower() or p.name == "build.py", p
+
+
+def _dimer_net(rb):
+    net = rb.Network(4)
+    for k, e, d in [(25.0, [1, 0, 0, 0], [0, 1, 0, 0]), (1000.0, [0, 1, 0, 0], [0, 0, 1, 0]),
+                    (0.001, [0, 0, 2, 0], [0, 0, -2, 1]), (0.1, [0, 1, 0, 0], [0, -1, 0, 0]),
+                    (1.0, [0, 0, 1, 0], [0, 0, -1, 0])]:
+        net.add_reaction(rb.Rate.lma(k, e), d)
+    return net
+
+
+def test_generated_network_source(rb):
+    # The generator unrolls every reaction (falling factorial in the written
+    # order) and turns each jump into per-species selects.
+    import ctypes as C
+    import importlib
+
+    L = importlib.import_module("rebop_gb300._lib").lib
+    buf = C.create_string_buffer(1 << 16)
+    net = _dimer_net(rb)
+    assert L.rbg_internal_jit_source(net._h, buf, 1 << 16) == 0
+    src = buf.value.decode()
+    assert "kMaxR = 5" in src and "int32_t n[4]" in src
+    assert "max(c.n[2] - 1, 0)" in src
+    assert "c.n[2] += (idx == 1 ? 1 : 0) + (idx == 2 ? -2 : 0) + (idx == 4 ? -1 : 0);" in src
+    big = rb.Network(40)
+    big.add_reaction(rb.Rate.lma(1.0, [1] + [0] * 39), [-1] + [0] * 39)
+    assert L.rbg_internal_jit_source(big._h, buf, 1 << 16) == 5  # RB_ERR_UNSUPPORTED
+
+
+def test_generated_network_compiles(rb, tmp_path, monkeypatch):
+    # NVRTC compiles the generated kernel for sm_103a without a GPU.
+    import ctypes as C
+    import importlib
+    import shutil
+
+    if shutil.which("nvcc") is None:
+        pytest.skip("no CUDA toolkit")
+    monkeypatch.setenv("RB_JIT_CACHE", str(tmp_path))
+    L = importlib.import_module("rebop_gb300._lib").lib
+    n = C.c_uint64()
+    net = _dimer_net(rb)
+    rc = L.rbg_internal_jit_compile(net._h, C.byref(n))
+    assert rc == 0, importlib.import_module("rebop_gb300._lib").last_error()
+    assert n.value > 10000
+    assert len(list(tmp_path.glob("net_*.cubin"))) == 1
