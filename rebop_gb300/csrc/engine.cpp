@@ -241,7 +241,7 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     const bool want_fast = pref && std::strcmp(pref, "fast") == 0;
     const int spec_grid = (int)std::max<int64_t>(
         1, std::min<int64_t>(ctx->sm_count, (r.n_traj + ssa_spec_block() - 1) / ssa_spec_block()));
-    const int spec_slots = ssa_spec_slots(a, spec_grid, ctx->smem_optin);
+    const int spec_slots = ssa_spec_slots(a, spec_grid, ctx->smem_optin, ssa_spec_block());
     const bool spec = !want_generic && !want_fast && r.times_ok && r.t_last < 0x1p60 &&
                       ssa_spec_supported(a, p.max_order) && spec_slots > 0;
     const bool fast = !spec && !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
@@ -255,6 +255,7 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     if (spec) {
         block = ssa_spec_block();
         a.n_slots = spec_slots;
+        if (const char *ph = std::getenv("RB_SPEC_PHASE")) a.phase_steps = std::atoi(ph);
         smem = ssa_spec_smem(a, spec_slots);
         per_sm = ssa_spec_occupancy(a, block, smem);
     } else if (fast) {
@@ -283,8 +284,21 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
         const char *jit = std::getenv("RB_JIT");
         const bool want = jit ? std::strcmp(jit, "0") != 0 : r.n_traj >= 4096;
         if (want) {
-            jk = jit_kernel(p);
-            if (!jk && jit && std::strcmp(jit, "1") == 0) return false;
+            // generated kernels may run larger blocks (fewer registers per lane)
+            int jb = 512;
+            if (const char *e = std::getenv("RB_JIT_BLOCK")) jb = std::max(32, std::min(1024, std::atoi(e) / 32 * 32));
+            const int jgrid = (int)std::max<int64_t>(1, std::min<int64_t>(ctx->sm_count, (r.n_traj + jb - 1) / jb));
+            const int jslots = ssa_spec_slots(a, jgrid, ctx->smem_optin, jb);
+            if (jslots > 0) {
+                jk = jit_kernel(p, jb);
+                if (!jk && jit && std::strcmp(jit, "1") == 0) return false;
+                if (jk) {
+                    block = jb;
+                    grid = jgrid;
+                    a.n_slots = jslots;
+                    smem = ssa_spec_smem(a, jslots);
+                }
+            }
         }
     }
     if (timed && !cuda_ok(cudaEventRecord(dn.ev_start, stream), "cudaEventRecord")) return false;

@@ -67,9 +67,12 @@ struct SsaArgs {
     // Largest sum of reactant orders over the reactions (float-pair error bound).
     int32_t max_mults;
 
-    // Speculative kernel: trajectory slots per block (a multiple of 32, at
-    // least the block size).
+    // Speculative kernel: trajectory slots per block (the same number for
+    // every warp, at least one per lane).
     int32_t n_slots;
+    // Speculative kernel: steps between two compactions of a warp's slots
+    // (0: the default).
+    int32_t phase_steps;
 };
 
 // Launch the thread-per-trajectory kernel; returns a cudaError_t value.
@@ -90,10 +93,10 @@ int launch_ssa_fast(const SsaArgs &a, int block, int grid, size_t smem, void *st
 bool ssa_spec_supported(const SsaArgs &a, int max_order);
 int ssa_spec_block();
 size_t ssa_spec_smem(const SsaArgs &a, int slots);
-// Slots per block for a launch of `grid` blocks: enough for every trajectory
-// to be resident at once when shared memory allows; 0 if not even one slot
-// per lane fits in smem_limit bytes.
-int ssa_spec_slots(const SsaArgs &a, int grid, size_t smem_limit);
+// Slots per block for a launch of `grid` blocks of `block` lanes: enough for
+// every trajectory to be resident at once when shared memory allows; 0 if not
+// even one slot per lane fits in smem_limit bytes.
+int ssa_spec_slots(const SsaArgs &a, int grid, size_t smem_limit, int block);
 int ssa_spec_occupancy(const SsaArgs &a, int block, size_t smem);
 int launch_ssa_spec(const SsaArgs &a, int block, int grid, size_t smem, void *stream);
 

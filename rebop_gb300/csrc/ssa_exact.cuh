@@ -77,14 +77,14 @@ __device__ __forceinline__ uint64_t exp1_emul(Xoshiro &g, const ExactTables &m, 
 // reaction fires (index and new clock out); commits the draws it consumes.
 template <int MAXR, bool MACRO>
 __device__ __noinline__ bool native_step(const SsaArgs &a, const ExactTables &m, Xoshiro &g, const int64_t *sp,
-                                         const uint64_t *rl, int BD, uint64_t t_bits, uint64_t T_bits, int &idx,
+                                         const uint64_t *rl, int RS, int BD, uint64_t t_bits, uint64_t T_bits, int &idx,
                                          uint64_t &tn_bits) {
     double cum[MAXR];
     double total = 0.0;
 #pragma unroll
     for (int r = 0; r < MAXR; ++r) {
         if (r < a.R) {
-            double acc = __longlong_as_double((long long)rl[r * BD]);
+            double acc = __longlong_as_double((long long)rl[r * RS]);
             for (int p = 0; p < a.P; ++p) {
                 const int f = m.fac[r * a.P + p];
                 const int o = f >> 16;
@@ -138,7 +138,7 @@ __device__ __forceinline__ uint64_t hot_add(uint64_t a, uint64_t b, bool &bad) {
 // the jump and the clock.  `nat` forces native binary64.
 template <int MAXR, bool MACRO, bool ADDN>
 __device__ __forceinline__ bool exact_step(const SsaArgs &a, const ExactTables &m, const int64_t *sp,
-                                           const uint64_t *rl, int BD, Xoshiro &g, uint64_t t, uint64_t T, bool nat,
+                                           const uint64_t *rl, int RS, int BD, Xoshiro &g, uint64_t t, uint64_t T, bool nat,
                                            int &idx, uint64_t &tn) {
     const int R = a.R, P = a.P;
     uint64_t cum[MAXR];
@@ -147,7 +147,7 @@ __device__ __forceinline__ bool exact_step(const SsaArgs &a, const ExactTables &
 #pragma unroll
     for (int r = 0; r < MAXR; ++r) {
         if (r < R) {
-            uint64_t acc = rl[r * BD];
+            uint64_t acc = rl[r * RS];
             for (int p = 0; p < P; ++p) {
                 const int f = m.fac[r * P + p];
                 const int o = f >> 16;
@@ -193,7 +193,7 @@ __device__ __forceinline__ bool exact_step(const SsaArgs &a, const ExactTables &
             if (r < R) idx += (cum[r] < chosen) ? 1 : 0;
     }
     bad = bad || (pos && bad_t) || (fire && bad_c);
-    if (bad) return native_step<MAXR, MACRO>(a, m, g, sp, rl, BD, t, T, idx, tn);
+    if (bad) return native_step<MAXR, MACRO>(a, m, g, sp, rl, RS, BD, t, T, idx, tn);
     g = fire ? g3 : (pos ? g2 : g);
     return fire;
 }

@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(128, 6) ssa_fast_kernel(const __grid_constant_
         }
         int idx;
         uint64_t tn;
-        const bool fire = exact_step<MAXR, MACRO, ADD_NATIVE>(a, m.ex, sp, rl, BD, g, t, T, nat, idx, tn);
+        const bool fire = exact_step<MAXR, MACRO, ADD_NATIVE>(a, m.ex, sp, rl, BD, BD, g, t, T, nat, idx, tn);
         if (fire) {
             t = tn;
             ++ev;

@@ -152,7 +152,7 @@ bool jit_supported(const Packed &p) {
     return true;
 }
 
-std::string jit_net_source(const Packed &p) {
+std::string jit_net_source(const Packed &p, int block) {
     const int S = p.S, R = p.R;
     std::ostringstream o;
     o << "// generated network operations: " << S << " species, " << R << " reactions\n";
@@ -178,12 +178,12 @@ std::string jit_net_source(const Packed &p) {
     o << "    }\n";
     // props: every reaction unrolled; counts outside [0, 2^23) leave the
     // float-pair range (one OR over all counts covers negative ones too)
-    o << "    __device__ static bool props(const SsaArgs &, const ExactTables &, const Counts &c, const int64_t *,\n"
-         "                                 const float2 *rf, int NS, DF *cum, DF &tot) {\n";
+    o << "    __device__ static bool props(const SsaArgs &, const ExactTables &, const Counts &c, const int64_t *, int,\n"
+         "                                 const float2 *rf, int RS, DF *cum, DF &tot) {\n";
     o << "        uint32_t m = 0;\n";
     for (int s = 0; s < S; s++) o << "        m |= (uint32_t)c.n[" << s << "];\n";
     for (int r = 0; r < R; r++) {
-        o << "        {\n            const float2 k = rf[" << r << " * NS];\n            DF acc{k.x, k.y};\n";
+        o << "        {\n            const float2 k = rf[" << r << " * RS];\n            DF acc{k.x, k.y};\n";
         for (int f = 0; f < p.P; f++) {
             const int32_t ord = p.fac_ord[(size_t)r * p.P + f];
             const int32_t sp = p.fac_sp[(size_t)r * p.P + f];
@@ -220,7 +220,7 @@ std::string jit_net_source(const Packed &p) {
         o << ";\n";
     }
     o << "    }\n};\n\n}  // namespace rbg\n\n";
-    o << "extern \"C\" __global__ void __launch_bounds__(rbg::kSpecBlock, 1)\n"
+    o << "extern \"C\" __global__ void __launch_bounds__(" << block << ", 1)\n"
          "rbg_net_kernel(const __grid_constant__ rbg::SsaArgs a) {\n    rbg::spec_body<rbg::NetOps>(a);\n}\n";
     return o.str();
 }
@@ -277,9 +277,9 @@ bool compile_image(const std::string &src, uint64_t key, Nvrtc *nv, std::string 
 
 }  // namespace
 
-bool jit_compile(const Packed &p, size_t *image_bytes) {
+bool jit_compile(const Packed &p, int block, size_t *image_bytes) {
     std::lock_guard<std::mutex> lk(g_mu);
-    const std::string src = jit_net_source(p);
+    const std::string src = jit_net_source(p, block);
     Nvrtc *nv = nvrtc();
     std::string image;
     if (!compile_image(src, image_key(src, nv), nv, image)) return false;
@@ -287,7 +287,7 @@ bool jit_compile(const Packed &p, size_t *image_bytes) {
     return true;
 }
 
-const void *jit_kernel(const Packed &p) {
+const void *jit_kernel(const Packed &p, int block) {
     std::lock_guard<std::mutex> lk(g_mu);
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -295,7 +295,7 @@ const void *jit_kernel(const Packed &p) {
         set_error("cudaGetDevice failed");
         return nullptr;
     }
-    const std::string src = jit_net_source(p);
+    const std::string src = jit_net_source(p, block);
     Nvrtc *nv = nvrtc();
     const uint64_t key = image_key(src, nv);
     auto it = g_loaded.find({dev, key});

@@ -13,14 +13,15 @@ namespace rbg {
 // Networks the generator covers: 1..16 species, 1..32 reactions, jumps of
 // magnitude below 2^23.
 bool jit_supported(const Packed &p);
-// CUDA source of the speculative kernel specialised for the network.
-std::string jit_net_source(const Packed &p);
+// CUDA source of the speculative kernel specialised for the network, for
+// blocks of `block` lanes (a multiple of 32, at most 1024).
+std::string jit_net_source(const Packed &p, int block);
 // Compile (or find in the disk cache) the network's kernel image without
 // loading it; false with the error set on failure.
-bool jit_compile(const Packed &p, size_t *image_bytes);
+bool jit_compile(const Packed &p, int block, size_t *image_bytes);
 // The compiled kernel for the current device (compiled on first use); null
 // with the error set on failure.
-const void *jit_kernel(const Packed &p);
+const void *jit_kernel(const Packed &p, int block);
 int launch_ssa_jit(const void *kern, const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st);
 
 }  // namespace rbg

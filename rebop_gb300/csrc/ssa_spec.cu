@@ -50,16 +50,20 @@ bool ssa_spec_supported(const SsaArgs &a, int max_order) {
     return a.R <= 16 && a.S < 65536 && max_order < 32768;
 }
 
-size_t ssa_spec_smem(const SsaArgs &a, int slots) { return spec_smem_bytes(a.S, a.R, a.P, a.Q, slots); }
+size_t ssa_spec_smem(const SsaArgs &a, int slots) {
+    return spec_smem_bytes(a.S, a.R, a.P, a.Q, slots, a.rate_stride != 0);
+}
 
-int ssa_spec_slots(const SsaArgs &a, int grid, size_t smem_limit) {
-    if (spec_smem_bytes(a.S, a.R, a.P, a.Q, kSpecBlock) > smem_limit) return 0;
-    int64_t want = (a.n_traj + grid - 1) / (grid > 0 ? grid : 1);
-    want = (want + 31) / 32 * 32;
-    int slots = kSpecBlock;
-    while (slots < want && slots + 32 <= kSpecMaxSlots &&
-           spec_smem_bytes(a.S, a.R, a.P, a.Q, slots + 32) <= smem_limit)
-        slots += 32;
+int ssa_spec_slots(const SsaArgs &a, int grid, size_t smem_limit, int block) {
+    // every warp owns the same number of slots (at least one per lane)
+    const int warps = block / 32;
+    const bool per_traj = a.rate_stride != 0;
+    if (spec_smem_bytes(a.S, a.R, a.P, a.Q, block, per_traj) > smem_limit) return 0;
+    const int64_t want = (a.n_traj + grid - 1) / (grid > 0 ? grid : 1);
+    int slots = block;
+    while (slots < want && slots + warps <= kSpecMaxSlots &&
+           spec_smem_bytes(a.S, a.R, a.P, a.Q, slots + warps, per_traj) <= smem_limit)
+        slots += warps;
     return slots;
 }
 

@@ -105,6 +105,40 @@ __device__ __forceinline__ DF df_from_double(double v) {
     return DF{h, __double2float_rn(__dsub_rn(v, (double)h))};
 }
 
+// Clock as an unevaluated sum of three floats.  Adding a float pair is exact
+// up to the rounding of the smallest part, so the clock keeps the reference's
+// binary64 clock to within that binary64 arithmetic's own rounding.
+struct TF {
+    float h, m, l;
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Exact triple of a double v = 0 or 2^-60 <= v < 2^60.
+__device__ __forceinline__ TF tf_from_double(double v) {
+    const float h = __double2float_rz(v);
+    const double r1 = __dsub_rn(v, (double)h);
+    const float m = __double2float_rz(r1);
+    return TF{h, m, __double2float_rn(__dsub_rn(r1, (double)m))};
+}
+
+// t + q for t, q >= 0 (t with |m| <= ulp(h)/2, q normalised).  Every step is
+// an error-free transformation except the two roundings into the low part,
+// which are bounded by 2^-24 (|l| + |e2 + e3|).
+__device__ __forceinline__ TF tf_add(TF t, DF q) {
+    float s, e1, m, e2, m2, e3;
+    two_sum(t.h, q.h, s, e1);
+    two_sum(t.m, q.l, m, e2);
+    two_sum(m, e1, m2, e3);
+    const float l = __fadd_rn(t.l, __fadd_rn(e2, e3));
+    const float h = __fadd_rn(s, m2);  // |m2| <= |s|: fast two-sum
+    return TF{h, __fsub_rn(m2, __fsub_rn(h, s)), l};
+}
+
 // Exp1 draw as a float pair, consuming the stream exactly as the reference
 // does (the wedge test is decided exactly, see wedge_accept).  xerr bounds
 // |x - rebop's binary64 draw|.
@@ -142,7 +176,7 @@ __device__ __forceinline__ bool spec_rate_ok(uint64_t v) {
 }
 
 constexpr int kSpecBlock = 512;   // lanes per block; one block per SM
-constexpr int kSpecPhase = 128;   // steps between two compactions of the block
+constexpr int kSpecPhase = 128;   // default steps between two compactions of a warp
 constexpr int kSpecMaxSlots = 2048;
 
 // Shared memory: block tables, then per-slot columns [field][slots].  A slot
@@ -151,14 +185,16 @@ constexpr int kSpecMaxSlots = 2048;
 // then the lanes rotate over the live slots, so every resident trajectory
 // advances at the same pace and no second wave of late starters is left to
 // run on a nearly empty SM.
-__host__ __device__ inline size_t spec_smem_bytes(int S, int R, int P, int Q, int slots) {
+// Rates live in per-slot columns when every trajectory has its own, else
+// once for the block.
+__host__ __device__ inline size_t spec_smem_bytes(int S, int R, int P, int Q, int slots, bool rate_per_traj) {
     size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;  // zxk, zf, zd, xdf
     b += 8 * (size_t)R * Q;                             // jd
-    b += 16 * (size_t)R * slots;                        // exact rate bits, float-pair rates
+    b += 16 * (size_t)R * (rate_per_traj ? slots : 1);  // exact rate bits, float-pair rates
     b += 16 * (size_t)S * slots;                        // counts, counts at interval start
     b += 32 * (size_t)slots;                            // generator at interval start
     b += 80 * (size_t)slots;                            // 10 state words
-    b += 24 * (size_t)slots;                            // 5 float state words, flags
+    b += 32 * (size_t)slots;                            // 7 float state words, flags
     b += 4 * (size_t)slots + 512;                       // slot list, block counters
     b += 4 * ((size_t)R * P + (size_t)R * Q);           // fac, jsp
     return (b + 15) & ~(size_t)15;
@@ -172,7 +208,7 @@ __host__ __device__ inline size_t spec_smem_bytes(int S, int R, int P, int Q, in
 template <int MAXR, bool MACRO>
 __device__ __noinline__ unsigned long long replay_interval(const SsaArgs &a, const ExactTables &ex, int64_t *sp,
                                                            const int64_t *sps, uint64_t *gsv, const uint64_t *rl,
-                                                           int BD, uint64_t t0, uint64_t T, bool nat,
+                                                           int RS, int BD, uint64_t t0, uint64_t T, bool nat,
                                                            unsigned long long ev0, int64_t t_start) {
     for (int s = 0; s < a.S; ++s) sp[s * BD] = sps[s * BD];
     Xoshiro h{gsv[0], gsv[BD], gsv[2 * BD], gsv[3 * BD]};
@@ -182,7 +218,7 @@ __device__ __noinline__ unsigned long long replay_interval(const SsaArgs &a, con
         if ((n & 255u) == 0 && global_ns() - t_start > a.budget_ns) return ~0ull;
         int ix;
         uint64_t tx;
-        if (!exact_step<MAXR, MACRO, true>(a, ex, sp, rl, BD, h, t, T, nat, ix, tx)) break;
+        if (!exact_step<MAXR, MACRO, true>(a, ex, sp, rl, RS, BD, h, t, T, nat, ix, tx)) break;
         t = tx;
         ++e;
         if (ix < a.R)
@@ -220,13 +256,13 @@ struct TableOps {
     // Float-pair propensities and running sums; true if a count leaves the
     // float-pair range (then the step is undecided).
     __device__ static bool props(const SsaArgs &a, const ExactTables &ex, const Counts &, const int64_t *sp,
-                                 const float2 *rf, int NS, DF *cum, DF &tot) {
+                                 int NS, const float2 *rf, int RS, DF *cum, DF &tot) {
         bool amb = false;
         tot = DF{0.f, 0.f};
 #pragma unroll
         for (int r = 0; r < MAXR; ++r) {
             if (r < a.R) {
-                const float2 k = rf[r * NS];
+                const float2 k = rf[r * RS];
                 DF acc{k.x, k.y};
                 for (int p = 0; p < a.P; ++p) {
                     const int f = ex.fac[r * a.P + p];
@@ -255,14 +291,17 @@ struct TableOps {
     }
 };
 
-// The kernel body: one block per SM, `a.n_slots` trajectory slots rotated
-// over the block's lanes in phases of kSpecPhase steps.
+// The kernel body: one block per SM; each warp rotates its lanes over its own
+// `a.n_slots / warps` trajectory slots in phases of `a.phase_steps` steps.
 template <class Ops>
 __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     constexpr int MAXR = Ops::kMaxR;
     constexpr bool MACRO = Ops::kMacro;
     const int BD = blockDim.x, tid = threadIdx.x;
-    const int NS = a.n_slots;  // slots per block, a multiple of 32, >= BD
+    const int NS = a.n_slots;  // slots per block: a multiple of the warps, >= 32 per warp
+    const int warp = tid >> 5, lane = tid & 31;
+    const int SPW = NS / (BD >> 5);  // slots per warp
+    const int wbase = warp * SPW;
     const int S = a.S, R = Ops::nr(a), P = a.P, Q = a.Q;
 
     // ---- shared memory: block tables, then per-slot columns
@@ -271,16 +310,18 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     uint64_t *zd = zf + 257;
     float2 *xdf = reinterpret_cast<float2 *>(zd + 256);
     int64_t *jd = reinterpret_cast<int64_t *>(xdf + 256);
+    const bool rate_cols = a.rate_stride != 0;  // per-slot rate columns
+    const int RS = rate_cols ? NS : 1;           // stride between two reactions' rates
     uint64_t *rate = reinterpret_cast<uint64_t *>(jd + (size_t)R * Q);
-    float2 *rdf = reinterpret_cast<float2 *>(rate + (size_t)R * NS);
-    int64_t *spa = reinterpret_cast<int64_t *>(rdf + (size_t)R * NS);
+    float2 *rdf = reinterpret_cast<float2 *>(rate + (size_t)R * RS);
+    int64_t *spa = reinterpret_cast<int64_t *>(rdf + (size_t)R * RS);
     int64_t *spsa = spa + (size_t)S * NS;
     uint64_t *gsva = reinterpret_cast<uint64_t *>(spsa + (size_t)S * NS);
     uint64_t *stw = gsva + 4 * (size_t)NS;                         // [10][NS]
-    float *stf = reinterpret_cast<float *>(stw + 10 * (size_t)NS);  // [5][NS]
-    uint32_t *stflag = reinterpret_cast<uint32_t *>(stf + 5 * (size_t)NS);
+    float *stf = reinterpret_cast<float *>(stw + 10 * (size_t)NS);  // [7][NS]
+    uint32_t *stflag = reinterpret_cast<uint32_t *>(stf + 7 * (size_t)NS);
     int32_t *slot_list = reinterpret_cast<int32_t *>(stflag + NS);
-    int32_t *ctr = slot_list + NS;  // [1] abort, [2..] live slots per (chunk, warp)
+    int32_t *ctr = slot_list + NS;  // [1] abort flag
     int32_t *fac = ctr + 128;
     int32_t *jsp = fac + (size_t)R * P;
     load_exact_tables(a, zxk, zf, zd, fac, jsp, jd);
@@ -288,6 +329,13 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
         const double v = a.zig[kZigOffXdf + k];
         xdf[k] = *reinterpret_cast<const float2 *>(&v);
     }
+    if (!a.rate_stride)
+        for (int r = tid; r < R; r += BD) {
+            const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[r]);
+            rate[r] = rb;
+            const DF d = spec_rate_ok(rb) ? df_from_double(__longlong_as_double((long long)rb)) : DF{0.f, 0.f};
+            rdf[r] = make_float2(d.h, d.l);
+        }
     // every slot starts live and empty (no trajectory taken yet)
     for (int k = tid; k < NS; k += BD) {
         stflag[k] = kLive;
@@ -301,16 +349,18 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     const float c_q = G + 6.0f * kGamma;                     // relative bound of Exp1/total
     const float c_sel = 2.0f * G + 8.0f * kGamma;            // choice margin / total
     const int64_t t_start = global_ns();
+    const int phase_steps = a.phase_steps > 0 ? a.phase_steps : kSpecPhase;
     unsigned int tick = 0, rot = 0;
     unsigned long long lane_events = 0;
 
     // ---- this lane's slot and its state, cached in registers during a phase
-    int slot = tid;
+    int slot = wbase + lane;
+    int32_t *const wlist = slot_list + wbase;
     typename Ops::Counts c{};
     Xoshiro g{0, 0, 0, 0};
     uint64_t t0 = 0, T = 0;
-    DF Tdf{0.f, 0.f}, tdf{0.f, 0.f};
-    float err_t = 0.f;
+    TF Tc{0.f, 0.f, 0.f}, tc{0.f, 0.f, 0.f};  // sample time, clock
+    float err_t = 0.f;                         // bound on |clock - reference clock|
     long long i = 0, traj = -1;
     unsigned long long ev = 0, ev0 = 0;
     bool live = true, nat = false, exact_traj = false, begin = false, abort_run = false;
@@ -321,9 +371,9 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
             int64_t *const sp = spa + slot;
             int64_t *const sps = spsa + slot;
             uint64_t *const gsv = gsva + slot;
-            uint64_t *const rl = rate + slot;
-            float2 *const rf = rdf + slot;
-            for (int step = 0; step < kSpecPhase && live; ++step) {
+            uint64_t *const rl = rate + (rate_cols ? slot : 0);
+            float2 *const rf = rdf + (rate_cols ? slot : 0);
+            for (int step = 0; step < phase_steps && live; ++step) {
                 if (traj < 0) {
                     // take the next trajectory into this slot
                     traj = (long long)atomicAdd(a.work, 1ull);
@@ -347,11 +397,13 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                     exact_traj = (t0 >> 52) > 1023 + 60;
                     for (int r = 0; r < R; ++r) {
                         const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[traj * a.rate_stride + r]);
-                        rl[r * NS] = rb;
                         nat |= !emul_domain(rb);
                         exact_traj |= !spec_rate_ok(rb);
-                        const DF d = df_from_double(__longlong_as_double((long long)rb));
-                        rf[r * NS] = make_float2(d.h, d.l);
+                        if (rate_cols) {
+                            rl[r * RS] = rb;
+                            const DF d = df_from_double(__longlong_as_double((long long)rb));
+                            rf[r * RS] = make_float2(d.h, d.l);
+                        }
                     }
                     exact_traj |= nat;
                     exact_traj |= !Ops::load(c, a, sp, NS);
@@ -362,9 +414,9 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                 if (begin) {
                     // a sample interval starts at t0: save what a re-run needs
                     T = (uint64_t)__double_as_longlong(a.sample_t[i]);
-                    Tdf = df_from_double(__longlong_as_double((long long)T));
-                    tdf = df_from_double(__longlong_as_double((long long)t0));
-                    err_t = kGamma * tdf.h;
+                    Tc = tf_from_double(__longlong_as_double((long long)T));
+                    tc = tf_from_double(__longlong_as_double((long long)t0));
+                    err_t = 0.f;
                     if (exact_traj)
                         for (int s = 0; s < S; ++s) sps[s * NS] = sp[s * NS];
                     else
@@ -390,19 +442,29 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                     // undecided step re-runs the interval from its saved state.
                     DF cum[MAXR];
                     DF tot;
-                    bool amb = Ops::props(a, ex, c, sp, rf, NS, cum, tot);
+                    bool amb = Ops::props(a, ex, c, sp, NS, rf, RS, cum, tot);
                     if (tot.h > 0.0f) {
                         amb |= tot.h < 0x1p-90f || tot.h > 0x1p90f;
                         float xerr;
                         const DF x = exp1_df(g, ex, xdf, xerr);
                         const float r = rcp_approx(tot.h);
                         const DF q = df_div(x, tot, r);
-                        const DF tn = df_add(tdf, q);
-                        const float err_tn = err_t + 1.001f * xerr * r + c_q * q.h + 2.0f * kGamma * tn.h;
-                        const float d = __fadd_rn(__fsub_rn(Tdf.h, tn.h), __fsub_rn(Tdf.l, tn.l));
-                        const float mt = err_tn + 4.0f * kGamma * Tdf.h;
-                        fire = d > mt;
-                        amb |= !(fire || d < -mt) || !(err_tn < 3.0e38f);
+                        const TF tn = tf_add(tc, q);
+                        // error bound, rounded up: previous bound, Exp1/total
+                        // against the reference's quotient, the reference's
+                        // rounding of its clock add, the low part's roundings
+                        float err_tn = __fadd_ru(err_t, __fmul_ru(c_q, q.h));
+                        err_tn = __fadd_ru(err_tn, __fmul_ru(__fmul_ru(xerr, r), 1.001f));
+                        err_tn = __fadd_ru(err_tn, __fmul_ru(0x1p-52f, tn.h));
+                        err_tn = __fadd_ru(err_tn, __fmul_ru(0x1p-23f, fabsf(tn.l)));
+                        // T - tn: the high difference is exact near T, the
+                        // rest is below 2^-46 max(T, tn) off
+                        const float d = __fadd_rn(__fsub_rn(Tc.h, tn.h),
+                                                  __fadd_rn(__fsub_rn(Tc.m, tn.m), __fsub_rn(Tc.l, tn.l)));
+                        const float mt = __fadd_ru(err_tn, __fmul_ru(0x1p-44f, fmaxf(Tc.h, tn.h)));
+                        const float dd = __fmul_rn(d, 1.0f - 0x1p-22f);
+                        fire = dd > mt;
+                        amb |= !(fire || dd < -mt) || !(err_tn < 1.0e30f) || q.h < 0x1p-100f;
                         if (fire && !amb) {
                             const DF ch = df_mul(tot, df_u53(xo_next(g) >> 11));
                             const float msel = c_sel * tot.h;
@@ -415,7 +477,7 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                                     amb |= fabsf(dr) <= msel;
                                 }
                             }
-                            tdf = tn;
+                            tc = tn;
                             err_t = err_tn;
                         }
                     }
@@ -423,7 +485,7 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                 }
                 if (replay) {
                     if (!exact_traj) atomicAdd(a.work + 3, 1ull);  // speculation undecided
-                    ev = replay_interval<MAXR, MACRO>(a, ex, sp, sps, gsv, rl, NS, t0, T, nat, ev0, t_start);
+                    ev = replay_interval<MAXR, MACRO>(a, ex, sp, sps, gsv, rl, RS, NS, t0, T, nat, ev0, t_start);
                     if (ev == ~0ull) {
                         ev = ev0;
                         abort_run = true;
@@ -473,56 +535,48 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                 stw[7 * NS + slot] = ev;
                 stw[8 * NS + slot] = ev0;
                 stw[9 * NS + slot] = (uint64_t)i;
-                stf[0 * NS + slot] = tdf.h;
-                stf[1 * NS + slot] = tdf.l;
-                stf[2 * NS + slot] = err_t;
-                stf[3 * NS + slot] = Tdf.h;
-                stf[4 * NS + slot] = Tdf.l;
+                stf[0 * NS + slot] = tc.h;
+                stf[1 * NS + slot] = tc.m;
+                stf[2 * NS + slot] = tc.l;
+                stf[3 * NS + slot] = err_t;
+                stf[4 * NS + slot] = Tc.h;
+                stf[5 * NS + slot] = Tc.m;
+                stf[6 * NS + slot] = Tc.l;
             }
             stflag[slot] = (live ? kLive : 0u) | (nat ? kNat : 0u) | (exact_traj ? kExactTraj : 0u) |
                            (begin ? kBegin : 0u);
             if (abort_run) ctr[1] = 1;
         }
-        __syncthreads();
+        __syncwarp();
         // ---------------------------------------------------------- compaction
-        // Live slots, in slot order, go to a list; lanes take consecutive
-        // list entries, so warps stay full while trajectories end at
-        // different times.  With more live slots than lanes the starting
-        // entry rotates by one block of lanes per phase.
-        const int warp = tid >> 5, lane = tid & 31, nw = BD >> 5;
-        const int nch = (NS + BD - 1) / BD;
-        for (int ch = 0; ch < nch; ++ch) {
-            const int j = ch * BD + tid;
-            const unsigned int bal = __ballot_sync(0xffffffffu, j < NS && (stflag[j] & kLive) != 0);
-            if (lane == 0) ctr[2 + ch * nw + warp] = __popc(bal);
-        }
-        __syncthreads();
+        // Each warp owns slots [wbase, wbase + SPW) and never waits for
+        // another warp: its live slots, in slot order, go to its list; lanes
+        // take consecutive list entries, so the warp stays full while
+        // trajectories end at different times.  With more live slots than
+        // lanes the starting entry rotates by 32 per phase.
         int n_live = 0;
-        for (int k = 0; k < nch * nw; ++k) n_live += ctr[2 + k];
-        for (int ch = 0, base = 0; ch < nch; ++ch) {
-            const int j = ch * BD + tid;
-            const bool alive = j < NS && (stflag[j] & kLive) != 0;
+        for (int c0 = 0; c0 < SPW; c0 += 32) {
+            const int j = c0 + lane;
+            const bool alive = j < SPW && (stflag[wbase + j] & kLive) != 0;
             const unsigned int bal = __ballot_sync(0xffffffffu, alive);
-            int b = base;
-            for (int w = 0; w < warp; ++w) b += ctr[2 + ch * nw + w];
-            if (alive) slot_list[b + __popc(bal & ((1u << lane) - 1u))] = j;
-            for (int w = 0; w < nw; ++w) base += ctr[2 + ch * nw + w];
+            if (alive) wlist[n_live + __popc(bal & ((1u << lane) - 1u))] = wbase + j;
+            n_live += __popc(bal);
         }
-        const bool stop = n_live == 0 || ctr[1] != 0;
-        __syncthreads();
-        if (stop) {
-            if (ctr[1] != 0 && tid == 0) atomicExch(a.work + 2, 1ull);
+        __syncwarp();
+        const bool aborted = *reinterpret_cast<volatile int32_t *>(ctr + 1) != 0;
+        if (n_live == 0 || aborted) {
+            if (aborted && lane == 0) atomicExch(a.work + 2, 1ull);
             break;
         }
-        if (n_live <= BD) {
-            slot = tid < n_live ? slot_list[tid] : -1;
+        if (n_live <= 32) {
+            slot = lane < n_live ? wlist[lane] : -1;
             rot = 0;
         } else {
             rot %= (unsigned int)n_live;
-            unsigned int k = rot + (unsigned int)tid;
+            unsigned int k = rot + (unsigned int)lane;
             if (k >= (unsigned int)n_live) k -= (unsigned int)n_live;
-            slot = slot_list[k];
-            rot += (unsigned int)BD;
+            slot = wlist[k];
+            rot += 32u;
         }
         live = slot >= 0;
         if (live) {
@@ -533,16 +587,16 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
             ev = stw[7 * NS + slot];
             ev0 = stw[8 * NS + slot];
             i = (long long)stw[9 * NS + slot];
-            tdf = DF{stf[0 * NS + slot], stf[1 * NS + slot]};
-            err_t = stf[2 * NS + slot];
-            Tdf = DF{stf[3 * NS + slot], stf[4 * NS + slot]};
+            tc = TF{stf[0 * NS + slot], stf[1 * NS + slot], stf[2 * NS + slot]};
+            err_t = stf[3 * NS + slot];
+            Tc = TF{stf[4 * NS + slot], stf[5 * NS + slot], stf[6 * NS + slot]};
             const uint32_t fl = stflag[slot];
             nat = (fl & kNat) != 0;
             exact_traj = (fl & kExactTraj) != 0;
             begin = (fl & kBegin) != 0;
             if (traj >= 0 && !exact_traj) Ops::load(c, a, spa + slot, NS);
         }
-        __syncthreads();  // slot flags are rewritten by the next phase
+        __syncwarp();  // slot flags are rewritten by the next phase
     }
     for (int off = 16; off > 0; off >>= 1) lane_events += __shfl_down_sync(0xffffffffu, lane_events, off);
     if ((tid & 31) == 0 && lane_events) atomicAdd(a.work + 1, lane_events);
