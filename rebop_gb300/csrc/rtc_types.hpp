@@ -12,6 +12,7 @@ typedef unsigned char uint8_t;
 typedef unsigned short uint16_t;
 typedef unsigned int uint32_t;
 typedef unsigned long long uint64_t;
+typedef unsigned long long uintptr_t;
 #else
 #include <cstddef>
 #include <cstdint>

@@ -147,8 +147,18 @@ std::map<std::pair<int, uint64_t>, Loaded> g_loaded;
 
 bool jit_supported(const Packed &p) {
     if (p.S < 1 || p.S > kJitMaxSpecies || p.R < 1 || p.R > kJitMaxReactions) return false;
-    for (int64_t d : p.jmp_d)
-        if (d <= -(1 << 23) || d >= (1 << 23)) return false;
+    // the summed change of each species by each reaction is exact in float
+    for (int r = 0; r < p.R; r++)
+        for (int sp = 0; sp < p.S; sp++) {
+            int64_t d = 0;
+            for (int k = 0; k < p.Q; k++) {
+                if (p.jmp_sp[(size_t)r * p.Q + k] != sp) continue;
+                const int64_t v = p.jmp_d[(size_t)r * p.Q + k];
+                if (v <= -(1 << 23) || v >= (1 << 23)) return false;
+                d += v;
+            }
+            if (d <= -(1 << 23) || d >= (1 << 23)) return false;
+        }
     return true;
 }
 
@@ -157,31 +167,63 @@ std::string jit_net_source(const Packed &p, int block) {
     std::ostringstream o;
     o << "// generated network operations: " << S << " species, " << R << " reactions\n";
     o << "#include \"ssa_spec_body.cuh\"\n\nnamespace rbg {\n\n";
+    // exact binary64 choice for the rare close float comparisons
+    o << "__device__ __noinline__ int net_exact_choice(float cn[" << S
+      << "], const uint64_t *rl, int RS, uint64_t u53) {\n";
+    o << "    double cum[" << R << "];\n    double total = 0.0, acc;\n";
+    for (int r = 0; r < R; r++) {
+        o << "    acc = __longlong_as_double((long long)rl[" << r << " * RS]);\n";
+        for (int f = 0; f < p.P; f++) {
+            const int32_t ord = p.fac_ord[(size_t)r * p.P + f];
+            const int32_t sp = p.fac_sp[(size_t)r * p.P + f];
+            if (ord == 0) continue;
+            if (p.macro_mode) {
+                o << "    { long long ff = (long long)cn[" << sp << "];";
+                for (int j = 1; j < ord; j++) o << " ff *= (long long)cn[" << sp << "] - " << j << ";";
+                o << " acc = __dmul_rn(acc, (double)ff); }\n";
+            } else {
+                for (int j = ord - 1; j >= 0; j--)
+                    o << "    acc = __dmul_rn(acc, (double)((long long)cn[" << sp << "] - " << j << "));\n";
+            }
+        }
+        o << "    total = __dadd_rn(total, acc);\n    cum[" << r << "] = total;\n";
+    }
+    o << "    const double chosen = __dmul_rn(total, (double)u53 * 0x1p-53);\n";
+    if (p.macro_mode) {
+        o << "    int idx = " << R << ";\n";
+        for (int r = R - 1; r >= 0; r--) o << "    if (chosen < cum[" << r << "]) idx = " << r << ";\n";
+    } else {
+        o << "    int idx = 0;\n";
+        for (int r = 0; r < R; r++) o << "    idx += cum[" << r << "] < chosen ? 1 : 0;\n";
+    }
+    o << "    return idx;\n}\n\n";
+
     o << "struct NetOps {\n";
     o << "    static constexpr int kMaxR = " << R << ";\n";
     o << "    static constexpr bool kMacro = " << (p.macro_mode ? "true" : "false") << ";\n";
-    o << "    struct Counts { int32_t n[" << S << "]; };\n";
+    // counts as exact floats in registers (|n| < 2^24)
+    o << "    struct Counts { float n[" << S << "]; };\n";
     o << "    __device__ static int nr(const SsaArgs &) { return " << R << "; }\n";
     // load: column -> registers, all counts in [0, 2^23)
     o << "    __device__ static bool load(Counts &c, const SsaArgs &, const int64_t *sp, int NS) {\n";
     o << "        uint64_t m = 0;\n";
     for (int s = 0; s < S; s++)
         o << "        { const int64_t v = sp[" << s << " * NS]; m |= (uint64_t)v; c.n[" << s
-          << "] = (int32_t)v; }\n";
+          << "] = __int2float_rn((int)(v & 0x7FFFFF)); }\n";
     o << "        return m < (1ull << 23);\n    }\n";
     o << "    __device__ static void store(const Counts &c, const SsaArgs &, int64_t *sp, int NS) {\n";
-    for (int s = 0; s < S; s++) o << "        sp[" << s << " * NS] = c.n[" << s << "];\n";
+    for (int s = 0; s < S; s++) o << "        sp[" << s << " * NS] = __float2int_rn(c.n[" << s << "]);\n";
     o << "    }\n";
     o << "    __device__ static void save(const Counts &c, const SsaArgs &, const int64_t *, int64_t *sps, int NS) "
          "{\n";
-    for (int s = 0; s < S; s++) o << "        sps[" << s << " * NS] = c.n[" << s << "];\n";
+    for (int s = 0; s < S; s++) o << "        sps[" << s << " * NS] = __float2int_rn(c.n[" << s << "]);\n";
     o << "    }\n";
-    // props: every reaction unrolled; counts outside [0, 2^23) leave the
-    // float-pair range (one OR over all counts covers negative ones too)
+    // props: every reaction unrolled; every count must lie in [0, 2^23)
+    // (a jump moves it by less than 2^23, so floats stay exact in between)
     o << "    __device__ static bool props(const SsaArgs &, const ExactTables &, const Counts &c, const int64_t *, int,\n"
-         "                                 const float2 *rf, int RS, DF *cum, DF &tot) {\n";
-    o << "        uint32_t m = 0;\n";
-    for (int s = 0; s < S; s++) o << "        m |= (uint32_t)c.n[" << s << "];\n";
+         "                                 const float2 *rf, int RS, float *cum, DF &tot) {\n";
+    o << "        float lo = c.n[0], hi = c.n[0];\n";
+    for (int s = 1; s < S; s++) o << "        lo = fminf(lo, c.n[" << s << "]); hi = fmaxf(hi, c.n[" << s << "]);\n";
     for (int r = 0; r < R; r++) {
         o << "        {\n            const float2 k = rf[" << r << " * RS];\n            DF acc{k.x, k.y};\n";
         for (int f = 0; f < p.P; f++) {
@@ -189,19 +231,24 @@ std::string jit_net_source(const Packed &p, int block) {
             const int32_t sp = p.fac_sp[(size_t)r * p.P + f];
             for (int j = 0; j < ord; j++) {
                 if (j == 0)
-                    o << "            acc = df_mul_f(acc, f23((uint32_t)c.n[" << sp << "] & 0x7FFFFFu));\n";
+                    o << "            acc = df_mul_fu(acc, c.n[" << sp << "]);\n";
                 else
-                    o << "            acc = df_mul_f(acc, f23((uint32_t)max(c.n[" << sp << "] - " << j
-                      << ", 0) & 0x7FFFFFu));\n";
+                    o << "            acc = df_mul_fu(acc, fmaxf(__fadd_rn(c.n[" << sp << "], -" << j
+                      << ".0f), 0.0f));\n";
             }
         }
         if (r == 0)
             o << "            tot = acc;\n";
         else
             o << "            tot = df_add(tot, acc);\n";
-        o << "            cum[" << r << "] = tot;\n        }\n";
+        o << "            cum[" << r << "] = tot.h;\n        }\n";
     }
-    o << "        return m >= (1u << 23);\n    }\n";
+    o << "        return !(lo >= 0.0f && hi < 8388608.0f);\n    }\n";
+    o << "    __device__ static int exact_choice(const SsaArgs &, const ExactTables &, const Counts &c, const int64_t "
+         "*, int,\n                                       const uint64_t *rl, int RS, uint64_t u53) {\n";
+    o << "        float cn[" << S << "];\n";
+    for (int s = 0; s < S; s++) o << "        cn[" << s << "] = c.n[" << s << "];\n";
+    o << "        return net_exact_choice(cn, rl, RS, u53);\n    }\n";
     // jump: per species, the sum of the deltas of the reaction that fired
     o << "    __device__ static void jump(Counts &c, const SsaArgs &, const ExactTables &, int64_t *, int, int idx) "
          "{\n";
@@ -216,7 +263,7 @@ std::string jit_net_source(const Packed &p, int block) {
         if (terms.empty()) continue;
         o << "        c.n[" << s << "] +=";
         for (size_t k = 0; k < terms.size(); k++)
-            o << (k ? " +" : "") << " (idx == " << terms[k].first << " ? " << terms[k].second << " : 0)";
+            o << (k ? " +" : "") << " (idx == " << terms[k].first << " ? " << terms[k].second << ".0f : 0.0f)";
         o << ";\n";
     }
     o << "    }\n};\n\n}  // namespace rbg\n\n";

@@ -51,18 +51,17 @@ bool ssa_spec_supported(const SsaArgs &a, int max_order) {
 }
 
 size_t ssa_spec_smem(const SsaArgs &a, int slots) {
-    return spec_smem_bytes(a.S, a.R, a.P, a.Q, slots, a.rate_stride != 0);
+    return spec_smem_bytes(a, slots);
 }
 
 int ssa_spec_slots(const SsaArgs &a, int grid, size_t smem_limit, int block) {
     // every warp owns the same number of slots (at least one per lane)
     const int warps = block / 32;
-    const bool per_traj = a.rate_stride != 0;
-    if (spec_smem_bytes(a.S, a.R, a.P, a.Q, block, per_traj) > smem_limit) return 0;
+    if (spec_smem_bytes(a, block) > smem_limit) return 0;
     const int64_t want = (a.n_traj + grid - 1) / (grid > 0 ? grid : 1);
     int slots = block;
     while (slots < want && slots + warps <= kSpecMaxSlots &&
-           spec_smem_bytes(a.S, a.R, a.P, a.Q, slots + warps, per_traj) <= smem_limit)
+           spec_smem_bytes(a, slots + warps) <= smem_limit)
         slots += warps;
     return slots;
 }

@@ -56,6 +56,13 @@ __device__ __forceinline__ DF df_mul_f(DF a, float f) {
     return fast2sum(p, __fmaf_rn(a.l, f, e));
 }
 
+// a * f without the final renormalisation: the low part stays below 2^-20 of
+// the high part for up to eight successive factors, which df_add accepts.
+__device__ __forceinline__ DF df_mul_fu(DF a, float f) {
+    const float p = __fmul_rn(a.h, f);
+    return DF{p, __fmaf_rn(a.l, f, __fmaf_rn(a.h, f, -p))};
+}
+
 __device__ __forceinline__ DF df_mul(DF a, DF b) {
     const float p = __fmul_rn(a.h, b.h);
     float e = __fmaf_rn(a.h, b.h, -p);
@@ -185,10 +192,20 @@ constexpr int kSpecMaxSlots = 2048;
 // then the lanes rotate over the live slots, so every resident trajectory
 // advances at the same pace and no second wave of late starters is left to
 // run on a nearly empty SM.
+constexpr int kSpecSampleCache = 256;  // sample times kept in shared memory
+
+__host__ __device__ inline int spec_sample_cache(const SsaArgs &a) {
+    return a.n_samples <= kSpecSampleCache ? (int)a.n_samples : 0;
+}
+
 // Rates live in per-slot columns when every trajectory has its own, else
 // once for the block.
-__host__ __device__ inline size_t spec_smem_bytes(int S, int R, int P, int Q, int slots, bool rate_per_traj) {
+__host__ __device__ inline size_t spec_smem_bytes(const SsaArgs &a, int slots) {
+    const int S = a.S, R = a.R, P = a.P, Q = a.Q;
+    const bool rate_per_traj = a.rate_stride != 0;
     size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;  // zxk, zf, zd, xdf
+    b += 24 * (size_t)spec_sample_cache(a);             // sample times: bits, float triple
+    b += 4 * (size_t)a.n_save + 16;                     // saved species
     b += 8 * (size_t)R * Q;                             // jd
     b += 16 * (size_t)R * (rate_per_traj ? slots : 1);  // exact rate bits, float-pair rates
     b += 16 * (size_t)S * slots;                        // counts, counts at interval start
@@ -231,8 +248,53 @@ __device__ __noinline__ unsigned long long replay_interval(const SsaArgs &a, con
     return e;
 }
 
+// The reference's choice #{r : cum_r < total * U} (or the macro's first r with
+// total * U < cum_r) in native binary64 from the counts in the slot column:
+// the rare steps whose float choice falls within its error margin.
+template <int MAXR, bool MACRO>
+__device__ __noinline__ int exact_choice_table(const SsaArgs &a, const ExactTables &m, const int64_t *sp, int NS,
+                                               const uint64_t *rl, int RS, uint64_t u53) {
+    double cum[MAXR];
+    double total = 0.0;
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r) {
+        if (r < a.R) {
+            double acc = __longlong_as_double((long long)rl[r * RS]);
+            for (int p = 0; p < a.P; ++p) {
+                const int f = m.fac[r * a.P + p];
+                const int o = f >> 16;
+                if (o == 0) continue;
+                const int64_t n = sp[(f & 0xFFFF) * NS];
+                if (MACRO) {
+                    int64_t ff = n;
+                    for (int j = 1; j < o; ++j) ff *= n - j;
+                    acc = __dmul_rn(acc, (double)ff);
+                } else {
+                    for (int j = o - 1; j >= 0; --j) acc = __dmul_rn(acc, (double)(n - j));
+                }
+            }
+            total = __dadd_rn(total, acc);
+            cum[r] = total;
+        }
+    }
+    const double chosen = __dmul_rn(total, (double)u53 * 0x1p-53);
+    int idx;
+    if (MACRO) {
+        idx = a.R;
+#pragma unroll
+        for (int r = MAXR - 1; r >= 0; --r)
+            if (r < a.R && chosen < cum[r]) idx = r;
+    } else {
+        idx = 0;
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r)
+            if (r < a.R) idx += (cum[r] < chosen) ? 1 : 0;
+    }
+    return idx;
+}
+
 // Slot flags.
-constexpr uint32_t kLive = 1, kNat = 2, kExactTraj = 4, kBegin = 8;
+constexpr uint32_t kLive = 1, kNat = 2, kExactTraj = 4, kBegin = 8, kHave = 16;
 
 // Network operations of the float-pair step over a data-driven descriptor:
 // the counts stay in the slot's shared-memory column and every reaction walks
@@ -253,10 +315,11 @@ struct TableOps {
     __device__ static void save(const Counts &, const SsaArgs &a, const int64_t *sp, int64_t *sps, int NS) {
         for (int s = 0; s < a.S; ++s) sps[s * NS] = sp[s * NS];
     }
-    // Float-pair propensities and running sums; true if a count leaves the
-    // float-pair range (then the step is undecided).
+    // Float-pair propensities: the total as a float pair, the running sums'
+    // high parts; true if a count leaves the float-pair range (then the step
+    // is undecided).
     __device__ static bool props(const SsaArgs &a, const ExactTables &ex, const Counts &, const int64_t *sp,
-                                 int NS, const float2 *rf, int RS, DF *cum, DF &tot) {
+                                 int NS, const float2 *rf, int RS, float *cum, DF &tot) {
         bool amb = false;
         tot = DF{0.f, 0.f};
 #pragma unroll
@@ -276,14 +339,19 @@ struct TableOps {
                     amb |= (uint64_t)n >= (1ull << 23);
                     for (int j = 0; j < o; ++j) {
                         const int64_t x = n - j > 0 ? n - j : 0;
-                        acc = df_mul_f(acc, f23((uint32_t)x & 0x7FFFFFu));
+                        acc = df_mul_fu(acc, f23((uint32_t)x & 0x7FFFFFu));
                     }
                 }
                 tot = df_add(tot, acc);
-                cum[r] = tot;
+                cum[r] = tot.h;
             }
         }
         return amb;
+    }
+    // The reference's choice for this state and uniform draw, in binary64.
+    __device__ static int exact_choice(const SsaArgs &a, const ExactTables &ex, const Counts &, const int64_t *sp,
+                                       int NS, const uint64_t *rl, int RS, uint64_t u53) {
+        return exact_choice_table<MAXR, MACRO>(a, ex, sp, NS, rl, RS, u53);
     }
     __device__ static void jump(Counts &, const SsaArgs &a, const ExactTables &ex, int64_t *sp, int NS, int idx) {
         if (idx < a.R)
@@ -324,7 +392,21 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     int32_t *ctr = slot_list + NS;  // [1] abort flag
     int32_t *fac = ctr + 128;
     int32_t *jsp = fac + (size_t)R * P;
+    int32_t *ssave = jsp + (size_t)R * Q;  // saved species indices
+    const int n_cache = spec_sample_cache(a);
+    uint64_t *sTb = reinterpret_cast<uint64_t *>(
+        (reinterpret_cast<uintptr_t>(ssave + a.n_save) + 15) & ~(uintptr_t)15);  // sample time bits
+    float *sTf = reinterpret_cast<float *>(sTb + n_cache);                         // as float triples
     load_exact_tables(a, zxk, zf, zd, fac, jsp, jd);
+    for (int k = tid; k < a.n_save; k += BD) ssave[k] = a.save_idx[k];
+    for (int k = tid; k < n_cache; k += BD) {
+        const double v = a.sample_t[k];
+        sTb[k] = (uint64_t)__double_as_longlong(v);
+        const TF f = tf_from_double(v);
+        sTf[3 * k] = f.h;
+        sTf[3 * k + 1] = f.m;
+        sTf[3 * k + 2] = f.l;
+    }
     for (int k = tid; k < 256; k += BD) {
         const double v = a.zig[kZigOffXdf + k];
         xdf[k] = *reinterpret_cast<const float2 *>(&v);
@@ -337,33 +419,30 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
             rdf[r] = make_float2(d.h, d.l);
         }
     // every slot starts live and empty (no trajectory taken yet)
-    for (int k = tid; k < NS; k += BD) {
-        stflag[k] = kLive;
-        stw[6 * (size_t)NS + k] = ~0ull;
-    }
+    for (int k = tid; k < NS; k += BD) stflag[k] = kLive;
     if (tid < 128) ctr[tid] = 0;
     __syncthreads();
     const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
 
     const float G = (float)(a.max_mults + R + 2) * kGamma;  // running-sum bound
     const float c_q = G + 6.0f * kGamma;                     // relative bound of Exp1/total
-    const float c_sel = 2.0f * G + 8.0f * kGamma;            // choice margin / total
+    const float c_sel = 0x1p-21f;                            // float32 choice margin / total
     const int64_t t_start = global_ns();
     const int phase_steps = a.phase_steps > 0 ? a.phase_steps : kSpecPhase;
     unsigned int tick = 0, rot = 0;
     unsigned long long lane_events = 0;
 
-    // ---- this lane's slot and its state, cached in registers during a phase
+    // ---- this lane's slot; the hot state sits in registers during a phase,
+    // the cold words (interval start t0, sample time T, trajectory, event
+    // count at the interval start, sample index) stay in the slot's columns
     int slot = wbase + lane;
     int32_t *const wlist = slot_list + wbase;
     typename Ops::Counts c{};
     Xoshiro g{0, 0, 0, 0};
-    uint64_t t0 = 0, T = 0;
     TF Tc{0.f, 0.f, 0.f}, tc{0.f, 0.f, 0.f};  // sample time, clock
     float err_t = 0.f;                         // bound on |clock - reference clock|
-    long long i = 0, traj = -1;
-    unsigned long long ev = 0, ev0 = 0;
-    bool live = true, nat = false, exact_traj = false, begin = false, abort_run = false;
+    unsigned long long ev = 0;
+    bool live = true, have = false, nat = false, exact_traj = false, begin = false, abort_run = false;
 
     for (;;) {
         // ---------------------------------------------------------- phase
@@ -371,16 +450,18 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
             int64_t *const sp = spa + slot;
             int64_t *const sps = spsa + slot;
             uint64_t *const gsv = gsva + slot;
+            uint64_t *const st = stw + slot;  // cold words: st[k * NS]
             uint64_t *const rl = rate + (rate_cols ? slot : 0);
             float2 *const rf = rdf + (rate_cols ? slot : 0);
             for (int step = 0; step < phase_steps && live; ++step) {
-                if (traj < 0) {
+                if (!have) {
                     // take the next trajectory into this slot
-                    traj = (long long)atomicAdd(a.work, 1ull);
+                    const long long traj = (long long)atomicAdd(a.work, 1ull);
                     if (traj >= a.n_traj) {
                         live = false;
                         break;
                     }
+                    uint64_t t0;
                     if (a.in_species) {
                         for (int s = 0; s < S; ++s) sp[s * NS] = a.in_species[traj * S + s];
                         t0 = (uint64_t)__double_as_longlong(a.in_t[traj]);
@@ -407,15 +488,26 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                     }
                     exact_traj |= nat;
                     exact_traj |= !Ops::load(c, a, sp, NS);
-                    i = 0;
+                    tc = tf_from_double(__longlong_as_double((long long)t0));
+                    st[4 * NS] = t0;
+                    st[6 * NS] = (uint64_t)traj;
+                    st[9 * NS] = 0;
                     ev = 0;
+                    have = true;
                     begin = true;
                 }
                 if (begin) {
-                    // a sample interval starts at t0: save what a re-run needs
-                    T = (uint64_t)__double_as_longlong(a.sample_t[i]);
-                    Tc = tf_from_double(__longlong_as_double((long long)T));
-                    tc = tf_from_double(__longlong_as_double((long long)t0));
+                    // a sample interval starts at t0 (the clock tc holds t0
+                    // exactly): save what a re-run needs
+                    const int si = (int)st[9 * NS];
+                    if (si < n_cache) {
+                        st[5 * NS] = sTb[si];
+                        Tc = TF{sTf[3 * si], sTf[3 * si + 1], sTf[3 * si + 2]};
+                    } else {
+                        const double T = a.sample_t[si];
+                        st[5 * NS] = (uint64_t)__double_as_longlong(T);
+                        Tc = tf_from_double(T);
+                    }
                     err_t = 0.f;
                     if (exact_traj)
                         for (int s = 0; s < S; ++s) sps[s * NS] = sp[s * NS];
@@ -425,7 +517,7 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                     gsv[NS] = g.s1;
                     gsv[2 * NS] = g.s2;
                     gsv[3 * NS] = g.s3;
-                    ev0 = ev;
+                    st[8 * NS] = ev;
                     begin = false;
                 }
                 if ((++tick & 1023u) == 0 && global_ns() - t_start > a.budget_ns) {
@@ -436,17 +528,35 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                 bool fire = false, replay = exact_traj;
                 int idx = 0;
                 if (!replay) {
-                    // float-pair step; the generator advances in place since
-                    // each draw happens only when the reference makes it (Exp1
-                    // when total > 0, the uniform when the reaction fires); an
-                    // undecided step re-runs the interval from its saved state.
-                    DF cum[MAXR];
+                    // Float-pair step.  Both draws the step may make are taken
+                    // ahead from a copy of the generator (the reference draws
+                    // Exp1 only when total > 0 and the uniform only when the
+                    // reaction fires), so they overlap the propensities; the
+                    // generator moves on only by the draws the step commits.
+                    // An undecided step re-runs the interval from its saved state.
+                    Xoshiro g2 = g;
+                    const uint64_t b1 = xo_next(g2);
+                    const uint64_t b2 = xo_next(g2);
+                    const int i1 = (int)(b1 & 0xff);
+                    const uint64_t k1 = b1 >> 12;
+                    const uint64_t K1 = ex.zxk[i1].y;
+                    const float2 X1 = xdf[i1];
+                    DF x = df_mul(df_u53(2 * k1 + 1), DF{X1.x, X1.y});
+                    float xerr = kGamma * X1.x;
+                    float cum[MAXR];
                     DF tot;
                     bool amb = Ops::props(a, ex, c, sp, NS, rf, RS, cum, tot);
+                    const bool slow = !(k1 < K1);
+                    uint64_t bu = b2;
                     if (tot.h > 0.0f) {
+                        if (slow) {
+                            // ziggurat rejection or tail: redo the draws in order
+                            Xoshiro gs = g;
+                            x = exp1_df(gs, ex, xdf, xerr);
+                            bu = xo_next(gs);
+                            g2 = gs;
+                        }
                         amb |= tot.h < 0x1p-90f || tot.h > 0x1p90f;
-                        float xerr;
-                        const DF x = exp1_df(g, ex, xdf, xerr);
                         const float r = rcp_approx(tot.h);
                         const DF q = df_div(x, tot, r);
                         const TF tn = tf_add(tc, q);
@@ -465,27 +575,41 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                         const float dd = __fmul_rn(d, 1.0f - 0x1p-22f);
                         fire = dd > mt;
                         amb |= !(fire || dd < -mt) || !(err_tn < 1.0e30f) || q.h < 0x1p-100f;
-                        if (fire && !amb) {
-                            const DF ch = df_mul(tot, df_u53(xo_next(g) >> 11));
-                            const float msel = c_sel * tot.h;
+                        // choice #{r : cum_r < total * U} in float32: the high
+                        // parts are within 2^-23.9 of the exact sums, U and the
+                        // product add 2^-23 each; a comparison inside that
+                        // margin is redone exactly in binary64
+                        const float ch = __fmul_rn(tot.h, f23((uint32_t)(bu >> 41)) * 0x1p-23f);
+                        const float msel = c_sel * tot.h;
+                        bool close = false;
 #pragma unroll
-                            for (int rr = 0; rr < MAXR; ++rr) {
-                                if (rr < R) {
-                                    const float dr =
-                                        __fadd_rn(__fsub_rn(cum[rr].h, ch.h), __fsub_rn(cum[rr].l, ch.l));
-                                    idx += dr < 0.0f ? 1 : 0;
-                                    amb |= fabsf(dr) <= msel;
-                                }
+                        for (int rr = 0; rr < MAXR; ++rr) {
+                            if (rr < R) {
+                                const float dr = __fsub_rn(cum[rr], ch);
+                                idx += dr < 0.0f ? 1 : 0;
+                                close |= fabsf(dr) <= msel;
                             }
-                            tc = tn;
-                            err_t = err_tn;
+                        }
+                        if (!amb) {
+                            if (fire) {
+                                if (close) idx = Ops::exact_choice(a, ex, c, sp, NS, rl, RS, bu >> 11);
+                                g = g2;
+                                tc = tn;
+                                err_t = err_tn;
+                            } else {
+                                // the sample records: the Exp1 draw alone was made
+                                if (slow) exp1_df(g, ex, xdf, xerr);
+                                else xo_next(g);
+                            }
                         }
                     }
                     replay = amb;
                 }
                 if (replay) {
                     if (!exact_traj) atomicAdd(a.work + 3, 1ull);  // speculation undecided
-                    ev = replay_interval<MAXR, MACRO>(a, ex, sp, sps, gsv, rl, RS, NS, t0, T, nat, ev0, t_start);
+                    const unsigned long long ev0 = st[8 * NS];
+                    ev = replay_interval<MAXR, MACRO>(a, ex, sp, sps, gsv, rl, RS, NS, st[4 * NS], st[5 * NS], nat,
+                                                      ev0, t_start);
                     if (ev == ~0ull) {
                         ev = ev0;
                         abort_run = true;
@@ -501,12 +625,17 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                 } else {
                     // record sample i at t = T
                     if (!replay) Ops::store(c, a, sp, NS);
+                    const long long traj = (long long)st[6 * NS];
+                    const uint64_t i = st[9 * NS];
                     int64_t *o = a.out + (size_t)i * a.n_save * a.n_traj + traj;
-                    for (int k = 0; k < a.n_save; ++k) o[(size_t)k * a.n_traj] = sp[a.save_idx[k] * NS];
-                    if (++i < a.n_samples) {
-                        t0 = T;
+                    for (int k = 0; k < a.n_save; ++k) o[(size_t)k * a.n_traj] = sp[ssave[k] * NS];
+                    if ((long long)i + 1 < a.n_samples) {
+                        st[9 * NS] = i + 1;
+                        st[4 * NS] = st[5 * NS];  // next interval starts at T
+                        tc = Tc;
                         begin = true;
                     } else {
+                        const uint64_t T = st[5 * NS];
                         if (a.fin_species)
                             for (int s = 0; s < S; ++s) a.fin_species[traj * S + s] = sp[s * NS];
                         if (a.fin_t) a.fin_t[traj] = __longlong_as_double((long long)T);
@@ -518,23 +647,18 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                         }
                         if (a.events) a.events[traj] = ev;
                         lane_events += ev;
-                        traj = -1;
+                        have = false;
                     }
                 }
             }
-            // ---- park the slot's state
+            // ---- park the slot's hot state
             if (live) {
-                if (traj >= 0 && !exact_traj) Ops::store(c, a, sp, NS);
-                stw[0 * NS + slot] = g.s0;
-                stw[1 * NS + slot] = g.s1;
-                stw[2 * NS + slot] = g.s2;
-                stw[3 * NS + slot] = g.s3;
-                stw[4 * NS + slot] = t0;
-                stw[5 * NS + slot] = T;
-                stw[6 * NS + slot] = (uint64_t)traj;
-                stw[7 * NS + slot] = ev;
-                stw[8 * NS + slot] = ev0;
-                stw[9 * NS + slot] = (uint64_t)i;
+                if (have && !exact_traj) Ops::store(c, a, sp, NS);
+                st[0 * NS] = g.s0;
+                st[1 * NS] = g.s1;
+                st[2 * NS] = g.s2;
+                st[3 * NS] = g.s3;
+                st[7 * NS] = ev;
                 stf[0 * NS + slot] = tc.h;
                 stf[1 * NS + slot] = tc.m;
                 stf[2 * NS + slot] = tc.l;
@@ -543,8 +667,8 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                 stf[5 * NS + slot] = Tc.m;
                 stf[6 * NS + slot] = Tc.l;
             }
-            stflag[slot] = (live ? kLive : 0u) | (nat ? kNat : 0u) | (exact_traj ? kExactTraj : 0u) |
-                           (begin ? kBegin : 0u);
+            stflag[slot] = (live ? kLive : 0u) | (have ? kHave : 0u) | (nat ? kNat : 0u) |
+                           (exact_traj ? kExactTraj : 0u) | (begin ? kBegin : 0u);
             if (abort_run) ctr[1] = 1;
         }
         __syncwarp();
@@ -580,21 +704,17 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
         }
         live = slot >= 0;
         if (live) {
-            g = Xoshiro{stw[0 * NS + slot], stw[1 * NS + slot], stw[2 * NS + slot], stw[3 * NS + slot]};
-            t0 = stw[4 * NS + slot];
-            T = stw[5 * NS + slot];
-            traj = (long long)stw[6 * NS + slot];
-            ev = stw[7 * NS + slot];
-            ev0 = stw[8 * NS + slot];
-            i = (long long)stw[9 * NS + slot];
-            tc = TF{stf[0 * NS + slot], stf[1 * NS + slot], stf[2 * NS + slot]};
-            err_t = stf[3 * NS + slot];
-            Tc = TF{stf[4 * NS + slot], stf[5 * NS + slot], stf[6 * NS + slot]};
             const uint32_t fl = stflag[slot];
+            have = (fl & kHave) != 0;
             nat = (fl & kNat) != 0;
             exact_traj = (fl & kExactTraj) != 0;
             begin = (fl & kBegin) != 0;
-            if (traj >= 0 && !exact_traj) Ops::load(c, a, spa + slot, NS);
+            g = Xoshiro{stw[0 * NS + slot], stw[1 * NS + slot], stw[2 * NS + slot], stw[3 * NS + slot]};
+            ev = stw[7 * NS + slot];
+            tc = TF{stf[0 * NS + slot], stf[1 * NS + slot], stf[2 * NS + slot]};
+            err_t = stf[3 * NS + slot];
+            Tc = TF{stf[4 * NS + slot], stf[5 * NS + slot], stf[6 * NS + slot]};
+            if (have && !exact_traj) Ops::load(c, a, spa + slot, NS);
         }
         __syncwarp();  // slot flags are rewritten by the next phase
     }

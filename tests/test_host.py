@@ -197,16 +197,18 @@ def test_generated_network_source(rb):
     import importlib
 
     L = importlib.import_module("rebop_gb300._lib").lib
-    buf = C.create_string_buffer(1 << 16)
+    buf = C.create_string_buffer(1 << 17)
     net = _dimer_net(rb)
-    assert L.rbg_internal_jit_source(net._h, buf, 1 << 16) == 0
+    assert L.rbg_internal_jit_source(net._h, buf, 1 << 17) == 0
     src = buf.value.decode()
-    assert "kMaxR = 5" in src and "int32_t n[4]" in src
-    assert "max(c.n[2] - 1, 0)" in src
-    assert "c.n[2] += (idx == 1 ? 1 : 0) + (idx == 2 ? -2 : 0) + (idx == 4 ? -1 : 0);" in src
+    assert "kMaxR = 5" in src and "float n[4]" in src
+    assert "fmaxf(__fadd_rn(c.n[2], -1.0f), 0.0f)" in src
+    assert "c.n[2] += (idx == 1 ? 1.0f : 0.0f) + (idx == 2 ? -2.0f : 0.0f) + (idx == 4 ? -1.0f : 0.0f);" in src
+    # the exact binary64 choice multiplies the reference's factors n-1, then n
+    assert "acc = __dmul_rn(acc, (double)((long long)cn[2] - 1));\n    acc = __dmul_rn(acc, (double)((long long)cn[2] - 0));" in src
     big = rb.Network(40)
     big.add_reaction(rb.Rate.lma(1.0, [1] + [0] * 39), [-1] + [0] * 39)
-    assert L.rbg_internal_jit_source(big._h, buf, 1 << 16) == 5  # RB_ERR_UNSUPPORTED
+    assert L.rbg_internal_jit_source(big._h, buf, 1 << 17) == 5  # RB_ERR_UNSUPPORTED
 
 
 def test_generated_network_compiles(rb, tmp_path, monkeypatch):
