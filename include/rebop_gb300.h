@@ -93,6 +93,21 @@ int rb_network_add_reaction_lma_sparse(rb_network *net, double rate, const uint3
                                        const uint32_t *exponents, int32_t n_pairs,
                                        const int64_t *differences, int32_t n_differences);
 
+/* add_reaction(Rate::expr(expr), differences): src/gillespie.rs:33-35, :88
+ * and :225-244; the expression tree of src/expr.rs:8-21 in postfix form.
+ * Each code word is op | argument << 8 with op
+ *   0 push constant consts[argument]   1 push species count [argument] as f64
+ *   2 negate   3 add   4 subtract   5 multiply   6 divide   7 powf
+ *   8 max   9 min   10 exp
+ * (binary operations pop y then x and push x op y).  The propensity is the
+ * program's value, evaluated in binary64 as Expr::eval does (expr.rs:23-39).
+ * A malformed program, an index out of range or a stack deeper than 16 is
+ * RB_ERR_INVALID.  Networks with such reactions run on the generic exact
+ * kernel; the no-allocation entry point refuses them (RB_ERR_UNSUPPORTED). */
+int rb_network_add_reaction_expr(rb_network *net, const int32_t *code, int32_t n_code,
+                                 const double *consts, int32_t n_consts, const int64_t *differences,
+                                 int32_t n_differences);
+
 /* Lower a define_system! body (src/gillespie_macro.rs:50-58):
  *     p1 p2 ...;  Name { A, B, ... }  rname: [k] A + ... => [k] B + ... @ rate ...
  * `rate` is a parameter name or a numeric literal.  Parameters start as NaN,
@@ -210,6 +225,9 @@ int rb_gillespie_add_reaction_lma(rb_gillespie *g, double rate, const uint32_t *
 int rb_gillespie_add_reaction_lma_sparse(rb_gillespie *g, double rate, const uint32_t *species,
                                          const uint32_t *exponents, int32_t n_pairs,
                                          const int64_t *differences, int32_t n_differences);
+int rb_gillespie_add_reaction_expr(rb_gillespie *g, const int32_t *code, int32_t n_code,
+                                   const double *consts, int32_t n_consts, const int64_t *differences,
+                                   int32_t n_differences);     /* Rate::expr, as above */
 double rb_gillespie_get_time(const rb_gillespie *g);           /* gillespie.rs:246-248 */
 void rb_gillespie_set_time(rb_gillespie *g, double t);         /* gillespie.rs:250-252 */
 int rb_gillespie_get_species(const rb_gillespie *g, int32_t s, int64_t *value); /* :260-262 */

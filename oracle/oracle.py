@@ -54,6 +54,9 @@ class _Net(C.Structure):
         ("mfac_off", C.POINTER(C.c_int32)),
         ("mfac_idx", C.POINTER(C.c_uint32)),
         ("mfac_ord", C.POINTER(C.c_uint32)),
+        ("ex_off", C.POINTER(C.c_int32)),
+        ("ex_code", C.POINTER(C.c_int32)),
+        ("ex_const", C.POINTER(C.c_double)),
     ]
 
 
@@ -112,6 +115,7 @@ class OracleNet:
         self.sparse: list[list[tuple[int, int]]] = []
         self.jumps: list[list[int]] = []
         self.mfac: list[list[tuple[int, int]]] = []
+        self.programs: list[tuple[list[int], list[float]]] = []
 
     # Gillespie::add_reaction(Rate::lma(rate, exps), differences)
     def add_lma(self, rate: float, exponents, differences) -> "OracleNet":
@@ -122,6 +126,20 @@ class OracleNet:
         self.sparse.append([])
         self.jumps.append([int(d) for d in differences])
         self.mfac.append([(s, int(e)) for s, e in enumerate(exponents) if e > 0])
+        self.programs.append(([], []))
+        return self
+
+    # Gillespie::add_reaction(Rate::expr(expr), differences): the expression as
+    # a postfix program (words op | arg << 8, see ssa_oracle.c) and its constants
+    def add_expr(self, code, consts, differences) -> "OracleNet":
+        assert len(differences) == self.S
+        self.rates.append(0.0)
+        self.kinds.append(2)
+        self.dense.append([0] * self.S)
+        self.sparse.append([])
+        self.jumps.append([int(d) for d in differences])
+        self.mfac.append([])
+        self.programs.append(([int(c) for c in code], [float(c) for c in consts]))
         return self
 
     # Gillespie::add_reaction(Rate::lma_sparse(rate, pairs), differences)
@@ -133,6 +151,7 @@ class OracleNet:
         self.sparse.append([(int(i), int(e)) for i, e in pairs])
         self.jumps.append([int(d) for d in differences])
         self.mfac.append([(int(i), int(e)) for i, e in pairs])
+        self.programs.append(([], []))
         return self
 
     # define_system! reaction: reactant factors (species, literal) in written order
@@ -146,6 +165,7 @@ class OracleNet:
         self.sparse.append([])
         self.jumps.append([int(x) for x in differences])
         self.mfac.append([(int(s), int(k)) for s, k in factors])
+        self.programs.append(([], []))
         return self
 
     @property
@@ -179,11 +199,24 @@ class OracleNet:
         keep["mfac_off"] = np.asarray(moff, dtype=np.int32)
         keep["mfac_idx"] = np.asarray(midx or [0], dtype=np.uint32)
         keep["mfac_ord"] = np.asarray(mord or [0], dtype=np.uint32)
+        eoff, ecode, econst = [0], [], []
+        for code, consts in self.programs:
+            base = len(econst)
+            for w in code:
+                op, arg = w & 0xFF, w >> 8
+                ecode.append(op | ((arg + base) << 8) if op == 0 else w)  # constants: global index
+            econst.extend(consts)
+            eoff.append(len(ecode))
+        keep["ex_off"] = np.asarray(eoff, dtype=np.int32)
+        keep["ex_code"] = np.asarray(ecode or [0], dtype=np.int32)
+        keep["ex_const"] = np.asarray(econst or [0.0], dtype=np.float64)
         n = _Net(S, R, _ptr(keep["rate"], C.c_double), _ptr(keep["kind"], C.c_int32),
                  _ptr(keep["lma"], C.c_uint32), _ptr(keep["sp_off"], C.c_int32),
                  _ptr(keep["sp_idx"], C.c_uint32), _ptr(keep["sp_exp"], C.c_uint32),
                  _ptr(keep["jump"], C.c_int64), int(self.macro), _ptr(keep["mfac_off"], C.c_int32),
-                 _ptr(keep["mfac_idx"], C.c_uint32), _ptr(keep["mfac_ord"], C.c_uint32))
+                 _ptr(keep["mfac_idx"], C.c_uint32), _ptr(keep["mfac_ord"], C.c_uint32),
+                 _ptr(keep["ex_off"], C.c_int32), _ptr(keep["ex_code"], C.c_int32),
+                 _ptr(keep["ex_const"], C.c_double))
         return n, keep
 
     def validate(self) -> bool:

@@ -126,7 +126,8 @@ typedef struct {
     int32_t n_species;
     int32_t n_reactions;
     const double *rate;        /* [R] rate constants                              */
-    const int32_t *rate_kind;  /* [R] 0 = Rate::LMA (dense), 1 = Rate::LMASparse */
+    const int32_t *rate_kind;  /* [R] 0 = Rate::LMA (dense), 1 = Rate::LMASparse,
+                                  2 = Rate::Expr                                  */
     const uint32_t *lma;       /* [R*S] dense exponents (kind 0)                  */
     const int32_t *sp_off;     /* [R+1] offsets into sp_idx/sp_exp (kind 1)       */
     const uint32_t *sp_idx;
@@ -136,12 +137,54 @@ typedef struct {
     const int32_t *mfac_off;   /* macro mode: [R+1] offsets of (species, order)   */
     const uint32_t *mfac_idx;  /*   factors in the order written in the reaction  */
     const uint32_t *mfac_ord;
+    const int32_t *ex_off;     /* kind 2: [R+1] offsets into ex_code              */
+    const int32_t *ex_code;    /*   postfix program: op | argument << 8           */
+    const double *ex_const;    /*   constants the program pushes                  */
 } orc_net;
+
+/* Postfix form of an Expr tree (expr.rs:8-21): each word is op | arg << 8. */
+enum { EX_CONST = 0, EX_SPECIES, EX_NEG, EX_ADD, EX_SUB, EX_MUL, EX_DIV, EX_POW, EX_MAX, EX_MIN, EX_EXP };
+#define EX_MAX_DEPTH 64
+
+/* Expr::eval, expr.rs:23-39: species counts as f64, IEEE operations, powf
+ * and exp from the C library, max/min returning the non-NaN operand. */
+static double expr_eval(const orc_net *net, int r, const int64_t *sp) {
+    double st[EX_MAX_DEPTH];
+    int top = 0;
+    for (int k = net->ex_off[r]; k < net->ex_off[r + 1]; k++) {
+        const int32_t w = net->ex_code[k];
+        const int op = w & 0xff, arg = w >> 8;
+        if (op == EX_CONST) {
+            st[top++] = net->ex_const[arg];
+        } else if (op == EX_SPECIES) {
+            st[top++] = (double)sp[arg];
+        } else if (op == EX_NEG) {
+            st[top - 1] = -st[top - 1];
+        } else if (op == EX_EXP) {
+            st[top - 1] = exp(st[top - 1]);
+        } else {
+            const double b = st[--top], a = st[top - 1];
+            double v;
+            switch (op) {
+            case EX_ADD: v = a + b; break;
+            case EX_SUB: v = a - b; break;
+            case EX_MUL: v = a * b; break;
+            case EX_DIV: v = a / b; break;
+            case EX_POW: v = pow(a, b); break;
+            case EX_MAX: v = fmax(a, b); break;
+            default: v = fmin(a, b); break;
+            }
+            st[top - 1] = v;
+        }
+    }
+    return st[0];
+}
 
 /* Rate::rate for LMA, gillespie.rs:71-87: a fold over species in index order,
  * multiplying the running product by each factor of n(n-1)...(n-e+1) taken
  * from the lowest factor up, each converted to f64 on its own. */
 static double rate_lma(const orc_net *net, const double *rates, int r, const int64_t *sp) {
+    if (net->rate_kind[r] == 2) return expr_eval(net, r, sp);  /* gillespie.rs:88 */
     double acc = rates[r];
     if (net->rate_kind[r] == 0) {
         const uint32_t *e = net->lma + (size_t)r * net->n_species;
@@ -162,6 +205,7 @@ static double rate_lma(const orc_net *net, const double *rates, int r, const int
  * parameter times, for each reactant in the order written, the integer
  * falling factorial n(n-1)...(n-k+1) computed in isize and cast once. */
 static double rate_macro(const orc_net *net, const double *rates, int r, const int64_t *sp) {
+    if (net->rate_kind[r] == 2) return expr_eval(net, r, sp);
     double acc = rates[r];
     for (int p = net->mfac_off[r]; p < net->mfac_off[r + 1]; p++) {
         int64_t n = sp[net->mfac_idx[p]];
@@ -274,6 +318,18 @@ int orc_validate(const orc_net *net) {
         if (net->macro_mode) {
             for (int p = net->mfac_off[r]; p < net->mfac_off[r + 1]; p++)
                 if ((int64_t)net->mfac_idx[p] >= net->n_species) return -1;
+        }
+        if (net->rate_kind[r] == 2) {
+            /* a well-formed postfix program leaves exactly one value */
+            int depth = 0;
+            for (int k = net->ex_off[r]; k < net->ex_off[r + 1]; k++) {
+                const int op = net->ex_code[k] & 0xff, arg = net->ex_code[k] >> 8;
+                if (op == EX_SPECIES && (arg < 0 || arg >= net->n_species)) return -1;
+                if (op > EX_EXP) return -1;
+                depth += (op <= EX_SPECIES) ? 1 : (op == EX_NEG || op == EX_EXP) ? 0 : -1;
+                if (depth < 1 || depth > EX_MAX_DEPTH) return -1;
+            }
+            if (depth != 1) return -1;
         }
     }
     return 0;

@@ -62,6 +62,7 @@ _SIGS = {
     "rb_network_nb_reactions": ([_vp], _i32),
     "rb_network_add_reaction_lma": ([_vp, _f64, P(_u32), _i32, P(_i64), _i32], C.c_int),
     "rb_network_add_reaction_lma_sparse": ([_vp, _f64, P(_u32), P(_u32), _i32, P(_i64), _i32], C.c_int),
+    "rb_network_add_reaction_expr": ([_vp, P(_i32), _i32, P(_f64), _i32, P(_i64), _i32], C.c_int),
     "rb_network_from_dsl": ([_cp, P(_vp)], C.c_int),
     "rb_network_set_param": ([_vp, _cp, _f64], C.c_int),
     "rb_network_nb_params": ([_vp], _i32),
@@ -88,6 +89,7 @@ _SIGS = {
     "rb_gillespie_nb_reactions": ([_vp], _i32),
     "rb_gillespie_add_reaction_lma": ([_vp, _f64, P(_u32), _i32, P(_i64), _i32], C.c_int),
     "rb_gillespie_add_reaction_lma_sparse": ([_vp, _f64, P(_u32), P(_u32), _i32, P(_i64), _i32], C.c_int),
+    "rb_gillespie_add_reaction_expr": ([_vp, P(_i32), _i32, P(_f64), _i32, P(_i64), _i32], C.c_int),
     "rb_gillespie_get_time": ([_vp], _f64),
     "rb_gillespie_set_time": ([_vp, _f64], None),
     "rb_gillespie_get_species": ([_vp, _i32, P(_i64)], C.c_int),

@@ -32,6 +32,7 @@ class Rate:
     rate: float
     exponents: tuple = ()
     pairs: tuple | None = None
+    expr: object = None  # Rate::Expr: a resolved expression tree (rebop_gb300.expr.Expr)
 
     @staticmethod
     def lma(rate: float, exponents: Iterable[int]) -> "Rate":
@@ -40,6 +41,12 @@ class Rate:
     @staticmethod
     def lma_sparse(rate: float, pairs: Iterable[tuple[int, int]]) -> "Rate":
         return Rate(float(rate), (), tuple((int(i), int(e)) for i, e in pairs))
+
+    @staticmethod
+    def expression(expr) -> "Rate":
+        """``Rate::expr`` (gillespie.rs:33-35): the propensity is the value of a
+        resolved expression tree over species counts (src/expr.rs:8-39)."""
+        return Rate(0.0, (), None, expr)
 
     @property
     def is_sparse(self) -> bool:
@@ -186,7 +193,13 @@ class Network:
     def add_reaction(self, rate: Rate, differences: Sequence[int]) -> "Network":
         """``Gillespie::add_reaction`` (src/gillespie.rs:225-244)."""
         d = _i64a(differences)
-        if rate.is_sparse:
+        if rate.expr is not None:
+            code, consts = rate.expr.to_program()
+            c = np.ascontiguousarray(np.asarray(code, dtype=np.int32))
+            k = np.ascontiguousarray(np.asarray(consts or [0.0], dtype=np.float64))
+            check(lib.rb_network_add_reaction_expr(self._h, ptr(c, _i32), c.size, ptr(k, _f64), len(consts),
+                                                   ptr(d, _i64), d.size))
+        elif rate.is_sparse:
             idx = _u32a([i for i, _ in rate.pairs])
             ex = _u32a([e for _, e in rate.pairs])
             check(lib.rb_network_add_reaction_lma_sparse(self._h, rate.rate, ptr(idx, _u32), ptr(ex, _u32),
@@ -329,7 +342,13 @@ class Gillespie:
 
     def add_reaction(self, rate: Rate, differences: Sequence[int]) -> None:
         d = _i64a(differences)
-        if rate.is_sparse:
+        if rate.expr is not None:
+            code, consts = rate.expr.to_program()
+            c = np.ascontiguousarray(np.asarray(code, dtype=np.int32))
+            k = np.ascontiguousarray(np.asarray(consts or [0.0], dtype=np.float64))
+            check(lib.rb_gillespie_add_reaction_expr(self._h, ptr(c, _i32), c.size, ptr(k, _f64), len(consts),
+                                                     ptr(d, _i64), d.size))
+        elif rate.is_sparse:
             idx = _u32a([i for i, _ in rate.pairs])
             ex = _u32a([e for _, e in rate.pairs])
             check(lib.rb_gillespie_add_reaction_lma_sparse(self._h, rate.rate, ptr(idx, _u32), ptr(ex, _u32),

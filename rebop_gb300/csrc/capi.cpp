@@ -167,6 +167,9 @@ int events_run(const rbg::Network &net, int64_t *species, double *t, uint64_t *r
     a.fac_ord = dn.fac_ord;
     a.jmp_sp = dn.jmp_sp;
     a.jmp_d = dn.jmp_d;
+    a.ex_off = dn.ex_off;
+    a.ex_code = dn.ex_code;
+    a.ex_const = dn.ex_const;
     a.n_traj = 1;
     a.species = reinterpret_cast<int64_t *>(b + o_sp);
     a.t = reinterpret_cast<double *>(b + o_t);
@@ -258,6 +261,14 @@ int rb_network_add_reaction_lma_sparse(rb_network *net, double rate, const uint3
     if (!net) return fail(RB_ERR_INVALID, "null network");
     std::lock_guard<std::mutex> lk(net->net.mu);
     std::string e = net->net.add_lma_sparse(rate, species, exponents, n_pairs, differences, n_differences);
+    return e.empty() ? RB_OK : fail(RB_ERR_INVALID, e);
+}
+
+int rb_network_add_reaction_expr(rb_network *net, const int32_t *code, int32_t n_code, const double *consts,
+                                 int32_t n_consts, const int64_t *differences, int32_t n_differences) {
+    if (!net) return fail(RB_ERR_INVALID, "null network");
+    std::lock_guard<std::mutex> lk(net->net.mu);
+    std::string e = net->net.add_expr(code, n_code, consts, n_consts, differences, n_differences);
     return e.empty() ? RB_OK : fail(RB_ERR_INVALID, e);
 }
 
@@ -547,6 +558,14 @@ int rb_gillespie_add_reaction_lma_sparse(rb_gillespie *g, double rate, const uin
     if (!g) return fail(RB_ERR_INVALID, "null handle");
     std::lock_guard<std::mutex> lk(g->net.mu);
     std::string e = g->net.add_lma_sparse(rate, species, exponents, n_pairs, differences, n_differences);
+    return e.empty() ? RB_OK : fail(RB_ERR_INVALID, e);
+}
+
+int rb_gillespie_add_reaction_expr(rb_gillespie *g, const int32_t *code, int32_t n_code, const double *consts,
+                                   int32_t n_consts, const int64_t *differences, int32_t n_differences) {
+    if (!g) return fail(RB_ERR_INVALID, "null handle");
+    std::lock_guard<std::mutex> lk(g->net.mu);
+    std::string e = g->net.add_expr(code, n_code, consts, n_consts, differences, n_differences);
     return e.empty() ? RB_OK : fail(RB_ERR_INVALID, e);
 }
 

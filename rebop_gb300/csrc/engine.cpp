@@ -131,7 +131,10 @@ bool ensure_device(const Network &net) {
     size_t off_fsp = align_up(off_jd + sizeof(int64_t) * std::max<size_t>(R * Q, 1), 16);
     size_t off_ford = align_up(off_fsp + sizeof(int32_t) * std::max<size_t>(R * P, 1), 16);
     size_t off_jsp = align_up(off_ford + sizeof(int32_t) * std::max<size_t>(R * P, 1), 16);
-    size_t total = align_up(off_jsp + sizeof(int32_t) * std::max<size_t>(R * Q, 1), 16);
+    size_t off_exo = align_up(off_jsp + sizeof(int32_t) * std::max<size_t>(R * Q, 1), 16);
+    size_t off_exc = align_up(off_exo + sizeof(int32_t) * (R + 1), 16);
+    size_t off_exk = align_up(off_exc + sizeof(int32_t) * std::max<size_t>(p.ex_code.size(), 1), 16);
+    size_t total = align_up(off_exk + sizeof(double) * std::max<size_t>(p.ex_const.size(), 1), 16);
     if (dn.desc) {
         cudaFree(dn.desc);
         dn.desc = nullptr;
@@ -144,7 +147,11 @@ bool ensure_device(const Network &net) {
         std::memcpy(img.data() + off_fsp, p.fac_sp.data(), sizeof(int32_t) * R * P);
         std::memcpy(img.data() + off_ford, p.fac_ord.data(), sizeof(int32_t) * R * P);
         std::memcpy(img.data() + off_jsp, p.jmp_sp.data(), sizeof(int32_t) * R * Q);
+        std::memcpy(img.data() + off_exo, p.ex_off.data(), sizeof(int32_t) * (R + 1));
     }
+    if (!p.ex_code.empty()) std::memcpy(img.data() + off_exc, p.ex_code.data(), sizeof(int32_t) * p.ex_code.size());
+    if (!p.ex_const.empty())
+        std::memcpy(img.data() + off_exk, p.ex_const.data(), sizeof(double) * p.ex_const.size());
     if (!cuda_ok(cudaMemcpy(dn.desc, img.data(), total, cudaMemcpyHostToDevice), "cudaMemcpy(descriptor)"))
         return false;
     unsigned char *b = static_cast<unsigned char *>(dn.desc);
@@ -153,6 +160,9 @@ bool ensure_device(const Network &net) {
     dn.fac_sp = reinterpret_cast<int32_t *>(b + off_fsp);
     dn.fac_ord = reinterpret_cast<int32_t *>(b + off_ford);
     dn.jmp_sp = reinterpret_cast<int32_t *>(b + off_jsp);
+    dn.ex_off = p.has_expr ? reinterpret_cast<int32_t *>(b + off_exo) : nullptr;
+    dn.ex_code = reinterpret_cast<int32_t *>(b + off_exc);
+    dn.ex_const = reinterpret_cast<double *>(b + off_exk);
     dn.packed = std::move(p);
     dn.version = net.version;
     return true;
@@ -202,6 +212,9 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     a.fac_ord = dn.fac_ord;
     a.jmp_sp = dn.jmp_sp;
     a.jmp_d = dn.jmp_d;
+    a.ex_off = dn.ex_off;
+    a.ex_code = dn.ex_code;
+    a.ex_const = dn.ex_const;
     a.n_traj = r.n_traj;
     a.x0 = r.x0;
     a.x0_stride = r.x0_stride;
@@ -242,9 +255,10 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     const int spec_grid = (int)std::max<int64_t>(
         1, std::min<int64_t>(ctx->sm_count, (r.n_traj + ssa_spec_block() - 1) / ssa_spec_block()));
     const int spec_slots = ssa_spec_slots(a, spec_grid, ctx->smem_optin, ssa_spec_block());
-    const bool spec = !want_generic && !want_fast && r.times_ok && r.t_last < 0x1p60 &&
+    // Rate::Expr networks run on the generic kernel (native binary64 programs).
+    const bool spec = !p.has_expr && !want_generic && !want_fast && r.times_ok && r.t_last < 0x1p60 &&
                       ssa_spec_supported(a, p.max_order) && spec_slots > 0;
-    const bool fast = !spec && !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
+    const bool fast = !spec && !p.has_expr && !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
                       ssa_fast_smem(a, 128) <= ctx->smem_optin;
     if (pref && ((want_fast && !fast) || (std::strcmp(pref, "spec") == 0 && !spec))) {
         set_error(std::string("RB_SSA_KERNEL=") + pref + " does not cover this network or sample grid");

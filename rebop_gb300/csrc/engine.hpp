@@ -40,6 +40,8 @@ struct DeviceNet {
     double *rate = nullptr;
     int64_t *jmp_d = nullptr;
     int32_t *fac_sp = nullptr, *fac_ord = nullptr, *jmp_sp = nullptr;
+    int32_t *ex_off = nullptr, *ex_code = nullptr;  // ex_off null: no Rate::Expr reaction
+    double *ex_const = nullptr;
     unsigned long long *scratch = nullptr;  // [4]: trajectory ticket, event total, timeout flag
     void *io = nullptr;                 // staging for rb_ensemble_run & friends
     size_t io_bytes = 0;

@@ -8,8 +8,11 @@
 #include <map>
 
 #include "engine.hpp"
+#include "ssa_args.hpp"
 
 namespace rbg {
+
+static_assert(kExMaxDepth == kExprMaxDepth, "expression stack depth");
 
 Network::Network() = default;
 Network::~Network() = default;
@@ -86,6 +89,38 @@ std::string Network::add_lma_sparse(double rate, const uint32_t *species, const 
     return "";
 }
 
+// add_reaction with Rate::expr: the difference vector has one entry per
+// species (gillespie.rs:225-244); the program must be a well-formed postfix
+// form of an Expr tree over this network's species.
+std::string Network::add_expr(const int32_t *code, int32_t n_code, const double *consts, int32_t n_consts,
+                              const int64_t *diffs, int32_t n_diffs) {
+    if (n_code < 1 || !code) return "empty rate expression";
+    if (n_consts < 0 || (n_consts > 0 && !consts)) return "null expression constants";
+    if (n_diffs != n_species)
+        return "assertion failed: differences length " + std::to_string(n_diffs) +
+               " != number of species " + std::to_string(n_species);
+    if (n_species > 0 && !diffs) return "null difference pointer";
+    int depth = 0;
+    for (int32_t k = 0; k < n_code; k++) {
+        const int32_t op = code[k] & 0xff, arg = code[k] >> 8;
+        if (op > ExExp) return "unknown expression operation " + std::to_string(op);
+        if (op == ExConst && (arg < 0 || arg >= n_consts)) return "expression constant index out of range";
+        if (op == ExSpecies && (arg < 0 || arg >= n_species))
+            return "expression species index " + std::to_string(arg) + " out of range";
+        depth += (op <= ExSpecies) ? 1 : (op == ExNeg || op == ExExp) ? 0 : -1;
+        if (depth < 1) return "malformed rate expression";
+        if (depth > kExMaxDepth) return "rate expression nests too deeply";
+    }
+    if (depth != 1) return "malformed rate expression";
+    Reaction r;
+    r.ex_code.assign(code, code + n_code);
+    r.ex_const.assign(consts, consts + n_consts);
+    r.jump = jump_from_dense(diffs, n_diffs);
+    reactions.push_back(std::move(r));
+    version++;
+    return "";
+}
+
 std::string Network::set_param(const std::string &pname, double value) {
     for (size_t i = 0; i < param_names.size(); i++) {
         if (param_names[i] == pname) {
@@ -120,8 +155,15 @@ Packed Network::pack() const {
     p.fac_ord.assign((size_t)p.R * P, 0);
     p.jmp_sp.assign((size_t)p.R * Q, 0);
     p.jmp_d.assign((size_t)p.R * Q, 0);
+    p.ex_off.assign((size_t)p.R + 1, 0);
     for (int32_t i = 0; i < p.R; i++) {
         const Reaction &r = reactions[i];
+        const int32_t base = (int32_t)p.ex_const.size();
+        for (int32_t w : r.ex_code)
+            p.ex_code.push_back((w & 0xff) == ExConst ? (ExConst | (((w >> 8) + base) << 8)) : w);
+        p.ex_const.insert(p.ex_const.end(), r.ex_const.begin(), r.ex_const.end());
+        p.ex_off[(size_t)i + 1] = (int32_t)p.ex_code.size();
+        if (!r.ex_code.empty()) p.has_expr = 1;
         p.rate[i] = r.rate;
         for (size_t k = 0; k < r.factors.size(); k++) {
             p.fac_sp[(size_t)i * P + k] = r.factors[k].species;

@@ -38,9 +38,17 @@ struct RateExpr {
     double eval(const std::vector<double> &params) const;
 };
 
+// Rate::Expr of the run-time API (src/expr.rs:8-39) as a postfix program:
+// each word is op | argument << 8, the argument a constant index (ExConst) or
+// a species index (ExSpecies).
+enum ExOp : int32_t { ExConst = 0, ExSpecies, ExNeg, ExAdd, ExSub, ExMul, ExDiv, ExPow, ExMax, ExMin, ExExp };
+constexpr int kExMaxDepth = 16;  // evaluation stack of the device interpreter (kExprMaxDepth)
+
 struct Reaction {
     double rate = 0.0;
     std::shared_ptr<RateExpr> rate_expr;  // DSL networks only
+    std::vector<int32_t> ex_code;         // Rate::Expr: the propensity is this program's value
+    std::vector<double> ex_const;
     std::vector<Factor> factors;          // propensity multiply sequence
     std::vector<JumpEntry> jump;          // non-zero differences, ascending species
     std::string name;
@@ -57,6 +65,12 @@ struct Packed {
     std::vector<int32_t> fac_ord;   // [R*P]
     std::vector<int32_t> jmp_sp;    // [R*Q]
     std::vector<int64_t> jmp_d;     // [R*Q]
+    // Rate::Expr programs: reaction r's words are ex_code[ex_off[r] .. ex_off[r+1])
+    // (empty for mass action), constant arguments index ex_const.
+    int32_t has_expr = 0;
+    std::vector<int32_t> ex_off;    // [R+1]
+    std::vector<int32_t> ex_code;
+    std::vector<double> ex_const;
 };
 
 struct DeviceNet;  // engine.cpp
@@ -83,6 +97,9 @@ struct Network {
                         int32_t n_diffs);
     std::string add_lma_sparse(double rate, const uint32_t *species, const uint32_t *exps,
                                int32_t n_pairs, const int64_t *diffs, int32_t n_diffs);
+    // Rate::expr(program) + differences (gillespie.rs:33-35, :88)
+    std::string add_expr(const int32_t *code, int32_t n_code, const double *consts, int32_t n_consts,
+                         const int64_t *diffs, int32_t n_diffs);
     std::string set_param(const std::string &pname, double value);
     void refresh_rates();
     Packed pack() const;

@@ -6,6 +6,7 @@
 
 namespace rbg {
 
+constexpr int kExprMaxDepth = 16;  // evaluation stack of Rate::Expr programs
 constexpr int kZigLayers = 256;            // ziggurat layers of the Exp1 sampler
 constexpr int kZigTable = kZigLayers + 1;  // abscissae x[0..256] / f(x) values
 // Device table layout (doubles / u64 words): x[257] | f[257] | k[256] | d[256]
@@ -29,6 +30,11 @@ struct SsaArgs {
     const int32_t *fac_ord;  // [R*P]
     const int32_t *jmp_sp;   // [R*Q]
     const int64_t *jmp_d;    // [R*Q]
+    // Rate::Expr programs (null ex_off: none): reaction r's postfix words are
+    // ex_code[ex_off[r] .. ex_off[r+1]), empty for mass-action reactions
+    const int32_t *ex_off;
+    const int32_t *ex_code;
+    const double *ex_const;
 
     // trajectories
     int64_t n_traj;
@@ -109,6 +115,8 @@ struct EventArgs {
     const double *rate;      // [R]
     const int32_t *fac_sp, *fac_ord, *jmp_sp;
     const int64_t *jmp_d;
+    const int32_t *ex_off, *ex_code;  // as in SsaArgs
+    const double *ex_const;
     int64_t n_traj;
     int64_t *species;        // [n_traj][S] in/out
     double *t;               // [n_traj] in/out

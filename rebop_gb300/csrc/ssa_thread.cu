@@ -65,6 +65,42 @@ __device__ inline ThreadSmem thread_smem_layout(int S, int R, int P, int Q, int 
     return m;
 }
 
+// Rate::Expr propensity (expr.rs:23-39, gillespie.rs:88) in native binary64:
+// IEEE operations, powf and exp from CUDA's math library, max/min returning
+// the operand that is not NaN.  Counts are read at sp[s * stride].
+__device__ __noinline__ double expr_eval(const int32_t *code, int32_t b, int32_t e, const double *consts,
+                                         const int64_t *sp, int stride) {
+    double st[kExprMaxDepth];
+    int top = 0;
+    for (int32_t k = b; k < e; ++k) {
+        const int32_t w = code[k];
+        const int op = w & 0xff, arg = w >> 8;
+        if (op == 0) {
+            st[top++] = consts[arg];
+        } else if (op == 1) {
+            st[top++] = (double)sp[(size_t)arg * stride];
+        } else if (op == 2) {
+            st[top - 1] = -st[top - 1];
+        } else if (op == 10) {
+            st[top - 1] = exp(st[top - 1]);
+        } else {
+            const double y = st[--top], x = st[top - 1];
+            double v;
+            switch (op) {
+                case 3: v = __dadd_rn(x, y); break;
+                case 4: v = __dsub_rn(x, y); break;
+                case 5: v = __dmul_rn(x, y); break;
+                case 6: v = __ddiv_rn(x, y); break;
+                case 7: v = pow(x, y); break;
+                case 8: v = fmax(x, y); break;
+                default: v = fmin(x, y); break;
+            }
+            st[top - 1] = v;
+        }
+    }
+    return st[0];
+}
+
 template <bool MACRO>
 __global__ void __launch_bounds__(256) ssa_thread_kernel(const __grid_constant__ SsaArgs a) {
     const int BD = blockDim.x, tid = threadIdx.x;
@@ -124,6 +160,9 @@ __global__ void __launch_bounds__(256) ssa_thread_kernel(const __grid_constant__
                 total = 0.0;
                 for (int r = 0; r < R; ++r) {
                     double acc = rates[r];
+                    if (a.ex_off && a.ex_off[r] < a.ex_off[r + 1])
+                        acc = expr_eval(a.ex_code, a.ex_off[r], a.ex_off[r + 1], a.ex_const, sp, BD);
+                    else
                     for (int p = 0; p < P; ++p) {
                         const int o = m.ford[r * P + p];
                         if (o == 0) continue;
@@ -240,6 +279,8 @@ int ssa_thread_occupancy(const SsaArgs &a, int block, size_t smem) {
 // Propensity of reaction r at counts sp (API fold or macro factorials).
 template <bool MACRO>
 __device__ __forceinline__ double event_propensity(const EventArgs &a, const int64_t *sp, int r) {
+    if (a.ex_off && a.ex_off[r] < a.ex_off[r + 1])
+        return expr_eval(a.ex_code, a.ex_off[r], a.ex_off[r + 1], a.ex_const, sp, 1);
     double acc = a.rate[r];
     for (int p = 0; p < a.P; ++p) {
         const int o = a.fac_ord[r * a.P + p];
@@ -392,6 +433,8 @@ int noalloc_ensemble_run(const Network &net, int64_t n_traj, const int64_t *d_x0
     if (n_traj && S && !d_x0) return err = "null x0", 1;
     if (n_traj && !d_seeds) return err = "null seeds", 1;
     if (n_traj && NS && !d_out) return err = "null out", 1;
+    for (const Reaction &r : net.reactions)
+        if (!r.ex_code.empty()) return err = "rate expressions need the allocating entry points", 5;
     int64_t P = 1, Q = 1;
     for (const Reaction &r : net.reactions) {
         P = std::max<int64_t>(P, (int64_t)r.factors.size());

@@ -19,13 +19,30 @@ except ImportError:  # pragma: no cover
     xr = None
 
 
+class DataArray(np.ndarray):
+    """A numpy array that also answers ``.values`` and ``.dims`` like an
+    ``xarray.DataArray`` variable of the reference's result."""
+
+    dims: tuple = ()
+
+    @property
+    def values(self) -> np.ndarray:
+        return np.asarray(self)
+
+
+def _array(a, dims) -> DataArray:
+    v = np.asarray(a).view(DataArray)
+    v.dims = dims
+    return v
+
+
 class Dataset(Mapping):
     """Species name -> counts array, plus coordinates (``time``, ``trajectory``)."""
 
     def __init__(self, data_vars: Mapping[str, np.ndarray], coords: Mapping[str, np.ndarray],
                  dims: tuple[str, ...]):
-        self.data_vars = dict(data_vars)
-        self.coords = dict(coords)
+        self.data_vars = {k: _array(v, dims) for k, v in data_vars.items()}
+        self.coords = {k: _array(v, (k,)) for k, v in coords.items()}
         self.dims = dims
 
     def __getitem__(self, key):

@@ -74,6 +74,9 @@ class PExpr:
 
 
 _INFIX = {"add": "+", "sub": "-", "mul": "*", "div": "/", "pow": "^"}
+# Postfix operation codes of the engine's expression programs.
+_OPS = {"const": 0, "species": 1, "neg": 2, "add": 3, "sub": 4, "mul": 5, "div": 6, "pow": 7, "max": 8,
+        "min": 9, "exp": 10}
 
 
 @dataclass(frozen=True)
@@ -85,6 +88,27 @@ class Expr:
     index: int = -1
     a: "Expr | None" = None
     b: "Expr | None" = None
+
+    def to_program(self) -> tuple[list[int], list[float]]:
+        """Postfix form for the engine (``rb_network_add_reaction_expr``): words
+        ``op | arg << 8`` in evaluation order, and the constants they push."""
+        code: list[int] = []
+        consts: list[float] = []
+
+        def emit(e: "Expr") -> None:
+            if e.op == "const":
+                code.append(_OPS["const"] | (len(consts) << 8))
+                consts.append(float(e.value))
+            elif e.op == "species":
+                code.append(_OPS["species"] | (int(e.index) << 8))
+            else:
+                emit(e.a)
+                if e.b is not None:
+                    emit(e.b)
+                code.append(_OPS[e.op])
+
+        emit(self)
+        return code, consts
 
     def eval(self, species) -> float:
         """Host evaluation (expr.rs:23-39), for tests."""
@@ -361,10 +385,3 @@ def parse(s: str) -> PExpr:
     if p.i != len(s):
         raise ParseError(s)
     return e
-
-
-class ExprNetwork:
-    """Placeholder until the device bytecode path exists."""
-
-    def __init__(self, n_species: int):
-        raise NotImplementedError("string rate expressions are not supported on the GPU path yet")

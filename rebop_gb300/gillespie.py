@@ -114,11 +114,7 @@ class Gillespie:
                 if v not in self._species:
                     raise ValueError(f"Unknown species {v!r} in var_names")
         save = [self._species[v] for v in names]
-        has_expr = any(not isinstance(pr, float) for pr, _, _, _ in self._reactions)
-        if has_expr:
-            net = _expr.ExprNetwork(S)
-        else:
-            net = Network(S)
+        net = Network(S)
         for prate, reactants, products, _ in self._reactions:
             exps = [0] * S
             for r in reactants:
@@ -131,7 +127,8 @@ class Gillespie:
             if isinstance(prate, float):
                 net.add_reaction(Rate.lma(prate, exps), diff)
             else:
-                net.add_expr_reaction(prate.to_expr(self._species, params), diff)
+                # Rate::Expr: the expression alone is the propensity (gillespie.rs:88)
+                net.add_reaction(Rate.expression(prate.to_expr(self._species, params)), diff)
         return net, x0, names, save
 
     # -- runs
