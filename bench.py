@@ -45,7 +45,38 @@ SIR = dict(
     reactions=[(1e-4, [1, 1, 0], [-1, 1, 0]), (0.01, [0, 1, 0], [0, -1, 1])],
     x0=[999, 1, 0], tmax=250.0, nb_steps=250, n_traj=10_000, cpu_sample=10_000,
 )
-WORKLOADS = {"dimer": DIMER, "sir": SIR}
+
+
+def random_network(seed: int, S: int, R: int, rate_lo: float = 1e-4, rate_hi: float = 1e1, x0_mean: float = 200.0):
+    """Random mass-action network: every reaction takes 0-2 reactant molecules
+    (order <= 2) and makes 0-2 product molecules, stoichiometry in {-2..2}; rate
+    constants log-uniform in [rate_lo, rate_hi]; initial counts Poisson(x0_mean)."""
+    rng = np.random.default_rng(seed)
+    reactions = []
+    for _ in range(R):
+        order = int(rng.choice([0, 1, 2], p=[0.1, 0.5, 0.4]))
+        exps = [0] * S
+        diff = [0] * S
+        for sp in rng.integers(0, S, size=order):
+            exps[int(sp)] += 1
+            diff[int(sp)] -= 1
+        for sp in rng.integers(0, S, size=int(rng.integers(0, 3))):
+            diff[int(sp)] += 1
+        k = float(np.exp(rng.uniform(np.log(rate_lo), np.log(rate_hi))))
+        reactions.append((k, exps, diff))
+    x0 = rng.poisson(x0_mean, size=S).astype(np.int64).tolist()
+    return reactions, x0
+
+
+_LR, _LX0 = random_network(20260104, 200, 1000)
+LARGE = dict(
+    name="large",
+    desc=("large random mass-action network: 200 species, 1000 reactions, reactant order <= 2, rates "
+          "log-uniform in [1e-4, 1e1], x0 ~ Poisson(200) (seed 20260104); one warp per trajectory; "
+          "tmax = 4e-3 (~1e5 events per trajectory), nb_steps = 100"),
+    S=200, reactions=_LR, x0=_LX0, tmax=4e-3, nb_steps=100, n_traj=10_000, cpu_sample=16,
+)
+WORKLOADS = {"dimer": DIMER, "sir": SIR, "large": LARGE}
 
 
 def f_event(w) -> int:
@@ -120,7 +151,10 @@ def cpu_reference(w, n_traj: int, steps: int, warmup: int, threads: int) -> dict
 
     net = O.OracleNet(w["S"])
     for k, e, d in w["reactions"]:
-        net.add_lma(k, e, d)
+        if w.get("sparse"):  # Rate::lma_sparse: the reference's form for large networks
+            net.add_lma_sparse(k, [(i, x) for i, x in enumerate(e) if x], d)
+        else:
+            net.add_lma(k, e, d)
     tot_ev, tot_s = 0, 0.0
     for step in range(warmup + steps):
         seeds = seeds_for(0, 1000 + step, n_traj)
@@ -158,6 +192,8 @@ def run_reference_arm(args, w):
 # ---------------------------------------------------------------- GPU side
 # Kernel that runs each mapping (rb_run_stats.mapping) and what it is.
 MAPPINGS = {
+    5: ("ssa_warp_kernel", "warp per trajectory: lanes share the reaction list, float-pair scan, exact binary64 "
+                           "re-runs of undecided intervals"),
     4: ("rbg_net_kernel", "thread per trajectory, kernel generated for the network and compiled at run time "
                           "(NVRTC); float-pair speculation with exact binary64 re-runs"),
     3: ("ssa_spec_kernel", "thread per trajectory, packed-descriptor speculative kernel"),

@@ -100,6 +100,7 @@ DeviceNet::~DeviceNet() {
     // are ignored here.
     if (desc) cudaFree(desc);
     if (scratch) cudaFree(scratch);
+    if (warp_scratch) cudaFree(warp_scratch);
     if (io) cudaFree(io);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_stop) cudaEventDestroy(ev_stop);
@@ -258,14 +259,42 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     // Rate::Expr networks run on the generic kernel (native binary64 programs).
     const bool spec = !p.has_expr && !want_generic && !want_fast && r.times_ok && r.t_last < 0x1p60 &&
                       ssa_spec_supported(a, p.max_order) && spec_slots > 0;
-    const bool fast = !spec && !p.has_expr && !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
+    // Networks beyond the thread kernels' reach (more than 32 reactions, or
+    // too large for their shared memory) take a warp per trajectory.
+    const bool want_warp = pref && std::strcmp(pref, "warp") == 0;
+    const int warp_w = ssa_warp_supported(a, p.max_order) ? ssa_warp_warps(a, ctx->smem_optin) : 0;
+    const bool warp = warp_w > 0 && !want_generic && !p.has_expr &&
+                      (want_warp || (!spec && !(p.R <= 32 && ssa_thread_max_block(a, ctx->smem_optin) > 0)));
+    const bool fast = !warp && !spec && !p.has_expr && !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
                       ssa_fast_smem(a, 128) <= ctx->smem_optin;
-    if (pref && ((want_fast && !fast) || (std::strcmp(pref, "spec") == 0 && !spec))) {
+    if (pref && ((want_fast && !fast) || (want_warp && !warp) || (std::strcmp(pref, "spec") == 0 && !spec))) {
         set_error(std::string("RB_SSA_KERNEL=") + pref + " does not cover this network or sample grid");
         return false;
     }
     int block, per_sm;
     size_t smem;
+    if (warp) {
+        block = 32 * warp_w;
+        smem = ssa_warp_smem(a, warp_w);
+        per_sm = std::max(1, ssa_warp_occupancy(a, warp_w, smem));
+        const int64_t blocks = std::max<int64_t>(
+            1, std::min<int64_t>((r.n_traj + warp_w - 1) / warp_w, (int64_t)ctx->sm_count * per_sm));
+        const size_t need = (size_t)blocks * warp_w * std::max<int32_t>(p.R, 1) * sizeof(double);
+        if (dn.warp_scratch_bytes < need) {
+            if (dn.warp_scratch) cudaFree(dn.warp_scratch);
+            dn.warp_scratch = nullptr;
+            dn.warp_scratch_bytes = 0;
+            if (!cuda_ok(cudaMalloc(&dn.warp_scratch, need), "cudaMalloc(warp scratch)")) return false;
+            dn.warp_scratch_bytes = need;
+        }
+        a.warp_scratch = dn.warp_scratch;
+        if (timed && !cuda_ok(cudaEventRecord(dn.ev_start, stream), "cudaEventRecord")) return false;
+        const int err = launch_ssa_warp(a, warp_w, (int)blocks, smem, stream);
+        if (err != 0) return cuda_ok((cudaError_t)err, "SSA kernel launch");
+        if (timed && !cuda_ok(cudaEventRecord(dn.ev_stop, stream), "cudaEventRecord")) return false;
+        if (mapping) *mapping = 5;
+        return true;
+    }
     if (spec) {
         block = ssa_spec_block();
         a.n_slots = spec_slots;

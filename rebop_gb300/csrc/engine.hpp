@@ -43,6 +43,8 @@ struct DeviceNet {
     int32_t *ex_off = nullptr, *ex_code = nullptr;  // ex_off null: no Rate::Expr reaction
     double *ex_const = nullptr;
     unsigned long long *scratch = nullptr;  // [4]: trajectory ticket, event total, timeout flag
+    double *warp_scratch = nullptr;         // exact steps of the warp-per-trajectory kernel
+    size_t warp_scratch_bytes = 0;
     void *io = nullptr;                 // staging for rb_ensemble_run & friends
     size_t io_bytes = 0;
     cudaStream_t stream = nullptr;      // library stream of host-pointer calls

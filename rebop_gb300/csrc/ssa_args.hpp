@@ -79,6 +79,10 @@ struct SsaArgs {
     // Speculative kernel: steps between two compactions of a warp's slots
     // (0: the default).
     int32_t phase_steps;
+
+    // Warp-per-trajectory kernel: [grid * warps per block][R] doubles of
+    // scratch for its exact steps.
+    double *warp_scratch;
 };
 
 // Launch the thread-per-trajectory kernel; returns a cudaError_t value.
@@ -105,6 +109,15 @@ size_t ssa_spec_smem(const SsaArgs &a, int slots);
 int ssa_spec_slots(const SsaArgs &a, int grid, size_t smem_limit, int block);
 int ssa_spec_occupancy(const SsaArgs &a, int block, size_t smem);
 int launch_ssa_spec(const SsaArgs &a, int block, int grid, size_t smem, void *stream);
+
+// Warp-per-trajectory kernel for large networks (ssa_warp.cu): any network
+// without rate expressions.  ssa_warp_warps gives the warps per block that fit
+// in smem_limit (0: none).
+bool ssa_warp_supported(const SsaArgs &a, int max_order);
+int ssa_warp_warps(const SsaArgs &a, size_t smem_limit);
+size_t ssa_warp_smem(const SsaArgs &a, int warps);
+int ssa_warp_occupancy(const SsaArgs &a, int warps, size_t smem);
+int launch_ssa_warp(const SsaArgs &a, int warps, int grid, size_t smem, void *stream);
 
 // Every-event runs (src/pyo3_gillespie.rs:209-223) and single
 // _advance_one_reaction steps (src/gillespie.rs:269-297): one thread per

@@ -418,3 +418,63 @@ def test_generated_network_kernel_matches_oracle(rb, O):
          .add_macro(0.1, [(1, 1)], [0, -1, 0, 0]).add_macro(1.0, [(2, 1)], [0, 0, -1, 0]))
     ref, ev, _, _ = o.run_ensemble([1, 0, 0, 0], seeds[:600], 0.5, 10)
     np.testing.assert_array_equal(res.counts, ref)
+
+
+def _random_net(rb, O, seed, S, R, x0_mean):
+    import bench
+
+    reactions, x0 = bench.random_network(seed, S, R, x0_mean=x0_mean)
+    net = rb.Network(S)
+    onet = O.OracleNet(S)
+    for k, e, d in reactions:
+        net.add_reaction(rb.Rate.lma(k, e), d)
+        onet.add_lma_sparse(k, [(i, x) for i, x in enumerate(e) if x], d)
+    return net, onet, x0
+
+
+def test_warp_kernel_matches_oracle(rb, O):
+    # Warp per trajectory: a random network beyond the thread kernels (chosen
+    # by the dispatcher), then small networks forced onto it.
+    net, onet, x0 = _random_net(rb, O, 7, 40, 120, 60.0)
+    seeds = _seeds(64, 61)
+    res = net.run_ensemble(x0, seeds, 2e-2, 12)
+    ref, ev, tot, _ = onet.run_ensemble(x0, seeds, 2e-2, 12)
+    assert res.stats["mapping"] == 5
+    assert ev.min() > 200
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+    assert res.total_events == tot
+    seeds = _seeds(300, 62)
+    res = _with_kernel("warp", lambda: _dimer(rb).run_ensemble([1, 0, 0, 0], seeds, 0.3, 6))
+    ref, ev, _, _ = O.dimer_net().run_ensemble([1, 0, 0, 0], seeds, 0.3, 6)
+    assert res.stats["mapping"] == 5
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+    # per-trajectory rates, some outside the float-pair range (exact intervals)
+    rng = np.random.default_rng(12)
+    rates = np.stack([10 ** rng.uniform(-5, -3, 300), 10 ** rng.uniform(-3, -1, 300)], axis=1)
+    rates[::40, 0] = 1e-25
+    rates[::55, 1] = np.nan
+    res = _with_kernel("warp", lambda: _sir(rb).run_ensemble([999, 1, 0], seeds, 150.0, 15, rates=rates))
+    ref, ev, _, _ = O.sir_net().run_ensemble([999, 1, 0], seeds, 150.0, 15, rates=rates)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+    # counts that go negative
+    n2 = rb.Network(2)
+    n2.add_reaction(rb.Rate.lma(1.0, [0, 1]), [-1, 0])
+    n2.add_reaction(rb.Rate.lma(0.5, [1, 0]), [0, 1])
+    o2 = O.OracleNet(2).add_lma(1.0, [0, 1], [-1, 0]).add_lma(0.5, [1, 0], [0, 1])
+    res = _with_kernel("warp", lambda: n2.run_ensemble([3, 5], seeds[:100], 3.0, 6))
+    ref, ev, _, _ = o2.run_ensemble([3, 5], seeds[:100], 3.0, 6)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+    # macro arithmetic
+    D = rb.define_system(DIMER_DSL)
+    d = D.with_parameters(25.0, 1000.0, 0.001, 0.1, 1.0)
+    d.gene = 1
+    res = _with_kernel("warp", lambda: d.run_ensemble(seeds[:200], 0.3, 5))
+    o = (O.OracleNet(4, macro=True).add_macro(25.0, [(0, 1)], [0, 1, 0, 0])
+         .add_macro(1000.0, [(1, 1)], [0, 0, 1, 0]).add_macro(0.001, [(2, 2)], [0, 0, -2, 1])
+         .add_macro(0.1, [(1, 1)], [0, -1, 0, 0]).add_macro(1.0, [(2, 1)], [0, 0, -1, 0]))
+    ref, ev, _, _ = o.run_ensemble([1, 0, 0, 0], seeds[:200], 0.3, 5)
+    np.testing.assert_array_equal(res.counts, ref)
