@@ -48,19 +48,27 @@ SIR = dict(
 
 
 def random_network(seed: int, S: int, R: int, rate_lo: float = 1e-4, rate_hi: float = 1e1, x0_mean: float = 200.0):
-    """Random mass-action network: every reaction takes 0-2 reactant molecules
-    (order <= 2) and makes 0-2 product molecules, stoichiometry in {-2..2}; rate
-    constants log-uniform in [rate_lo, rate_hi]; initial counts Poisson(x0_mean)."""
+    """Random mass-action network that keeps its activity: reactions take 0-2
+    reactant molecules (order <= 2) and mostly give back as many product
+    molecules (conversions A -> B, exchanges A + B -> C + D), with a few
+    inflows, degradations and bindings, so stoichiometries stay in {-2..2};
+    rate constants log-uniform in [rate_lo, rate_hi]; counts Poisson(x0_mean)."""
     rng = np.random.default_rng(seed)
     reactions = []
     for _ in range(R):
-        order = int(rng.choice([0, 1, 2], p=[0.1, 0.5, 0.4]))
+        order = int(rng.choice([0, 1, 2], p=[0.05, 0.5, 0.45]))
+        if order == 0:
+            n_prod = 1
+        elif order == 1:
+            n_prod = 1 if rng.random() < 0.9 else 0
+        else:
+            n_prod = 2 if rng.random() < 0.9 else 1
         exps = [0] * S
         diff = [0] * S
         for sp in rng.integers(0, S, size=order):
             exps[int(sp)] += 1
             diff[int(sp)] -= 1
-        for sp in rng.integers(0, S, size=int(rng.integers(0, 3))):
+        for sp in rng.integers(0, S, size=n_prod):
             diff[int(sp)] += 1
         k = float(np.exp(rng.uniform(np.log(rate_lo), np.log(rate_hi))))
         reactions.append((k, exps, diff))
@@ -73,8 +81,8 @@ LARGE = dict(
     name="large",
     desc=("large random mass-action network: 200 species, 1000 reactions, reactant order <= 2, rates "
           "log-uniform in [1e-4, 1e1], x0 ~ Poisson(200) (seed 20260104); one warp per trajectory; "
-          "tmax = 4e-3 (~1e5 events per trajectory), nb_steps = 100"),
-    S=200, reactions=_LR, x0=_LX0, tmax=4e-3, nb_steps=100, n_traj=10_000, cpu_sample=16,
+          "tmax = 1.5 (~1e5 events per trajectory), nb_steps = 100"),
+    S=200, reactions=_LR, x0=_LX0, tmax=1.5, nb_steps=100, n_traj=10_000, cpu_sample=32, sparse=True,
 )
 WORKLOADS = {"dimer": DIMER, "sir": SIR, "large": LARGE}
 

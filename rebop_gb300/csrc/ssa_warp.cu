@@ -37,20 +37,29 @@ struct WarpLayout {
     size_t block_bytes, warp_bytes;
 };
 
+// Lane l owns the C = ceil(R / 32) reactions l*C .. l*C + C - 1.  Arrays the
+// lanes walk together are stored lane-major -- reaction l*C + i at position
+// i*32 + l -- so one step of the walk touches 32 consecutive words.
+__host__ __device__ inline int warp_chunk(int R) { return (R + 31) / 32; }
+
 // Shared memory: block tables (Exp1 tables, float-pair rates when shared,
-// reactant factors), then per warp: counts, counts at the interval start,
-// float-pair propensities (and float-pair rates when per trajectory).
+// reactant factors in both layouts, jumps), then per warp: counts, counts at
+// the interval start, float-pair propensities (and float-pair rates when per
+// trajectory).
 __host__ __device__ inline WarpLayout warp_layout(const SsaArgs &a) {
     WarpLayout l;
+    const size_t RP = 32 * (size_t)warp_chunk(a.R);     // lane-major positions
     size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;  // zxk, zf, zd, xdf
-    b += 8 * (size_t)a.R;                               // shared float-pair rates
-    b += 4 * (size_t)a.R * a.P;                         // factors
+    b += 8 * RP;                                        // shared float-pair rates (lane-major)
+    b += 4 * (size_t)a.R * a.P + 4 * RP * a.P;          // factors: reaction-major, lane-major
+    b += 4 * RP;                                        // two-slot reaction shapes (lane-major)
     b += 4 * (size_t)a.R * a.Q + 8 * (size_t)a.R * a.Q; // jumps (exact tables' layout)
     b += 16;                                            // alignment of the jump deltas
     l.block_bytes = (b + 15) & ~(size_t)15;
     size_t w = 16 * (size_t)a.S;                        // counts, interval-start counts
-    w += 8 * (size_t)a.R;                               // propensities
-    if (a.rate_stride) w += 8 * (size_t)a.R;            // per-trajectory float-pair rates
+    w += 4 * ((size_t)a.S + 1);                         // counts as floats, plus the constant 1
+    w += 8 * RP + 8;                                    // propensities (lane-major), alignment
+    if (a.rate_stride) w += 8 * RP;                     // per-trajectory float-pair rates
     l.warp_bytes = (w + 15) & ~(size_t)15;
     return l;
 }
@@ -140,7 +149,10 @@ __device__ __noinline__ int warp_exact_step(const SsaArgs &a, const int32_t *fac
     return 1;
 }
 
-template <bool MACRO>
+// SHAPE2: every reaction has reactant order <= 2, so its propensity is
+// rate * max(n1 - o1, 0) * max(n2 - o2, 0) over two (species, offset) slots
+// -- species S is a constant 1 -- and the propensity pass has no branches.
+template <bool MACRO, bool SHAPE2>
 __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __grid_constant__ SsaArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
     const int S = a.S, R = a.R, P = a.P, Q = a.Q;
@@ -151,8 +163,11 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
     uint64_t *zf = reinterpret_cast<uint64_t *>(zxk + 256);
     uint64_t *zd = zf + 257;
     float2 *xdf = reinterpret_cast<float2 *>(zd + 256);
+    const int C = warp_chunk(R), RP = 32 * C;
     float2 *rdf_sh = xdf + 256;
-    int32_t *fac = reinterpret_cast<int32_t *>(rdf_sh + R);
+    int32_t *facl = reinterpret_cast<int32_t *>(rdf_sh + RP);  // [C][P][32] lane-major factors
+    uint32_t *shape = reinterpret_cast<uint32_t *>(facl + (size_t)RP * P);  // [RP] lane-major
+    int32_t *fac = reinterpret_cast<int32_t *>(shape + RP);
     int32_t *jsp = fac + (size_t)R * P;
     int64_t *jd = reinterpret_cast<int64_t *>(
         (reinterpret_cast<uintptr_t>(jsp + (size_t)R * Q) + 7) & ~(uintptr_t)7);
@@ -161,11 +176,30 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
         const double v = a.zig[kZigOffXdf + k];
         xdf[k] = *reinterpret_cast<const float2 *>(&v);
     }
-    if (!a.rate_stride)
-        for (int r = tid; r < R; r += blockDim.x) {
-            const DF d = df_from_double(a.rate[r]);
-            rdf_sh[r] = make_float2(d.h, d.l);
+    // lane-major copies: reaction r = l*C + i at position i*32 + l (padding
+    // positions hold rate 0 and no factors)
+    for (int q = tid; q < RP; q += blockDim.x) {
+        const int i = q >> 5, l = q & 31, r = l * C + i;
+        if (!a.rate_stride) {
+            const DF d = r < R ? df_from_double(a.rate[r]) : DF{0.f, 0.f};
+            rdf_sh[q] = make_float2(d.h, d.l);
         }
+        for (int p = 0; p < P; ++p)
+            facl[(i * P + p) * 32 + l] = r < R ? (a.fac_sp[r * P + p] | (a.fac_ord[r * P + p] << 16)) : 0;
+        if (SHAPE2) {
+            // slots (species, offset): 2A -> (A,0)(A,1); A+B -> (A,0)(B,0); A -> (A,0)(1); none -> (1)(1)
+            uint32_t sl[2] = {(uint32_t)S, (uint32_t)S}, of[2] = {0, 0};
+            int k = 0;
+            for (int p = 0; r < R && p < P; ++p) {
+                const int o = a.fac_ord[r * P + p];
+                for (int j = 0; j < o && k < 2; ++j, ++k) {
+                    sl[k] = (uint32_t)a.fac_sp[r * P + p];
+                    of[k] = (uint32_t)j;
+                }
+            }
+            shape[q] = sl[0] | of[0] << 15 | sl[1] << 16 | of[1] << 31;
+        }
+    }
     __syncthreads();
     const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
 
@@ -173,15 +207,17 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
     unsigned char *wbase = g_spec_smem + L.block_bytes + (size_t)warp * L.warp_bytes;
     int64_t *cnt = reinterpret_cast<int64_t *>(wbase);
     int64_t *cnt0 = cnt + S;
-    float2 *prop = reinterpret_cast<float2 *>(cnt0 + S);
-    float2 *rdf = a.rate_stride ? prop + R : rdf_sh;
+    float *cntf = reinterpret_cast<float *>(cnt0 + S);                                  // [S + 1]
+    float2 *prop = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(cntf + S + 1) + 7) & ~(uintptr_t)7);
+    float2 *rdf = a.rate_stride ? prop + RP : rdf_sh;      // lane-major
     double *scr = a.warp_scratch + ((size_t)blockIdx.x * nw + warp) * (size_t)R;
 
-    // lane l owns reactions [l * C, min(R, (l + 1) * C))
-    const int C = (R + 31) / 32;
+    // lane l owns reactions [l * C, min(R, (l + 1) * C)); local index i sits at i*32 + l
     const int r_lo = min(R, lane * C), r_hi = min(R, r_lo + C);
+    const int n_own = r_hi - r_lo;
     const float gam = kGamma;
-    const float c_tot = (float)(a.max_mults + 1 + C + 5) * gam + (float)(R + a.max_mults + 4) * 0x1p-53f;
+    const int mm = SHAPE2 ? 2 : a.max_mults;  // multiplies per propensity
+    const float c_tot = (float)(mm + 1 + C + 5) * gam + (float)(R + mm + 4) * 0x1p-53f;
     const float c_q = c_tot + 6.0f * gam;
     const float c_sel = 2.0f * (c_tot + (float)(C + 4) * gam);
     const int64_t t_start = global_ns();
@@ -210,15 +246,15 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
         }
         const double *rates = a.rate + traj * a.rate_stride;
         bool exact_traj = !spec_rate_ok((uint64_t)__double_as_longlong(t)) || !(t < 0x1p60);
-        for (int r = lane; r < R; r += 32) {
-            const uint64_t rb = (uint64_t)__double_as_longlong(rates[r]);
-            exact_traj |= !spec_rate_ok(rb);
-            if (a.rate_stride) {
-                const DF d = df_from_double(rates[r]);
-                rdf[r] = make_float2(d.h, d.l);
+        for (int r = lane; r < R; r += 32) exact_traj |= !spec_rate_ok((uint64_t)__double_as_longlong(rates[r]));
+        if (a.rate_stride)
+            for (int q = lane; q < RP; q += 32) {
+                const int r = (q & 31) * C + (q >> 5);
+                const DF d = r < R ? df_from_double(rates[r]) : DF{0.f, 0.f};
+                rdf[q] = make_float2(d.h, d.l);
             }
-        }
         exact_traj = __any_sync(0xffffffffu, exact_traj);
+        for (int s = lane; s <= S; s += 32) cntf[s] = s < S ? (float)cnt[s] : 1.0f;
         __syncwarp();
         unsigned long long ev = 0;
 
@@ -246,11 +282,24 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                 // ---- float-pair propensities of this lane's chunk and their sum
                 DF ls{0.f, 0.f};
                 bool amb = false;
-                for (int r = r_lo; r < r_hi; ++r) {
-                    const float2 k = rdf[r];
+                if (SHAPE2) {
+                    for (int i = 0; i < n_own; ++i) {
+                        const float2 k = rdf[i * 32 + lane];
+                        const uint32_t w = shape[i * 32 + lane];
+                        const float n1 = cntf[w & 0x7FFFu], n2 = cntf[(w >> 16) & 0x7FFFu];
+                        amb |= !(n1 >= 0.0f && n1 < 8388608.0f && n2 >= 0.0f && n2 < 8388608.0f);
+                        const float f1 = fmaxf(__fsub_rn(n1, (float)((w >> 15) & 1u)), 0.0f);
+                        const float f2 = fmaxf(__fsub_rn(n2, (float)(w >> 31)), 0.0f);
+                        const DF acc = df_mul_fu(df_mul_fu(DF{k.x, k.y}, f1), f2);
+                        prop[i * 32 + lane] = make_float2(acc.h, acc.l);
+                        ls = df_add(ls, acc);
+                    }
+                } else
+                for (int i = 0; i < n_own; ++i) {
+                    const float2 k = rdf[i * 32 + lane];
                     DF acc{k.x, k.y};
                     for (int p = 0; p < P; ++p) {
-                        const int f = fac[r * P + p];
+                        const int f = facl[(i * P + p) * 32 + lane];
                         const int o = f >> 16;
                         if (o == 0) continue;
                         const int64_t n = cnt[f & 0xFFFF];
@@ -260,7 +309,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                             acc = df_mul_fu(acc, f23((uint32_t)x & 0x7FFFFFu));
                         }
                     }
-                    prop[r] = make_float2(acc.h, acc.l);
+                    prop[i * 32 + lane] = make_float2(acc.h, acc.l);
                     ls = df_add(ls, acc);
                 }
                 // inclusive scan of the chunk sums
@@ -322,28 +371,46 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                 const unsigned int below = __ballot_sync(0xffffffffu, di < 0.0f);
                 bool close = fabsf(di) <= msel;
                 const int k = __popc(below);  // chunks entirely below the choice
-                int local = 0;
-                if (lane == k && k < 32) {
-                    DF run = excl;
-                    for (int r = r_lo; r < r_hi; ++r) {
-                        const float2 pa = prop[r];
-                        run = df_add(run, DF{pa.x, pa.y});
-                        const float dr = __fadd_rn(__fsub_rn(run.h, ch.h), __fsub_rn(run.l, ch.l));
-                        local += dr < 0.0f ? 1 : 0;
-                        close |= fabsf(dr) <= msel;
+                // walk chunk k with the whole warp: lane j takes its reaction k*C + j
+                int idx = R;
+                if (k < 32) {
+                    DF carry = shfl_df(excl, k);
+                    int count = 0;
+                    for (int seg = 0; seg < C; seg += 32) {
+                        const int j = seg + lane;
+                        const bool valid = j < C && k * C + j < R;
+                        DF v{0.f, 0.f};
+                        if (valid) {
+                            const float2 pa = prop[j * 32 + k];
+                            v = DF{pa.x, pa.y};
+                        }
+#pragma unroll
+                        for (int dd2 = 1; dd2 < 32; dd2 <<= 1) {
+                            const DF o = shfl_up_df(v, dd2);
+                            if (lane >= dd2) v = df_add(o, v);
+                        }
+                        const DF cum = df_add(carry, v);
+                        const float dr = __fadd_rn(__fsub_rn(cum.h, ch.h), __fsub_rn(cum.l, ch.l));
+                        count += __popc(__ballot_sync(0xffffffffu, valid && dr < 0.0f));
+                        close |= valid && fabsf(dr) <= msel;
+                        carry = shfl_df(cum, 31);
                     }
+                    idx = k * C + count;
                 }
                 if (__any_sync(0xffffffffu, close)) {
                     replay = true;
                     break;
                 }
-                int idx = (k < 32) ? min(R, k * C) + __shfl_sync(0xffffffffu, local, k) : R;
                 // ---- jump
                 ++ev;
                 if (idx < R)
                     for (int q = lane; q < Q; q += 32) {
                         const int64_t dlt = jd[idx * Q + q];
-                        if (dlt != 0) cnt[jsp[idx * Q + q]] += dlt;
+                        if (dlt != 0) {
+                            const int sp = jsp[idx * Q + q];
+                            cnt[sp] += dlt;
+                            cntf[sp] = __fadd_rn(cntf[sp], (float)dlt);
+                        }
                     }
                 __syncwarp();
             }
@@ -375,6 +442,8 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                     __syncwarp();
                 }
                 if (abort_run) break;
+                for (int s = lane; s < S; s += 32) cntf[s] = (float)cnt[s];
+                __syncwarp();
             }
             // ---- record sample i at t = T
             t = T;
@@ -404,9 +473,9 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
     if (lane == 0 && warp_events) atomicAdd(a.work + 1, warp_events);
 }
 
-template <bool MACRO>
+template <bool MACRO, bool SHAPE2>
 int warp_launch(const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st) {
-    auto kern = ssa_warp_kernel<MACRO>;
+    auto kern = ssa_warp_kernel<MACRO, SHAPE2>;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return (int)err;
     kern<<<grid, block, smem, st>>>(a);
@@ -432,20 +501,21 @@ bool ssa_warp_supported(const SsaArgs &a, int max_order) {
 
 int ssa_warp_occupancy(const SsaArgs &a, int warps, size_t smem) {
     int n = 0;
-    if (a.macro_mode) {
-        cudaFuncSetAttribute(ssa_warp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_warp_kernel<true>, 32 * warps, smem);
-    } else {
-        cudaFuncSetAttribute(ssa_warp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_warp_kernel<false>, 32 * warps, smem);
-    }
+    // all instances share the block shape and shared memory use
+    cudaFuncSetAttribute(ssa_warp_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_warp_kernel<false, true>, 32 * warps, smem);
     return n;
 }
 
 int launch_ssa_warp(const SsaArgs &a, int warps, int grid, size_t smem, void *stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    return a.macro_mode ? warp_launch<true>(a, 32 * warps, grid, smem, st)
-                        : warp_launch<false>(a, 32 * warps, grid, smem, st);
+    // two-slot shapes need reactant order <= 2 and species indices below 2^15
+    const bool shape2 = a.max_mults <= 2 && a.S < 32767;
+    if (a.macro_mode)
+        return shape2 ? warp_launch<true, true>(a, 32 * warps, grid, smem, st)
+                      : warp_launch<true, false>(a, 32 * warps, grid, smem, st);
+    return shape2 ? warp_launch<false, true>(a, 32 * warps, grid, smem, st)
+                  : warp_launch<false, false>(a, 32 * warps, grid, smem, st);
 }
 
 }  // namespace rbg
