@@ -57,7 +57,9 @@ typedef struct {
     uint64_t d2h_bytes;    /* device->host bytes copied by the call         */
     int32_t kernel_launches;
     int32_t mapping;       /* kernel that ran: 0 generic thread-per-trajectory,
-                            * 2 lockstep exact, 3 speculative float-pair */
+                            * 2 lockstep exact, 3 speculative float-pair,
+                            * 4 speculative generated for the network (NVRTC),
+                            * 5 warp per trajectory, 6 batch graph */
     uint64_t exact_reruns; /* sample intervals the speculative kernel re-ran
                             * exactly because a decision fell inside its
                             * error margin */
@@ -204,6 +206,36 @@ int rb_trajectory_advance_until(const rb_network *net, int64_t *species, double 
 /* The generator state SmallRng::seed_from_u64(seed) starts from
  * (src/gillespie.rs:184; gillespie_macro.rs:81-84). */
 void rb_rng_state_from_seed(uint64_t seed, uint64_t *state);
+
+/* ------------------------------------------------ heterogeneous batch ---
+ * No counterpart in the reference, which runs one network and one parameter
+ * set per call.  A batch holds many ensembles -- different networks, rate
+ * constants, initial counts, horizons, trajectory counts -- and runs them all
+ * with one CUDA graph: ensembles of one network structure and sample grid
+ * merge into a single thread-per-trajectory launch with per-trajectory rates
+ * and counts; the rest share one warp-per-trajectory launch that takes the
+ * items with the most estimated work first.  Every result equals what
+ * rb_ensemble_run gives for the same item, bit for bit. */
+typedef struct rb_batch rb_batch;
+int rb_batch_create(rb_batch **out);
+void rb_batch_destroy(rb_batch *b);
+/* Add one ensemble.  Arguments mean what they mean for rb_ensemble_run; the
+ * host buffers (x0, rates, seeds, save_idx, out, events) are kept by pointer
+ * and must outlive the batch: every rb_batch_run reads the inputs' current
+ * contents and writes the outputs.  A network must not change after it is
+ * added (RB_ERR_INVALID at run time). */
+int rb_batch_add(rb_batch *b, const rb_network *net, int64_t n_traj, const int64_t *x0, int32_t x0_per_traj,
+                 const double *rates, int32_t rates_per_traj, const uint64_t *seeds, double tmax,
+                 int64_t nb_steps, const int32_t *save_idx, int32_t n_save, int64_t *out, uint64_t *events);
+/* Run every ensemble.  The first run plans, uploads the tables and captures
+ * the graph; later runs replay it.  stats->kernel_ms is the graph's device
+ * time (copies included), stats->kernel_launches its kernel count. */
+int rb_batch_run(rb_batch *b, rb_run_stats *stats);
+/* The launch classes the planner forms (no GPU needed), and the kernel an
+ * item runs on (rb_run_stats.mapping codes; 4 until the first run confirms
+ * whether the generated kernel compiled). */
+int rb_batch_plan(rb_batch *b, int32_t *n_thread_launches, int32_t *n_warp_items);
+int rb_batch_item_mapping(const rb_batch *b, int32_t item, int32_t *mapping);
 
 /* ------------------------------------------ stateful single trajectory ---
  * The Rust API's `Gillespie` object (src/gillespie.rs:157-344) with the same

@@ -81,6 +81,13 @@ _SIGS = {
                           C.c_int),
     "rb_trajectory_advance_until": ([_vp, P(_i64), P(_f64), P(_u64), _f64], C.c_int),
     "rb_rng_state_from_seed": ([_u64, P(_u64)], None),
+    "rb_batch_create": ([P(_vp)], C.c_int),
+    "rb_batch_destroy": ([_vp], None),
+    "rb_batch_add": ([_vp, _vp, _i64, P(_i64), _i32, P(_f64), _i32, P(_u64), _f64, _i64, P(_i32), _i32, P(_i64),
+                      P(_u64)], C.c_int),
+    "rb_batch_run": ([_vp, P(RunStats)], C.c_int),
+    "rb_batch_plan": ([_vp, P(_i32), P(_i32)], C.c_int),
+    "rb_batch_item_mapping": ([_vp, _i32, P(_i32)], C.c_int),
     "rb_gillespie_new": ([P(_i64), _i32, _i32, P(_vp)], C.c_int),
     "rb_gillespie_new_with_seed": ([P(_i64), _i32, _i32, _u64, P(_vp)], C.c_int),
     "rb_gillespie_free": ([_vp], None),

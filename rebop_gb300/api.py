@@ -380,6 +380,77 @@ class Gillespie:
         check(lib.rb_gillespie_advance_until(self._h, float(tmax)))
 
 
+class Batch:
+    """Many ensembles -- different networks, parameters, horizons -- run by one
+    CUDA graph (``rb_batch_*``).  ``add`` returns the item's index; after
+    ``run``, ``counts(k)`` and ``events(k)`` hold its results, identical to
+    ``Network.run_ensemble`` on the same item."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib.rb_batch_create(C.byref(h)))
+        self._h = h
+        self._keep = []   # inputs and outputs the library points to
+        self._out = []
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib.rb_batch_destroy(h)
+            self._h = None
+
+    def add(self, network: "Network", x0, seeds, tmax: float, nb_steps: int, *, rates=None, save=None,
+            want_events: bool = True) -> int:
+        S, R = network.nb_species, network.nb_reactions
+        seeds = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(-1))
+        n = seeds.size
+        x0 = np.ascontiguousarray(np.asarray(x0, dtype=np.int64))
+        x0_per = 1 if x0.ndim == 2 else 0
+        if x0.size != (n * S if x0_per else S):
+            raise ValueError("x0 must have one count per species, or one row per trajectory")
+        r_arr, r_per = None, 0
+        if rates is not None:
+            r_arr = np.ascontiguousarray(np.asarray(rates, dtype=np.float64))
+            r_per = 1 if r_arr.ndim == 2 else 0
+            if r_arr.size != (n * R if r_per else R):
+                raise ValueError("rates must have one entry per reaction, or one row per trajectory")
+        save_arr, n_save = (None, -1) if save is None else (np.ascontiguousarray(np.asarray(save, np.int32)), len(save))
+        ns = S if n_save < 0 else n_save
+        out = np.zeros((int(nb_steps) + 1, ns, n), dtype=np.int64)
+        ev = np.zeros(n, dtype=np.uint64) if want_events else None
+        check(lib.rb_batch_add(self._h, network._h, n, ptr(x0, _i64), x0_per, ptr(r_arr, _f64), r_per,
+                               ptr(seeds, _u64), float(tmax), int(nb_steps), ptr(save_arr, _i32), n_save,
+                               ptr(out, _i64), ptr(ev, _u64)))
+        self._keep.append((network, seeds, x0, r_arr, save_arr))
+        self._out.append((out, ev))
+        return len(self._out) - 1
+
+    def seeds(self, k: int) -> np.ndarray:
+        """Item k's seed array: change it in place between runs for fresh trajectories."""
+        return self._keep[k][1]
+
+    def run(self) -> dict:
+        st = RunStats()
+        check(lib.rb_batch_run(self._h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in RunStats._fields_}
+
+    def counts(self, k: int) -> np.ndarray:
+        return self._out[k][0]
+
+    def events(self, k: int):
+        return self._out[k][1]
+
+    def plan(self) -> tuple[int, int]:
+        a, b = C.c_int32(), C.c_int32()
+        check(lib.rb_batch_plan(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def mapping(self, k: int) -> int:
+        m = C.c_int32()
+        check(lib.rb_batch_item_mapping(self._h, int(k), C.byref(m)))
+        return m.value
+
+
 def zig_tables() -> tuple[np.ndarray, np.ndarray]:
     """The Exp1 ziggurat tables the engine uploads (for tests)."""
     x = np.empty(257)

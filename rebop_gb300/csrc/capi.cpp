@@ -7,6 +7,7 @@
 #include <random>
 
 #include "engine.hpp"
+#include "batch.hpp"
 #include "ssa_jit.hpp"
 #include "network.hpp"
 
@@ -640,6 +641,75 @@ int rbg_internal_jit_compile(const rb_network *net, uint64_t *image_bytes) {
     size_t n = 0;
     if (!rbg::jit_compile(p, 512, &n)) return RB_ERR_UNSUPPORTED;
     if (image_bytes) *image_bytes = n;
+    return RB_OK;
+}
+
+// ---------------------------------------------------------------- batch
+struct rb_batch {
+    rbg::Batch b;
+};
+
+int rb_batch_create(rb_batch **out) {
+    if (!out) return fail(RB_ERR_INVALID, "null argument");
+    *out = new (std::nothrow) rb_batch();
+    return *out ? RB_OK : fail(RB_ERR_NOMEM, "out of host memory");
+}
+
+void rb_batch_destroy(rb_batch *b) { delete b; }
+
+int rb_batch_add(rb_batch *b, const rb_network *net, int64_t n_traj, const int64_t *x0, int32_t x0_per_traj,
+                 const double *rates, int32_t rates_per_traj, const uint64_t *seeds, double tmax, int64_t nb_steps,
+                 const int32_t *save_idx, int32_t n_save, int64_t *out, uint64_t *events) {
+    if (!b || !net) return fail(RB_ERR_INVALID, "null argument");
+    rbg::Batch::ItemIn in;
+    in.n_traj = n_traj;
+    in.x0 = x0;
+    in.x0_per_traj = x0_per_traj;
+    in.rates = rates;
+    in.rates_per_traj = rates_per_traj;
+    in.seeds = seeds;
+    in.tmax = tmax;
+    in.nb_steps = nb_steps;
+    in.save_idx = save_idx;
+    in.n_save = n_save;
+    in.out = out;
+    in.events = events;
+    b->b.free_device_if_built();
+    const std::string e = b->b.add(&net->net, in);
+    return e.empty() ? RB_OK : fail(RB_ERR_INVALID, e);
+}
+
+int rb_batch_run(rb_batch *b, rb_run_stats *stats) {
+    if (!b) return fail(RB_ERR_INVALID, "null batch");
+    const auto t0 = std::chrono::steady_clock::now();
+    rbg::rb_stats_out st;
+    const bool ok = b->b.run(st);
+    if (stats) {
+        std::memset(stats, 0, sizeof *stats);
+        stats->events = st.events;
+        stats->kernel_ms = st.graph_ms;
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        stats->h2d_bytes = st.h2d;
+        stats->d2h_bytes = st.d2h;
+        stats->kernel_launches = st.launches;
+        stats->mapping = 6;
+    }
+    if (ok) return RB_OK;
+    return st.timeout ? RB_ERR_TIMEOUT : RB_ERR_CUDA;
+}
+
+int rb_batch_plan(rb_batch *b, int32_t *n_thread_launches, int32_t *n_warp_items) {
+    if (!b) return fail(RB_ERR_INVALID, "null batch");
+    if (!b->b.planned) b->b.plan();
+    if (n_thread_launches) *n_thread_launches = (int32_t)b->b.classes.size();
+    if (n_warp_items) *n_warp_items = (int32_t)b->b.warp_items.size();
+    return RB_OK;
+}
+
+int rb_batch_item_mapping(const rb_batch *b, int32_t item, int32_t *mapping) {
+    if (!b || !mapping || item < 0 || item >= (int32_t)b->b.items.size())
+        return fail(RB_ERR_INVALID, "item index out of range");
+    *mapping = b->b.items[item].mapping;
     return RB_OK;
 }
 

@@ -14,7 +14,7 @@ static thread_local std::string g_last_error;
 void set_error(const std::string &msg) { g_last_error = msg; }
 const std::string &last_error() { return g_last_error; }
 
-static bool cuda_ok(cudaError_t e, const char *what) {
+bool cuda_ok(cudaError_t e, const char *what) {
     if (e == cudaSuccess) return true;
     set_error(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
     return false;

@@ -15,6 +15,8 @@ namespace rbg {
 // Thread-local error channel of the C ABI.
 void set_error(const std::string &msg);
 const std::string &last_error();
+// true for cudaSuccess; otherwise sets the error ("<what>: <CUDA message>").
+bool cuda_ok(cudaError_t e, const char *what);
 
 // Per-device immutable state: ziggurat tables and device properties.
 struct DeviceCtx {

@@ -83,6 +83,20 @@ struct SsaArgs {
     // Warp-per-trajectory kernel: [grid * warps per block][R] doubles of
     // scratch for its exact steps.
     double *warp_scratch;
+
+    // Warp kernel over a batch of networks (batch != null): item k is
+    // batch[k], its trajectories are the tickets batch_start[k] ..
+    // batch_start[k+1] - 1; the launch's own S, R, P, Q are the largest of the
+    // items'.  An item's lm_* fields point to its lane-major tables (reaction
+    // l*C + i at position i*32 + l, C = ceil(R/32)): float-pair rates,
+    // two-slot shapes (null unless every reaction has order <= 2) and factors
+    // ([C][P][32], species | order << 16).
+    const SsaArgs *batch;
+    const int64_t *batch_start;
+    int32_t batch_n;
+    const float2 *lm_rdf;
+    const uint32_t *lm_shape;
+    const int32_t *lm_fac;
 };
 
 // Launch the thread-per-trajectory kernel; returns a cudaError_t value.
@@ -118,6 +132,8 @@ int ssa_warp_warps(const SsaArgs &a, size_t smem_limit);
 size_t ssa_warp_smem(const SsaArgs &a, int warps);
 int ssa_warp_occupancy(const SsaArgs &a, int warps, size_t smem);
 int launch_ssa_warp(const SsaArgs &a, int warps, int grid, size_t smem, void *stream);
+// Two-slot shape word of reaction r for the lane-major tables of a batch item.
+uint32_t warp_shape_word(const int32_t *fac_sp, const int32_t *fac_ord, int P, int S, int r);
 
 // Every-event runs (src/pyo3_gillespie.rs:209-223) and single
 // _advance_one_reaction steps (src/gillespie.rs:269-297): one thread per

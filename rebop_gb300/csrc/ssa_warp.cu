@@ -50,11 +50,13 @@ __host__ __device__ inline WarpLayout warp_layout(const SsaArgs &a) {
     WarpLayout l;
     const size_t RP = 32 * (size_t)warp_chunk(a.R);     // lane-major positions
     size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;  // zxk, zf, zd, xdf
-    b += 8 * RP;                                        // shared float-pair rates (lane-major)
-    b += 4 * (size_t)a.R * a.P + 4 * RP * a.P;          // factors: reaction-major, lane-major
-    b += 4 * RP;                                        // two-slot reaction shapes (lane-major)
-    b += 4 * (size_t)a.R * a.Q + 8 * (size_t)a.R * a.Q; // jumps (exact tables' layout)
-    b += 16;                                            // alignment of the jump deltas
+    if (!a.batch) {  // a batch's networks stay in global memory
+        b += 8 * RP;                                        // shared float-pair rates (lane-major)
+        b += 4 * (size_t)a.R * a.P + 4 * RP * a.P;          // factors: reaction-major, lane-major
+        b += 4 * RP;                                        // two-slot reaction shapes (lane-major)
+        b += 4 * (size_t)a.R * a.Q + 8 * (size_t)a.R * a.Q; // jumps (exact tables' layout)
+        b += 16;                                            // alignment of the jump deltas
+    }
     l.block_bytes = (b + 15) & ~(size_t)15;
     size_t w = 16 * (size_t)a.S;                        // counts, interval-start counts
     w += 4 * ((size_t)a.S + 1);                         // counts as floats, plus the constant 1
@@ -80,14 +82,12 @@ __device__ __forceinline__ double shfl_d(double v, int src) {
 // Rate::rate's fold (gillespie.rs:71-90), or the macro's integer falling
 // factorials (gillespie_macro.rs:133-146).
 template <bool MACRO>
-__device__ __forceinline__ double exact_propensity(const SsaArgs &a, const int32_t *fac, const int64_t *cnt,
-                                                   double rate, int r) {
+__device__ __forceinline__ double exact_propensity(const SsaArgs &it, const int64_t *cnt, double rate, int r) {
     double acc = rate;
-    for (int p = 0; p < a.P; ++p) {
-        const int f = fac[r * a.P + p];
-        const int o = f >> 16;
+    for (int p = 0; p < it.P; ++p) {
+        const int o = it.fac_ord[r * it.P + p];
         if (o == 0) continue;
-        const int64_t n = cnt[f & 0xFFFF];
+        const int64_t n = cnt[it.fac_sp[r * it.P + p]];
         if (MACRO) {
             int64_t ff = n;
             for (int j = 1; j < o; ++j) ff *= n - j;
@@ -103,10 +103,11 @@ __device__ __forceinline__ double exact_propensity(const SsaArgs &a, const int32
 // generator).  Returns 1 when a reaction fires (its index in idx, the clock in
 // t), 0 when the step records the sample.  scr is this warp's [R] scratch.
 template <bool MACRO>
-__device__ __noinline__ int warp_exact_step(const SsaArgs &a, const int32_t *fac, int64_t *cnt, const double *rates,
-                                            double *scr, Xoshiro &g, double &t, double T, int &idx) {
-    const int lane = threadIdx.x & 31, R = a.R;
-    for (int r = lane; r < R; r += 32) scr[r] = exact_propensity<MACRO>(a, fac, cnt, rates[r], r);
+__device__ __noinline__ int warp_exact_step(const SsaArgs &it, const int64_t *cnt, const double *rates,
+                                            const double *zig, double *scr, Xoshiro &g, double &t, double T,
+                                            int &idx) {
+    const int lane = threadIdx.x & 31, R = it.R;
+    for (int r = lane; r < R; r += 32) scr[r] = exact_propensity<MACRO>(it, cnt, rates[r], r);
     __syncwarp();
     int fire = 0;
     double chosen = 0.0;
@@ -118,7 +119,7 @@ __device__ __noinline__ int warp_exact_step(const SsaArgs &a, const int32_t *fac
             scr[r] = total;
         }
         if (0.0 < total) {
-            const double tn = __dadd_rn(t, __ddiv_rn(xo_exp1(g, a.zig, a.zig + kZigOffF), total));
+            const double tn = __dadd_rn(t, __ddiv_rn(xo_exp1(g, zig, zig + kZigOffF), total));
             if (!(tn > T)) {
                 fire = 1;
                 t = tn;
@@ -149,117 +150,152 @@ __device__ __noinline__ int warp_exact_step(const SsaArgs &a, const int32_t *fac
     return 1;
 }
 
-// SHAPE2: every reaction has reactant order <= 2, so its propensity is
-// rate * max(n1 - o1, 0) * max(n2 - o2, 0) over two (species, offset) slots
-// -- species S is a constant 1 -- and the propensity pass has no branches.
-template <bool MACRO, bool SHAPE2>
+// Two-slot shape of reaction r (reactant order <= 2): slots (species, offset)
+// 2A -> (A,0)(A,1); A+B -> (A,0)(B,0); A -> (A,0)(one); none -> (one)(one),
+// species S standing for a constant 1.  The propensity is then
+// rate * max(n1 - o1, 0) * max(n2 - o2, 0), without branches.
+__host__ __device__ inline uint32_t shape_word(const int32_t *fac_sp, const int32_t *fac_ord, int P, int S, int r) {
+    uint32_t sl[2] = {(uint32_t)S, (uint32_t)S}, of[2] = {0, 0};
+    int k = 0;
+    for (int p = 0; p < P; ++p) {
+        const int o = fac_ord[r * P + p];
+        for (int j = 0; j < o && k < 2; ++j, ++k) {
+            sl[k] = (uint32_t)fac_sp[r * P + p];
+            of[k] = (uint32_t)j;
+        }
+    }
+    return sl[0] | of[0] << 15 | sl[1] << 16 | of[1] << 31;
+}
+
+// BATCH: the launch runs a.batch's networks (each item's tables in global
+// memory, lane-major); otherwise the one network of `a`, whose tables the
+// block copies to shared memory.
+template <bool MACRO, bool BATCH>
 __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __grid_constant__ SsaArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    const int S = a.S, R = a.R, P = a.P, Q = a.Q;
-    const WarpLayout L = warp_layout(a);
+    const WarpLayout L = warp_layout(a);  // sized for the largest network of the launch
 
-    // ---- block tables
+    // ---- block tables: Exp1 tables; in single-network mode also the
+    // network's lane-major rates, factors, shapes and its jumps
     ulonglong2 *zxk = reinterpret_cast<ulonglong2 *>(g_spec_smem);
     uint64_t *zf = reinterpret_cast<uint64_t *>(zxk + 256);
     uint64_t *zd = zf + 257;
     float2 *xdf = reinterpret_cast<float2 *>(zd + 256);
-    const int C = warp_chunk(R), RP = 32 * C;
     float2 *rdf_sh = xdf + 256;
-    int32_t *facl = reinterpret_cast<int32_t *>(rdf_sh + RP);  // [C][P][32] lane-major factors
-    uint32_t *shape = reinterpret_cast<uint32_t *>(facl + (size_t)RP * P);  // [RP] lane-major
-    int32_t *fac = reinterpret_cast<int32_t *>(shape + RP);
-    int32_t *jsp = fac + (size_t)R * P;
-    int64_t *jd = reinterpret_cast<int64_t *>(
-        (reinterpret_cast<uintptr_t>(jsp + (size_t)R * Q) + 7) & ~(uintptr_t)7);
-    load_exact_tables(a, zxk, zf, zd, fac, jsp, jd);
+    const int C0 = warp_chunk(a.R), RP0 = 32 * C0;
+    int32_t *facl_sh = reinterpret_cast<int32_t *>(rdf_sh + RP0);
+    uint32_t *shape_sh = reinterpret_cast<uint32_t *>(facl_sh + (size_t)RP0 * a.P);
+    int32_t *fac_sh = reinterpret_cast<int32_t *>(shape_sh + RP0);
+    int32_t *jsp_sh = fac_sh + (size_t)a.R * a.P;
+    int64_t *jd_sh = reinterpret_cast<int64_t *>(
+        (reinterpret_cast<uintptr_t>(jsp_sh + (size_t)a.R * a.Q) + 7) & ~(uintptr_t)7);
+    if (BATCH) {
+        for (int k = tid; k < 256; k += blockDim.x) {
+            zxk[k] = make_ulonglong2((uint64_t)__double_as_longlong(a.zig[k]),
+                                     (uint64_t)__double_as_longlong(a.zig[kZigOffK + k]));
+            zd[k] = (uint64_t)__double_as_longlong(a.zig[kZigOffD + k]) & ~(1ull << 63);
+        }
+        for (int k = tid; k < 257; k += blockDim.x) zf[k] = (uint64_t)__double_as_longlong(a.zig[kZigOffF + k]);
+    } else {
+        load_exact_tables(a, zxk, zf, zd, fac_sh, jsp_sh, jd_sh);
+        const bool shape2 = a.max_mults <= 2 && a.S < 32767;
+        for (int q = tid; q < RP0; q += blockDim.x) {
+            const int i = q >> 5, l = q & 31, r = l * C0 + i;
+            if (!a.rate_stride) {
+                const DF d = r < a.R ? df_from_double(a.rate[r]) : DF{0.f, 0.f};
+                rdf_sh[q] = make_float2(d.h, d.l);
+            }
+            for (int p = 0; p < a.P; ++p)
+                facl_sh[(i * a.P + p) * 32 + l] =
+                    r < a.R ? (a.fac_sp[r * a.P + p] | (a.fac_ord[r * a.P + p] << 16)) : 0;
+            if (shape2) shape_sh[q] = r < a.R ? shape_word(a.fac_sp, a.fac_ord, a.P, a.S, r) : (uint32_t)a.S << 16 | a.S;
+        }
+    }
     for (int k = tid; k < 256; k += blockDim.x) {
         const double v = a.zig[kZigOffXdf + k];
         xdf[k] = *reinterpret_cast<const float2 *>(&v);
     }
-    // lane-major copies: reaction r = l*C + i at position i*32 + l (padding
-    // positions hold rate 0 and no factors)
-    for (int q = tid; q < RP; q += blockDim.x) {
-        const int i = q >> 5, l = q & 31, r = l * C + i;
-        if (!a.rate_stride) {
-            const DF d = r < R ? df_from_double(a.rate[r]) : DF{0.f, 0.f};
-            rdf_sh[q] = make_float2(d.h, d.l);
-        }
-        for (int p = 0; p < P; ++p)
-            facl[(i * P + p) * 32 + l] = r < R ? (a.fac_sp[r * P + p] | (a.fac_ord[r * P + p] << 16)) : 0;
-        if (SHAPE2) {
-            // slots (species, offset): 2A -> (A,0)(A,1); A+B -> (A,0)(B,0); A -> (A,0)(1); none -> (1)(1)
-            uint32_t sl[2] = {(uint32_t)S, (uint32_t)S}, of[2] = {0, 0};
-            int k = 0;
-            for (int p = 0; r < R && p < P; ++p) {
-                const int o = a.fac_ord[r * P + p];
-                for (int j = 0; j < o && k < 2; ++j, ++k) {
-                    sl[k] = (uint32_t)a.fac_sp[r * P + p];
-                    of[k] = (uint32_t)j;
-                }
-            }
-            shape[q] = sl[0] | of[0] << 15 | sl[1] << 16 | of[1] << 31;
-        }
-    }
     __syncthreads();
-    const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
+    const ExactTables ex{zxk, zf, zd, fac_sh, jsp_sh, jd_sh};
 
-    // ---- this warp's region
+    // ---- this warp's region (sized for the largest network)
     unsigned char *wbase = g_spec_smem + L.block_bytes + (size_t)warp * L.warp_bytes;
     int64_t *cnt = reinterpret_cast<int64_t *>(wbase);
-    int64_t *cnt0 = cnt + S;
-    float *cntf = reinterpret_cast<float *>(cnt0 + S);                                  // [S + 1]
-    float2 *prop = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(cntf + S + 1) + 7) & ~(uintptr_t)7);
-    float2 *rdf = a.rate_stride ? prop + RP : rdf_sh;      // lane-major
-    double *scr = a.warp_scratch + ((size_t)blockIdx.x * nw + warp) * (size_t)R;
-
-    // lane l owns reactions [l * C, min(R, (l + 1) * C)); local index i sits at i*32 + l
-    const int r_lo = min(R, lane * C), r_hi = min(R, r_lo + C);
-    const int n_own = r_hi - r_lo;
-    const float gam = kGamma;
-    const int mm = SHAPE2 ? 2 : a.max_mults;  // multiplies per propensity
-    const float c_tot = (float)(mm + 1 + C + 5) * gam + (float)(R + mm + 4) * 0x1p-53f;
-    const float c_q = c_tot + 6.0f * gam;
-    const float c_sel = 2.0f * (c_tot + (float)(C + 4) * gam);
+    int64_t *cnt0 = cnt + a.S;
+    float *cntf = reinterpret_cast<float *>(cnt0 + a.S);  // [S + 1]
+    float2 *prop = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(cntf + a.S + 1) + 7) & ~(uintptr_t)7);
+    float2 *rdf_w = prop + RP0;  // per-trajectory float-pair rates (single-network mode)
+    double *scr = a.warp_scratch + ((size_t)blockIdx.x * nw + warp) * (size_t)a.R;
     const int64_t t_start = global_ns();
     unsigned long long warp_events = 0;
     bool abort_run = false;
 
     for (;;) {
-        long long traj = 0;
-        if (lane == 0) traj = (long long)atomicAdd(a.work, 1ull);
-        traj = __shfl_sync(0xffffffffu, traj, 0);
-        if (traj >= a.n_traj) break;
+        long long ticket = 0;
+        if (lane == 0) ticket = (long long)atomicAdd(a.work, 1ull);
+        ticket = __shfl_sync(0xffffffffu, ticket, 0);
+        if (ticket >= a.n_traj) break;
+
+        // ---- the trajectory's network and run
+        long long traj = ticket;
+        const SsaArgs *itp = &a;
+        if (BATCH) {
+            int lo = 0, hi = a.batch_n - 1;  // last item with batch_start <= ticket
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (a.batch_start[mid] <= ticket) lo = mid;
+                else hi = mid - 1;
+            }
+            itp = a.batch + lo;
+            traj = ticket - a.batch_start[lo];
+        }
+        const SsaArgs &it = *itp;
+        const int S = it.S, R = it.R, P = it.P, Q = it.Q;
+        const int C = warp_chunk(R);
+        const float2 *rdf = BATCH ? it.lm_rdf : (it.rate_stride ? rdf_w : rdf_sh);
+        const int32_t *facl = BATCH ? it.lm_fac : facl_sh;
+        const uint32_t *shape = BATCH ? it.lm_shape : shape_sh;
+        const bool use_shape = BATCH ? it.lm_shape != nullptr : (it.max_mults <= 2 && it.S < 32767);
+        const int32_t *jsp = BATCH ? it.jmp_sp : jsp_sh;
+        const int64_t *jd = BATCH ? it.jmp_d : jd_sh;
+        // lane l owns reactions [l * C, min(R, (l + 1) * C)); local index i sits at i*32 + l
+        const int r_lo = min(R, lane * C), r_hi = min(R, r_lo + C);
+        const int n_own = r_hi - r_lo;
+        const int mm = use_shape ? 2 : it.max_mults;  // multiplies per propensity
+        const float c_tot = (float)(mm + 1 + C + 5) * kGamma + (float)(R + mm + 4) * 0x1p-53f;
+        const float c_q = c_tot + 6.0f * kGamma;
+        const float c_sel = 2.0f * (c_tot + (float)(C + 4) * kGamma);
 
         // ---- start (or resume) the trajectory
         Xoshiro g{0, 0, 0, 0};
         double t;
-        if (a.in_species) {
-            for (int s = lane; s < S; s += 32) cnt[s] = a.in_species[traj * S + s];
-            t = a.in_t[traj];
+        if (it.in_species) {
+            for (int s = lane; s < S; s += 32) cnt[s] = it.in_species[traj * S + s];
+            t = it.in_t[traj];
             if (lane == 0)
-                g = Xoshiro{a.in_rng[traj * 4], a.in_rng[traj * 4 + 1], a.in_rng[traj * 4 + 2],
-                            a.in_rng[traj * 4 + 3]};
+                g = Xoshiro{it.in_rng[traj * 4], it.in_rng[traj * 4 + 1], it.in_rng[traj * 4 + 2],
+                            it.in_rng[traj * 4 + 3]};
         } else {
-            for (int s = lane; s < S; s += 32) cnt[s] = a.x0[traj * a.x0_stride + s];
+            for (int s = lane; s < S; s += 32) cnt[s] = it.x0[traj * it.x0_stride + s];
             t = 0.0;
-            if (lane == 0) xo_seed(g, a.seeds[traj]);
+            if (lane == 0) xo_seed(g, it.seeds[traj]);
         }
-        const double *rates = a.rate + traj * a.rate_stride;
+        const double *rates = it.rate + traj * it.rate_stride;
         bool exact_traj = !spec_rate_ok((uint64_t)__double_as_longlong(t)) || !(t < 0x1p60);
         for (int r = lane; r < R; r += 32) exact_traj |= !spec_rate_ok((uint64_t)__double_as_longlong(rates[r]));
-        if (a.rate_stride)
-            for (int q = lane; q < RP; q += 32) {
+        if (!BATCH && it.rate_stride)
+            for (int q = lane; q < 32 * C; q += 32) {
                 const int r = (q & 31) * C + (q >> 5);
                 const DF d = r < R ? df_from_double(rates[r]) : DF{0.f, 0.f};
-                rdf[q] = make_float2(d.h, d.l);
+                rdf_w[q] = make_float2(d.h, d.l);
             }
         exact_traj = __any_sync(0xffffffffu, exact_traj);
         for (int s = lane; s <= S; s += 32) cntf[s] = s < S ? (float)cnt[s] : 1.0f;
         __syncwarp();
         unsigned long long ev = 0;
 
-        for (long long i = 0; i < a.n_samples && !abort_run; ++i) {
-            const double T = a.sample_t[i];
+        for (long long i = 0; i < it.n_samples && !abort_run; ++i) {
+            const double T = it.sample_t[i];
             // ---- interval start: save what an exact re-run needs
             for (int s = lane; s < S; s += 32) cnt0[s] = cnt[s];
             const Xoshiro g0 = g;
@@ -282,35 +318,36 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                 // ---- float-pair propensities of this lane's chunk and their sum
                 DF ls{0.f, 0.f};
                 bool amb = false;
-                if (SHAPE2) {
-                    for (int i = 0; i < n_own; ++i) {
-                        const float2 k = rdf[i * 32 + lane];
-                        const uint32_t w = shape[i * 32 + lane];
+                if (use_shape) {
+                    for (int i2 = 0; i2 < n_own; ++i2) {
+                        const float2 k = rdf[i2 * 32 + lane];
+                        const uint32_t w = shape[i2 * 32 + lane];
                         const float n1 = cntf[w & 0x7FFFu], n2 = cntf[(w >> 16) & 0x7FFFu];
                         amb |= !(n1 >= 0.0f && n1 < 8388608.0f && n2 >= 0.0f && n2 < 8388608.0f);
                         const float f1 = fmaxf(__fsub_rn(n1, (float)((w >> 15) & 1u)), 0.0f);
                         const float f2 = fmaxf(__fsub_rn(n2, (float)(w >> 31)), 0.0f);
                         const DF acc = df_mul_fu(df_mul_fu(DF{k.x, k.y}, f1), f2);
-                        prop[i * 32 + lane] = make_float2(acc.h, acc.l);
+                        prop[i2 * 32 + lane] = make_float2(acc.h, acc.l);
                         ls = df_add(ls, acc);
                     }
-                } else
-                for (int i = 0; i < n_own; ++i) {
-                    const float2 k = rdf[i * 32 + lane];
-                    DF acc{k.x, k.y};
-                    for (int p = 0; p < P; ++p) {
-                        const int f = facl[(i * P + p) * 32 + lane];
-                        const int o = f >> 16;
-                        if (o == 0) continue;
-                        const int64_t n = cnt[f & 0xFFFF];
-                        amb |= (uint64_t)n >= (1ull << 23);
-                        for (int j = 0; j < o; ++j) {
-                            const int64_t x = n - j > 0 ? n - j : 0;
-                            acc = df_mul_fu(acc, f23((uint32_t)x & 0x7FFFFFu));
+                } else {
+                    for (int i2 = 0; i2 < n_own; ++i2) {
+                        const float2 k = rdf[i2 * 32 + lane];
+                        DF acc{k.x, k.y};
+                        for (int p = 0; p < P; ++p) {
+                            const int f = facl[(i2 * P + p) * 32 + lane];
+                            const int o = f >> 16;
+                            if (o == 0) continue;
+                            const int64_t n = cnt[f & 0xFFFF];
+                            amb |= (uint64_t)n >= (1ull << 23);
+                            for (int j = 0; j < o; ++j) {
+                                const int64_t x = n - j > 0 ? n - j : 0;
+                                acc = df_mul_fu(acc, f23((uint32_t)x & 0x7FFFFFu));
+                            }
                         }
+                        prop[i2 * 32 + lane] = make_float2(acc.h, acc.l);
+                        ls = df_add(ls, acc);
                     }
-                    prop[i * 32 + lane] = make_float2(acc.h, acc.l);
-                    ls = df_add(ls, acc);
                 }
                 // inclusive scan of the chunk sums
                 DF incl = ls;
@@ -385,9 +422,9 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                             v = DF{pa.x, pa.y};
                         }
 #pragma unroll
-                        for (int dd2 = 1; dd2 < 32; dd2 <<= 1) {
-                            const DF o = shfl_up_df(v, dd2);
-                            if (lane >= dd2) v = df_add(o, v);
+                        for (int d2 = 1; d2 < 32; d2 <<= 1) {
+                            const DF o = shfl_up_df(v, d2);
+                            if (lane >= d2) v = df_add(o, v);
                         }
                         const DF cum = df_add(carry, v);
                         const float dr = __fadd_rn(__fsub_rn(cum.h, ch.h), __fsub_rn(cum.l, ch.l));
@@ -432,7 +469,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                         }
                     }
                     int idx = 0;
-                    if (!warp_exact_step<MACRO>(a, fac, cnt, rates, scr, g, t, T, idx)) break;
+                    if (!warp_exact_step<MACRO>(it, cnt, rates, a.zig, scr, g, t, T, idx)) break;
                     ++ev;
                     if (idx < R)
                         for (int q = lane; q < Q; q += 32) {
@@ -447,25 +484,25 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
             }
             // ---- record sample i at t = T
             t = T;
-            int64_t *o = a.out + (size_t)i * a.n_save * a.n_traj + traj;
-            for (int k = lane; k < a.n_save; k += 32) o[(size_t)k * a.n_traj] = cnt[a.save_idx[k]];
+            int64_t *o = it.out + (size_t)i * it.n_save * it.n_traj + traj;
+            for (int k = lane; k < it.n_save; k += 32) o[(size_t)k * it.n_traj] = cnt[it.save_idx[k]];
             __syncwarp();
         }
         if (abort_run) {
             if (lane == 0) atomicExch(a.work + 2, 1ull);
             break;
         }
-        if (a.fin_species)
-            for (int s = lane; s < S; s += 32) a.fin_species[traj * S + s] = cnt[s];
+        if (it.fin_species)
+            for (int s = lane; s < S; s += 32) it.fin_species[traj * S + s] = cnt[s];
         if (lane == 0) {
-            if (a.fin_t) a.fin_t[traj] = t;
-            if (a.fin_rng) {
-                a.fin_rng[traj * 4 + 0] = g.s0;
-                a.fin_rng[traj * 4 + 1] = g.s1;
-                a.fin_rng[traj * 4 + 2] = g.s2;
-                a.fin_rng[traj * 4 + 3] = g.s3;
+            if (it.fin_t) it.fin_t[traj] = t;
+            if (it.fin_rng) {
+                it.fin_rng[traj * 4 + 0] = g.s0;
+                it.fin_rng[traj * 4 + 1] = g.s1;
+                it.fin_rng[traj * 4 + 2] = g.s2;
+                it.fin_rng[traj * 4 + 3] = g.s3;
             }
-            if (a.events) a.events[traj] = ev;
+            if (it.events) it.events[traj] = ev;
         }
         warp_events += ev;
         __syncwarp();
@@ -473,9 +510,9 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
     if (lane == 0 && warp_events) atomicAdd(a.work + 1, warp_events);
 }
 
-template <bool MACRO, bool SHAPE2>
+template <bool MACRO, bool BATCH>
 int warp_launch(const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st) {
-    auto kern = ssa_warp_kernel<MACRO, SHAPE2>;
+    auto kern = ssa_warp_kernel<MACRO, BATCH>;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return (int)err;
     kern<<<grid, block, smem, st>>>(a);
@@ -502,20 +539,23 @@ bool ssa_warp_supported(const SsaArgs &a, int max_order) {
 int ssa_warp_occupancy(const SsaArgs &a, int warps, size_t smem) {
     int n = 0;
     // all instances share the block shape and shared memory use
-    cudaFuncSetAttribute(ssa_warp_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_warp_kernel<false, true>, 32 * warps, smem);
+    cudaFuncSetAttribute(ssa_warp_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_warp_kernel<false, false>, 32 * warps, smem);
     return n;
 }
 
 int launch_ssa_warp(const SsaArgs &a, int warps, int grid, size_t smem, void *stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // two-slot shapes need reactant order <= 2 and species indices below 2^15
-    const bool shape2 = a.max_mults <= 2 && a.S < 32767;
+    const bool batch = a.batch != nullptr;
     if (a.macro_mode)
-        return shape2 ? warp_launch<true, true>(a, 32 * warps, grid, smem, st)
-                      : warp_launch<true, false>(a, 32 * warps, grid, smem, st);
-    return shape2 ? warp_launch<false, true>(a, 32 * warps, grid, smem, st)
-                  : warp_launch<false, false>(a, 32 * warps, grid, smem, st);
+        return batch ? warp_launch<true, true>(a, 32 * warps, grid, smem, st)
+                     : warp_launch<true, false>(a, 32 * warps, grid, smem, st);
+    return batch ? warp_launch<false, true>(a, 32 * warps, grid, smem, st)
+                 : warp_launch<false, false>(a, 32 * warps, grid, smem, st);
+}
+
+uint32_t warp_shape_word(const int32_t *fac_sp, const int32_t *fac_ord, int P, int S, int r) {
+    return shape_word(fac_sp, fac_ord, P, S, r);
 }
 
 }  // namespace rbg

@@ -227,3 +227,29 @@ def test_generated_network_compiles(rb, tmp_path, monkeypatch):
     assert rc == 0, importlib.import_module("rebop_gb300._lib").last_error()
     assert n.value > 10000
     assert len(list(tmp_path.glob("net_*.cubin"))) == 1
+
+
+def test_batch_plan_groups_by_structure(rb):
+    # Parameter sets of one network merge into one thread-per-trajectory
+    # launch; large networks and rate expressions go elsewhere.
+    import bench
+
+    b = rb.Batch()
+    mm = rb.Network(4)  # E + S <-> ES -> E + P
+    mm.add_reaction(rb.Rate.lma(0.01, [1, 1, 0, 0]), [-1, -1, 1, 0])
+    mm.add_reaction(rb.Rate.lma(0.1, [0, 0, 1, 0]), [1, 1, -1, 0])
+    mm.add_reaction(rb.Rate.lma(0.05, [0, 0, 1, 0]), [1, 0, -1, 1])
+    seeds = np.arange(8, dtype=np.uint64)
+    for k in range(3):
+        assert b.add(mm, [50, 500, 0, 0], seeds, 10.0, 5, rates=[0.01 * (k + 1), 0.1, 0.05]) == k
+    b.add(mm, [50, 500, 0, 0], seeds, 20.0, 5)  # another horizon: another launch
+    reactions, x0 = bench.random_network(3, 20, 60)
+    big = rb.Network(20)
+    for k, e, d in reactions:
+        big.add_reaction(rb.Rate.lma(k, e), d)
+    b.add(big, x0, seeds, 0.01, 4)
+    b.add(big, x0, seeds, 0.02, 4)
+    assert b.plan() == (2, 2)
+    assert [b.mapping(k) for k in range(6)] == [4, 4, 4, 4, 5, 5]
+    with pytest.raises(ValueError):
+        b.add(mm, [1, 2, 3], seeds, 1.0, 2)
