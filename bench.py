@@ -86,6 +86,30 @@ LARGE = dict(
 )
 WORKLOADS = {"dimer": DIMER, "sir": SIR, "large": LARGE}
 
+BATCH = dict(
+    name="batch",
+    desc=("heterogeneous batch in one CUDA graph: 4096 Michaelis-Menten sets (E+S<->ES->E+P, rates log-uniform "
+          "in [1e-3, 1e1], E0 ~ U[10, 100], S0 ~ U[100, 1000], tmax 1) and 1024 random mass-action networks "
+          "(8-64 species, 16-256 reactions, order <= 2, stoichiometry in {-2..2}, counts ~ U[0, 500], tmax 1e-3); "
+          "64 trajectories each, nb_steps 100 (seed 20260105)"),
+    n_mm=4096, n_rand=1024, traj=64, nb_steps=100, tmax_mm=1.0, tmax_rand=1e-3, cpu_every=64,
+)
+MM_REACTIONS = [([1, 1, 0, 0], [-1, -1, 1, 0]), ([0, 0, 1, 0], [1, 1, -1, 0]), ([0, 0, 1, 0], [1, 0, -1, 1])]
+
+
+def batch_items(seed: int = 20260105):
+    """Items of the heterogeneous batch: ("mm", rates, x0) and ("rand", reactions, x0)."""
+    rng = np.random.default_rng(seed)
+    items = []
+    for _ in range(BATCH["n_mm"]):
+        rates = np.exp(rng.uniform(np.log(1e-3), np.log(1e1), 3))
+        items.append(("mm", rates, [int(rng.integers(10, 101)), int(rng.integers(100, 1001)), 0, 0]))
+    for k in range(BATCH["n_rand"]):
+        S, R = int(rng.integers(8, 65)), int(rng.integers(16, 257))
+        reactions, _ = random_network(seed * 7919 + k, S, R)
+        items.append(("rand", reactions, rng.integers(0, 501, size=S).tolist()))
+    return items
+
 
 def f_event(w) -> int:
     """Algorithmic binary64 operations per event of the direct method with full
@@ -379,17 +403,119 @@ def run_ours(args, w):
         dist.destroy_process_group()
 
 
+def _batch_cpu(items, every: int, traj: int, threads: int):
+    """Oracle on every `every`-th item of each kind: events/s on `threads` threads."""
+    from oracle import oracle as O
+
+    ev_tot, t_tot = 0, 0.0
+    for j, (kind, spec, x0) in enumerate(items):
+        if j % every:
+            continue
+        if kind == "mm":
+            net = O.OracleNet(4)
+            for (e, d), k in zip(MM_REACTIONS, spec):
+                net.add_lma(k, e, d)
+            tmax = BATCH["tmax_mm"]
+        else:
+            net = O.OracleNet(len(x0))
+            for k, e, d in spec:
+                net.add_lma_sparse(k, [(i, x) for i, x in enumerate(e) if x], d)
+            tmax = BATCH["tmax_rand"]
+        seeds = seeds_for(0, 7000 + j, traj)
+        t0 = time.perf_counter()
+        _, _, ev, _ = net.run_ensemble(x0, seeds, tmax, BATCH["nb_steps"], n_threads=threads)
+        t_tot += time.perf_counter() - t0
+        ev_tot += ev
+    return ev_tot / t_tot, ev_tot, t_tot
+
+
+def run_batch(args):
+    import torch
+
+    import rebop_gb300 as rb
+
+    items = batch_items()
+    traj = BATCH["traj"]
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        threads = os.cpu_count() or 1
+        v, ev, t = _batch_cpu(items, BATCH["cpu_every"], traj, threads)
+        print(json.dumps({"impl": "reference", "metric": "SSA reaction events/sec", "value": v, "unit": "events/s",
+                          "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * t,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+int64",
+                          "data": "synthetic", "config": {"workload": BATCH["desc"]},
+                          "cpu_baseline": {"value": v, "unit": "events/s", "cores": threads, "kind": "port",
+                                           "sample": f"every {BATCH['cpu_every']}th item of each kind, oracle port"},
+                          "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    b = rb.Batch()
+    mm = rb.Network(4)
+    for e, d in MM_REACTIONS:
+        mm.add_reaction(rb.Rate.lma(1.0, e), d)
+    nets = []
+    for j, (kind, spec, x0) in enumerate(items):
+        seeds = seeds_for(0, 100000 + j, traj)
+        if kind == "mm":
+            b.add(mm, x0, seeds, BATCH["tmax_mm"], BATCH["nb_steps"], rates=spec, want_events=False)
+        else:
+            net = rb.Network(len(x0))
+            for k, e, d in spec:
+                net.add_reaction(rb.Rate.lma(k, e), d)
+            nets.append(net)
+            b.add(net, x0, seeds, BATCH["tmax_rand"], BATCH["nb_steps"], want_events=False)
+    n_thread, n_warp = b.plan()
+    for s in range(args.warmup):
+        b.run()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    dev_ms, wall, events, h2d, d2h = 0.0, 0.0, 0, 0, 0
+    for s in range(args.steps):
+        for j in range(len(items)):
+            b.seeds(j)[:] = seeds_for(1 + s, 100000 + j, traj)
+        t0 = time.perf_counter()
+        st = b.run()
+        wall += time.perf_counter() - t0
+        dev_ms += st["kernel_ms"]
+        events += st["events"]
+        h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+    clk = clocks.stop()
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, _, _ = _batch_cpu(items, BATCH["cpu_every"] * 4, traj, threads)
+        cpu = {"value": v, "unit": "events/s", "cores": threads, "kind": "port",
+               "sample": f"every {BATCH['cpu_every'] * 4}th item of each kind, oracle port, {threads} threads"}
+    print(json.dumps({
+        "metric": "SSA reaction events/sec", "value": events / (dev_ms / 1e3), "unit": "events/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+int64", "data": "synthetic",
+        "config": {"workload": BATCH["desc"], "items": len(items), "trajectories": len(items) * traj,
+                   "events_per_step": events / args.steps, "thread_launches": n_thread, "warp_batch_items": n_warp,
+                   "timing": "device time of the replayed graph: input copy, kernels, result copy",
+                   "l2": "inputs and outputs far above L2 are copied in every step"},
+        "e2e": {"value": events / wall, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps * (n_thread + (1 if n_warp else 0)),
+        "cpu_baseline": cpu, "clocks": clk}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="dimer")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch"], default="dimer")
     ap.add_argument("--n-traj", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.workload == "batch":
+        run_batch(args)
+        return
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference_arm(args, w)

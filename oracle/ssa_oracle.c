@@ -412,6 +412,7 @@ typedef struct {
     int64_t *final_species;    /* [n_traj][S] or NULL           */
     uint64_t *events;          /* [n_traj] or NULL              */
     int64_t next;              /* shared work counter           */
+    int64_t chunk;             /* trajectories per work item    */
     int64_t total_events;
     pthread_mutex_t lock;
 } ens_job;
@@ -424,9 +425,9 @@ static void *ens_worker(void *arg) {
     int64_t *sp = (int64_t *)malloc(sizeof(int64_t) * (S ? S : 1));
     int64_t local_events = 0;
     for (;;) {
-        int64_t begin = __atomic_fetch_add(&job->next, 64, __ATOMIC_RELAXED);
+        int64_t begin = __atomic_fetch_add(&job->next, job->chunk, __ATOMIC_RELAXED);
         if (begin >= job->n_traj) break;
-        int64_t end = begin + 64 < job->n_traj ? begin + 64 : job->n_traj;
+        int64_t end = begin + job->chunk < job->n_traj ? begin + job->chunk : job->n_traj;
         for (int64_t j = begin; j < end; j++) {
             orc_state st;
             st.species = sp;
@@ -480,6 +481,10 @@ int64_t orc_run_ensemble(const orc_net *net, const double *rates, int64_t rates_
     job.total_events = 0;
     pthread_mutex_init(&job.lock, NULL);
     if (n_threads < 1) n_threads = 1;
+    /* up to 64 trajectories per work item, but at least four items per thread */
+    job.chunk = n_traj / (4 * (int64_t)n_threads);
+    if (job.chunk > 64) job.chunk = 64;
+    if (job.chunk < 1) job.chunk = 1;
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * n_threads);
     for (int i = 0; i < n_threads; i++) pthread_create(&th[i], NULL, ens_worker, &job);
     for (int i = 0; i < n_threads; i++) pthread_join(th[i], NULL);

@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 
@@ -147,6 +148,25 @@ bool Batch::plan() {
         c.n_traj += it.in.n_traj;
         it.mapping = 4;
     }
+    // a thread launch for a handful of trajectories wastes the GPU: small
+    // classes join the warp batch (RB_BATCH_MIN_THREAD trajectories, default
+    // 2048, make a class worth its own launch)
+    int64_t min_thread = 2048;
+    if (const char *e = std::getenv("RB_BATCH_MIN_THREAD")) min_thread = std::max<int64_t>(1, std::atoll(e));
+    std::vector<Class> kept;
+    for (Class &c : classes) {
+        bool movable = c.kind == Class::Merged && c.n_traj < min_thread;
+        for (int i : c.items) movable = movable && !items[i].in.rates_per_traj;
+        if (!movable) {
+            kept.push_back(c);
+            continue;
+        }
+        for (int i : c.items) {
+            items[i].mapping = 5;
+            warp_items.push_back(i);
+        }
+    }
+    classes.swap(kept);
     // the warp batch: most work first
     std::vector<std::pair<double, int>> order;
     for (int i : warp_items) {

@@ -67,21 +67,40 @@ def test_batch_matches_individual_runs(rb):
     specs.append((b.add(mm, [30, 300, 0, 0], seeds, 5.0, 10, rates=per), mm, [30, 300, 0, 0], seeds, 5.0, 10,
                   per, None))
     n_thread, n_warp = b.plan()
-    # the 8-species network and both Michaelis-Menten forms run on thread
-    # kernels, the expression alone; three random networks share the warp batch
-    assert n_warp == 3 and n_thread == 3
+    # the Michaelis-Menten sets merge with the per-trajectory-rate item (which
+    # only a thread launch runs) into one class; the rate expression runs
+    # alone; the small 8-species class and the other networks join the warp batch
+    assert n_warp == 4 and n_thread == 2
     st = b.run()
     assert st["mapping"] == 6 and st["events"] > 0
     for k, net, x0, seeds, tmax, nb, rates, save in specs:
         _check(b, k, net, x0, seeds, tmax, nb, rates, save)
-    # thread classes: generated kernels from 4096 trajectories up, below that
-    # the descriptor kernels
-    assert {b.mapping(k) for k in range(41)} <= {2, 3, 4}
-    assert {b.mapping(k) for k in range(41, 44)} == {5}
-    assert b.mapping(44) == 0 and b.mapping(45) in (2, 3, 4)
+    assert {b.mapping(k) for k in list(range(40)) + [45]} <= {2, 3, 4}
+    assert {b.mapping(k) for k in range(40, 44)} == {5}
+    assert b.mapping(44) == 0
     # replay the captured graph with new seeds
     for k, net, x0, seeds, tmax, nb, rates, save in specs:
         b.seeds(k)[:] = rng.integers(np.iinfo(np.uint64).max, size=b.seeds(k).size, dtype=np.uint64)
     st2 = b.run()
     for k, net, x0, seeds, tmax, nb, rates, save in specs:
         _check(b, k, net, x0, b.seeds(k), tmax, nb, rates, save)
+
+
+def test_batch_merges_parameter_sets(rb, monkeypatch):
+    # With every class worth a launch, parameter sets of one network run as one
+    # thread-per-trajectory ensemble with per-trajectory rates and counts.
+    monkeypatch.setenv("RB_BATCH_MIN_THREAD", "1")
+    rng = np.random.default_rng(6)
+    b = rb.Batch()
+    mm = _mm(rb)
+    specs = []
+    for k in range(30):
+        rates = 10 ** rng.uniform(-3, 1, 3)
+        x0 = [int(rng.integers(10, 101)), int(rng.integers(100, 1001)), 0, 0]
+        seeds = rng.integers(np.iinfo(np.uint64).max, size=int(rng.integers(1, 20)), dtype=np.uint64)
+        specs.append((b.add(mm, x0, seeds, 3.0, 12, rates=rates, save=[1, 3]), x0, seeds, rates))
+    assert b.plan() == (1, 0)
+    b.run()
+    for k, x0, seeds, rates in specs:
+        _check(b, k, mm, x0, seeds, 3.0, 12, rates, [1, 3])
+        assert b.mapping(k) in (2, 3, 4)

@@ -249,7 +249,22 @@ def test_batch_plan_groups_by_structure(rb):
         big.add_reaction(rb.Rate.lma(k, e), d)
     b.add(big, x0, seeds, 0.01, 4)
     b.add(big, x0, seeds, 0.02, 4)
-    assert b.plan() == (2, 2)
-    assert [b.mapping(k) for k in range(6)] == [4, 4, 4, 4, 5, 5]
+    # parameter sets merge by structure and horizon; classes below
+    # RB_BATCH_MIN_THREAD trajectories join the warp batch
+    assert b.plan() == (0, 6)
+    assert [b.mapping(k) for k in range(6)] == [5] * 6
+    import os
+
+    os.environ["RB_BATCH_MIN_THREAD"] = "1"
+    try:
+        b2 = rb.Batch()
+        for k in range(3):
+            b2.add(mm, [50, 500, 0, 0], seeds, 10.0, 5, rates=[0.01 * (k + 1), 0.1, 0.05])
+        b2.add(mm, [50, 500, 0, 0], seeds, 20.0, 5)
+        b2.add(big, x0, seeds, 0.01, 4)
+        assert b2.plan() == (2, 1)
+        assert [b2.mapping(k) for k in range(5)] == [4, 4, 4, 4, 5]
+    finally:
+        del os.environ["RB_BATCH_MIN_THREAD"]
     with pytest.raises(ValueError):
         b.add(mm, [1, 2, 3], seeds, 1.0, 2)
