@@ -221,6 +221,27 @@ def run_reference_arm(args, w):
     print(json.dumps(line), flush=True)
 
 
+def reduce_over_ranks(dist, seconds: float, events: float, device: str):
+    """Whole-job timing: the slowest rank's seconds and the sum of all ranks'
+    events (no data-path collective; trajectories never cross ranks)."""
+    if dist is None:
+        return seconds, events
+    import torch
+
+    t = torch.tensor([seconds, events], dtype=torch.float64, device=device)
+    m = t.clone()
+    dist.all_reduce(m[:1], op=dist.ReduceOp.MAX)
+    dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+    return float(m[0]), float(t[1])
+
+
+def shard_seeds(rank: int, step: int, n: int) -> np.ndarray:
+    """Rank `rank`'s trajectories of a step: its own seeds (weak scaling).  A
+    trajectory's stream depends on its seed alone, so any sharding of a seed
+    list reproduces the unsharded ensemble."""
+    return seeds_for(rank, step, n)
+
+
 # ---------------------------------------------------------------- GPU side
 # Kernel that runs each mapping (rb_run_stats.mapping) and what it is.
 MAPPINGS = {
@@ -278,7 +299,8 @@ def run_ours(args, w):
     stream = torch.cuda.current_stream()
     sid = stream.cuda_stream
     d_x0 = torch.tensor(w["x0"], dtype=torch.int64, device="cuda")
-    d_seeds = [torch.from_numpy(seeds_for(rank, s, n).view(np.int64)).cuda() for s in range(args.warmup + args.steps)]
+    d_seeds = [torch.from_numpy(shard_seeds(rank, s, n).view(np.int64)).cuda()
+               for s in range(args.warmup + args.steps)]
     d_out = torch.empty((NT, S, n), dtype=torch.int64, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
@@ -313,14 +335,7 @@ def run_ours(args, w):
     step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
     dev_s = sum(step_ms) / 1e3
     ev_total = sum(events_per_step)
-    if dist is not None:
-        t = torch.tensor([dev_s, float(ev_total)], dtype=torch.float64, device="cuda")
-        tmax_t = t.clone()
-        dist.all_reduce(tmax_t[:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-        dev_s_all, ev_all = float(tmax_t[0]), float(t[1])
-    else:
-        dev_s_all, ev_all = dev_s, float(ev_total)
+    dev_s_all, ev_all = reduce_over_ranks(dist, dev_s, float(ev_total), "cuda")
     value = ev_all / dev_s_all
 
     # e2e: the C-ABI host call with page-locked buffers, copies in the timed region.
@@ -338,12 +353,7 @@ def run_ours(args, w):
         e2e_s += time.perf_counter() - t0
         e2e_ev += res.total_events
         h2d, d2h = res.stats["h2d_bytes"], res.stats["d2h_bytes"]
-    if dist is not None:
-        t = torch.tensor([e2e_s, float(e2e_ev)], dtype=torch.float64, device="cuda")
-        m = t.clone()
-        dist.all_reduce(m[:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-        e2e_s, e2e_ev = float(m[0]), float(t[1])
+    e2e_s, e2e_ev = reduce_over_ranks(dist, e2e_s, float(e2e_ev), "cuda")
     e2e_value = e2e_ev / e2e_s
 
     # roofline of the dominant kernel: the binary64 work of the direct method
