@@ -114,6 +114,19 @@ lib.rbg_internal_zig_tables.argtypes = [P(_f64), P(_f64)]
 lib.rbg_internal_zig_tables.restype = None
 lib.rbg_internal_fp64_fma_rate.argtypes = [_vp]
 lib.rbg_internal_fp64_fma_rate.restype = _f64
+_f32 = C.c_float
+for _name, _args in {
+    "rbg_mdn_gemm": [_vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _f32,
+                     _vp],
+    "rbg_mdn_bias_act": [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp],
+    "rbg_mdn_silu_backward": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp],
+    "rbg_mdn_head_backward": [_vp, _vp, _vp, C.c_int, C.c_int, _vp],
+    "rbg_mdn_loss": [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp],
+    "rbg_mdn_adam": [_vp, _vp, _vp, _vp, _vp, C.c_int, _f32, _f32, _f32, _f32, C.c_int, _vp],
+    "rbg_mdn_sample": [_vp, C.c_int, C.c_int, _u64, _vp, _vp],
+}.items():
+    getattr(lib, _name).argtypes = _args
+    getattr(lib, _name).restype = C.c_int
 lib.rbg_internal_jit_source.argtypes = [_vp, _cp, _sz]
 lib.rbg_internal_jit_source.restype = C.c_int
 lib.rbg_internal_jit_compile.argtypes = [_vp, P(_u64)]

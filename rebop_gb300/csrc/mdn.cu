@@ -1,0 +1,297 @@
+// Kernels of the learned surrogate: a BF16 multilayer perceptron with a
+// mixture-density head over (log1p protein, log1p dimer) counts, trained on
+// ensembles the SSA engine generates.
+//
+//   * gemm_bf16: C[M][N] (+)= op(A) op(B) with BF16 operands and FP32
+//     accumulation on the tensor cores (mma m16n8k16); op = transpose or not,
+//     so one kernel serves the forward pass (H W^T), the input gradient
+//     (dZ W) and the weight gradient (dZ^T H).
+//   * bias_silu: Z += b; H = bf16(silu(Z)) (or identity for the head).
+//   * silu_backward: dZ = dH * silu'(Z), plus the bias gradient.
+//   * mdn_loss: negative log-likelihood of a K-component diagonal Gaussian
+//     mixture in two dimensions and its gradient with respect to the head's
+//     raw outputs (logits, means, softplus scales).
+//   * adam: FP32 master weights, BF16 copies refreshed in place.
+//   * mdn_sample: one draw from each row's mixture.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace rbg {
+
+namespace {
+
+constexpr int kTileM = 64, kTileN = 64, kTileK = 32;
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+// C = alpha * op(A) op(B) + beta * C, row-major everything.  op(A) is M x K:
+// A[m][k] at A[m*lda + k], or A[k][m] at A[k*lda + m] when TA.  op(B) is
+// K x N: B[k][n] at B[k*ldb + n], or B[n][k] at B[n*ldb + k] when TB.
+// Block 64 x 64 of C, four warps of 32 x 32, K in steps of 32.
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__restrict__ A, int lda,
+                                                        const __nv_bfloat16 *__restrict__ B, int ldb,
+                                                        float *__restrict__ C, int ldc, int M, int N, int K,
+                                                        float beta) {
+    __shared__ __nv_bfloat16 As[kTileM][kTileK + 8];  // [m][k]
+    __shared__ __nv_bfloat16 Bs[kTileN][kTileK + 8];  // [n][k]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileN;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int g = lane >> 2, tg = lane & 3;
+    float acc[2][4][4] = {};
+    const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+    for (int k0 = 0; k0 < K; k0 += kTileK) {
+        for (int e = tid; e < kTileM * kTileK; e += 128) {
+            const int mm = e / kTileK, kk = e % kTileK;
+            const int m = m0 + mm, k = k0 + kk;
+            As[mm][kk] = (m < M && k < K) ? (TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]) : zero;
+        }
+        for (int e = tid; e < kTileN * kTileK; e += 128) {
+            const int nn = e / kTileK, kk = e % kTileK;
+            const int n = n0 + nn, k = k0 + kk;
+            Bs[nn][kk] = (n < N && k < K) ? (TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n]) : zero;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < kTileK; ks += 16) {
+            uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = wm + i * 16 + g, c = ks + tg * 2;
+                af[i][0] = pack_bf16(As[r][c], As[r][c + 1]);
+                af[i][1] = pack_bf16(As[r + 8][c], As[r + 8][c + 1]);
+                af[i][2] = pack_bf16(As[r][c + 8], As[r][c + 9]);
+                af[i][3] = pack_bf16(As[r + 8][c + 8], As[r + 8][c + 9]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int n = wn + j * 8 + g, c = ks + tg * 2;
+                bfr[j][0] = pack_bf16(Bs[n][c], Bs[n][c + 1]);
+                bfr[j][1] = pack_bf16(Bs[n][c + 8], Bs[n][c + 9]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    asm volatile(
+                        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                        "{%8,%9}, {%0,%1,%2,%3};\n"
+                        : "+f"(acc[i][j][0]), "+f"(acc[i][j][1]), "+f"(acc[i][j][2]), "+f"(acc[i][j][3])
+                        : "r"(af[i][0]), "r"(af[i][1]), "r"(af[i][2]), "r"(af[i][3]), "r"(bfr[j][0]),
+                          "r"(bfr[j][1]));
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int m = m0 + wm + i * 16 + g + h * 8;
+                const int n = n0 + wn + j * 8 + tg * 2;
+                if (m >= M) continue;
+                for (int q = 0; q < 2; ++q) {
+                    if (n + q >= N) continue;
+                    float *c = C + (size_t)m * ldc + n + q;
+                    const float v = acc[i][j][h * 2 + q];
+                    *c = beta == 0.0f ? v : __fmaf_rn(beta, *c, v);
+                }
+            }
+}
+
+__device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + __expf(-x)); }
+
+// Z[m][n] += b[n]; H = bf16(silu(Z)) (act = 1) or bf16(Z) (act = 0).
+__global__ void bias_act_kernel(float *Z, const float *b, __nv_bfloat16 *H, int M, int N, int act) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)M * N) return;
+    const float z = Z[i] + b[i % N];
+    Z[i] = z;
+    if (H) H[i] = __float2bfloat16(act ? z * sigmoidf_(z) : z);
+}
+
+// dZ = dH * silu'(Z) as BF16 for the next GEMMs; db[n] += sum_m dZ[m][n].
+__global__ void silu_backward_kernel(const float *Z, const float *dH, __nv_bfloat16 *dZ, float *db, int M, int N) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    float s = 0.0f;
+    for (int m = 0; m < M; ++m) {
+        const size_t i = (size_t)m * N + n;
+        const float z = Z[i], sg = sigmoidf_(z);
+        const float d = dH[i] * sg * (1.0f + z * (1.0f - sg));
+        dZ[i] = __float2bfloat16(d);
+        s += d;
+    }
+    db[n] = s;
+}
+
+// Bias gradient of the head and its BF16 copy: db[n] = sum_m G[m][n].
+__global__ void head_backward_kernel(const float *G, __nv_bfloat16 *Gb, float *db, int M, int N) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    float s = 0.0f;
+    for (int m = 0; m < M; ++m) {
+        const float v = G[(size_t)m * N + n];
+        Gb[(size_t)m * N + n] = __float2bfloat16(v);
+        s += v;
+    }
+    db[n] = s;
+}
+
+__device__ __forceinline__ float softplusf_(float x) { return x > 20.0f ? x : log1pf(__expf(x)); }
+
+// Head layout per row (K components): logits[K] | mu1[K] | mu2[K] | s1[K] | s2[K],
+// sigma = softplus(s) + 1e-3.  loss[row] = -log sum_k pi_k N(y1; mu1, s1) N(y2; mu2, s2);
+// G = d(mean loss)/d(raw head outputs).
+__global__ void mdn_loss_kernel(const float *O, const float *Y, int B, int K, float *loss, float *G) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= B) return;
+    const float *o = O + (size_t)row * 5 * K;
+    float *gr = G + (size_t)row * 5 * K;
+    const float y1 = Y[2 * row], y2 = Y[2 * row + 1];
+    float lmax = -1e30f, mx = -1e30f;
+    for (int k = 0; k < K; ++k) lmax = fmaxf(lmax, o[k]);
+    float zs = 0.0f;
+    for (int k = 0; k < K; ++k) zs += __expf(o[k] - lmax);
+    const float logz = lmax + logf(zs);
+    float lp[16];
+    for (int k = 0; k < K; ++k) {
+        const float s1 = softplusf_(o[3 * K + k]) + 1e-3f, s2 = softplusf_(o[4 * K + k]) + 1e-3f;
+        const float e1 = (y1 - o[K + k]) / s1, e2 = (y2 - o[2 * K + k]) / s2;
+        lp[k] = (o[k] - logz) - 0.5f * (e1 * e1 + e2 * e2) - logf(s1) - logf(s2) - 1.8378770664f;
+        mx = fmaxf(mx, lp[k]);
+    }
+    float tot = 0.0f;
+    for (int k = 0; k < K; ++k) tot += __expf(lp[k] - mx);
+    const float ll = mx + logf(tot);
+    loss[row] = -ll;
+    const float inv_b = 1.0f / (float)B;
+    for (int k = 0; k < K; ++k) {
+        const float r = __expf(lp[k] - ll);              // responsibility
+        const float pi = __expf(o[k] - logz);
+        const float s1 = softplusf_(o[3 * K + k]) + 1e-3f, s2 = softplusf_(o[4 * K + k]) + 1e-3f;
+        const float e1 = (y1 - o[K + k]) / s1, e2 = (y2 - o[2 * K + k]) / s2;
+        gr[k] = (pi - r) * inv_b;
+        gr[K + k] = -r * e1 / s1 * inv_b;
+        gr[2 * K + k] = -r * e2 / s2 * inv_b;
+        // d/ds of -log N: (1 - e^2)/sigma * dsigma/ds, dsigma/ds = sigmoid(s)
+        gr[3 * K + k] = r * (1.0f - e1 * e1) / s1 * sigmoidf_(o[3 * K + k]) * inv_b;
+        gr[4 * K + k] = r * (1.0f - e2 * e2) / s2 * sigmoidf_(o[4 * K + k]) * inv_b;
+    }
+}
+
+__global__ void adam_kernel(float *w, __nv_bfloat16 *wb, const float *g, float *m, float *v, int n, float lr,
+                            float b1, float b2, float eps, float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16(wi);
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// One draw per row: component by its weight, then two Gaussians (Box-Muller).
+__global__ void mdn_sample_kernel(const float *O, int B, int K, uint64_t seed, float *out) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= B) return;
+    const float *o = O + (size_t)row * 5 * K;
+    const uint64_t h = mix64(seed ^ mix64((uint64_t)row + 0x9E3779B97F4A7C15ull));
+    const float u0 = (float)(h >> 40) * 0x1p-24f, u1 = ((float)((h >> 16) & 0xFFFFFF) + 0.5f) * 0x1p-24f;
+    const uint64_t h2 = mix64(h);
+    const float u2 = (float)(h2 >> 40) * 0x1p-24f;
+    float lmax = -1e30f;
+    for (int k = 0; k < K; ++k) lmax = fmaxf(lmax, o[k]);
+    float zs = 0.0f;
+    for (int k = 0; k < K; ++k) zs += __expf(o[k] - lmax);
+    float acc = 0.0f;
+    int c = K - 1;
+    for (int k = 0; k < K; ++k) {
+        acc += __expf(o[k] - lmax) / zs;
+        if (u0 < acc) {
+            c = k;
+            break;
+        }
+    }
+    const float rad = sqrtf(-2.0f * logf(u1)), ang = 6.2831853f * u2;
+    const float s1 = softplusf_(o[3 * K + c]) + 1e-3f, s2 = softplusf_(o[4 * K + c]) + 1e-3f;
+    out[2 * row] = o[K + c] + s1 * rad * cosf(ang);
+    out[2 * row + 1] = o[2 * K + c] + s2 * rad * sinf(ang);
+}
+
+}  // namespace
+
+}  // namespace rbg
+
+extern "C" {
+
+// Surrogate kernels (device pointers, the caller's stream).  Internal to the
+// Python surrogate module; no counterpart in the reference.
+int rbg_mdn_gemm(const void *A, int lda, int ta, const void *B, int ldb, int tb, float *C, int ldc, int M, int N,
+                 int K, float beta, void *stream) {
+    using namespace rbg;
+    const dim3 grid((N + kTileN - 1) / kTileN, (M + kTileM - 1) / kTileM);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto a = static_cast<const __nv_bfloat16 *>(A);
+    auto b = static_cast<const __nv_bfloat16 *>(B);
+    if (ta && tb) gemm_bf16_kernel<true, true><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta);
+    else if (ta) gemm_bf16_kernel<true, false><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta);
+    else if (tb) gemm_bf16_kernel<false, true><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta);
+    else gemm_bf16_kernel<false, false><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta);
+    return (int)cudaGetLastError();
+}
+
+int rbg_mdn_bias_act(float *Z, const float *b, void *H, int M, int N, int act, void *stream) {
+    const size_t n = (size_t)M * N;
+    rbg::bias_act_kernel<<<(unsigned)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        Z, b, static_cast<__nv_bfloat16 *>(H), M, N, act);
+    return (int)cudaGetLastError();
+}
+
+int rbg_mdn_silu_backward(const float *Z, const float *dH, void *dZ, float *db, int M, int N, void *stream) {
+    rbg::silu_backward_kernel<<<(N + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+        Z, dH, static_cast<__nv_bfloat16 *>(dZ), db, M, N);
+    return (int)cudaGetLastError();
+}
+
+int rbg_mdn_head_backward(const float *G, void *Gb, float *db, int M, int N, void *stream) {
+    rbg::head_backward_kernel<<<(N + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+        G, static_cast<__nv_bfloat16 *>(Gb), db, M, N);
+    return (int)cudaGetLastError();
+}
+
+int rbg_mdn_loss(const float *O, const float *Y, int B, int K, float *loss, float *G, void *stream) {
+    if (K > 16) return (int)cudaErrorInvalidValue;
+    rbg::mdn_loss_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, Y, B, K, loss, G);
+    return (int)cudaGetLastError();
+}
+
+int rbg_mdn_adam(float *w, void *wb, const float *g, float *m, float *v, int n, float lr, float b1, float b2,
+                 float eps, int step, void *stream) {
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    rbg::adam_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        w, static_cast<__nv_bfloat16 *>(wb), g, m, v, n, lr, b1, b2, eps, c1, c2);
+    return (int)cudaGetLastError();
+}
+
+int rbg_mdn_sample(const float *O, int B, int K, uint64_t seed, float *out, void *stream) {
+    rbg::mdn_sample_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, B, K, seed, out);
+    return (int)cudaGetLastError();
+}
+
+}  // extern "C"

@@ -1,0 +1,71 @@
+"""The learned surrogate's kernels: tensor-core GEMM against float64, the
+network's loss and gradients against the CPU oracle, and a short training run
+on engine-generated data."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+def test_gemm_bf16_all_transposes(torch):
+    from rebop_gb300._lib import check, lib
+
+    rng = np.random.default_rng(0)
+    for (M, N, K) in [(64, 64, 32), (100, 72, 40), (257, 130, 300), (40, 256, 4096)]:
+        for ta in (0, 1):
+            for tb in (0, 1):
+                a = torch.tensor(rng.standard_normal((K, M) if ta else (M, K)), dtype=torch.bfloat16).cuda()
+                b = torch.tensor(rng.standard_normal((N, K) if tb else (K, N)), dtype=torch.bfloat16).cuda()
+                c = torch.empty(M, N, dtype=torch.float32, device="cuda")
+                check(lib.rbg_mdn_gemm(a.data_ptr(), a.shape[1], ta, b.data_ptr(), b.shape[1], tb, c.data_ptr(), N,
+                                       M, N, K, 0.0, torch.cuda.current_stream().cuda_stream))
+                A = a.double().cpu().numpy()
+                B = b.double().cpu().numpy()
+                ref = (A.T if ta else A) @ (B.T if tb else B)
+                err = np.abs(c.cpu().numpy() - ref).max() / (np.abs(ref).max() + 1e-30)
+                assert err < 1e-5, (M, N, K, ta, tb, err)
+
+
+def test_mdn_gradients_match_oracle(torch):
+    from oracle import mdn_oracle
+    from rebop_gb300 import surrogate as sg
+
+    rng = np.random.default_rng(1)
+    model = sg.MDN(seed=3)
+    x = rng.uniform(-1, 1, size=(512, 6)).astype(np.float32)
+    x[:, 5] = rng.uniform(0, 1, 512)
+    y = np.stack([rng.uniform(0, 8, 512), rng.uniform(0, 6, 512)], axis=1).astype(np.float32)
+    model.x_mean = torch.tensor(x.mean(0)).cuda()
+    model.x_std = torch.tensor(x.std(0) + 1e-6).cuda()
+    loss, dW, db = model.loss_and_grad(torch.tensor(x).cuda(), torch.tensor(y).cuda())
+    W = [w.double().cpu().numpy() for w in model.Wb]
+    b = [v.double().cpu().numpy() for v in model.b]
+    rl, rW, rb = mdn_oracle.forward_backward(W, b, x.astype(np.float64), y.astype(np.float64),
+                                             model.x_mean.double().cpu().numpy(), model.x_std.double().cpu().numpy())
+    assert abs(float(loss) - rl) <= 1e-3 * abs(rl) + 1e-4
+    for i in range(len(W)):
+        g, r = dW[i].double().cpu().numpy(), rW[i]
+        assert np.linalg.norm(g - r) <= 2e-2 * np.linalg.norm(r) + 1e-7, ("dW", i)
+        g, r = db[i].double().cpu().numpy(), rb[i]
+        assert np.linalg.norm(g - r) <= 2e-2 * np.linalg.norm(r) + 1e-7, ("db", i)
+
+
+def test_mdn_training_lowers_the_loss(torch):
+    from rebop_gb300 import surrogate as sg
+
+    x, y, _ = sg.generate(400, seed=5, nb_steps=50)
+    model = sg.MDN(seed=1)
+    X, Y = torch.tensor(x).cuda(), torch.tensor(y).cuda()
+    model.x_mean, model.x_std = X.mean(0), X.std(0) + 1e-6
+    before = float(model.loss_and_grad(X[:4096], Y[:4096])[0])
+    model.fit(x, y, epochs=8, batch=1024, lr=3e-3)
+    after = float(model.loss_and_grad(X[:4096], Y[:4096])[0])
+    assert after < before - 1.0, (before, after)
+    c = model.sample_counts(x[:16], 200).cpu().numpy()
+    assert c.shape == (16, 200, 2) and (c >= 0).all()
