@@ -512,19 +512,104 @@ def run_batch(args):
         "cpu_baseline": cpu, "clocks": clk}), flush=True)
 
 
+SURROGATE = dict(
+    name="surrogate",
+    desc=("learned surrogate of the dimer ensemble: 2^20 training tuples generated by the engine, one per "
+          "trajectory (5 rate factors 10^U[-1,1] around 25, 1000, 0.001, 0.1, 1; t drawn from the 101-point grid "
+          "of [0, 1]); MLP 6 -> 4 x 256 "
+          "SiLU -> 8-component Gaussian mixture over log1p(protein, dimer), BF16 weights, FP32 accumulation; "
+          "held-out points judged against fresh SSA batches"),
+    n_traj=1 << 20, epochs=30, batch=4096, lr=2e-3, n_points=128, n_ssa=1000, n_points_big=32, n_ssa_big=10000,
+    n_queries=1_000_000, draws=1000,
+)
+
+
+def run_surrogate(args):
+    import torch
+
+    from rebop_gb300 import surrogate as sg
+
+    w = SURROGATE
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    t0 = time.perf_counter()
+    x, y, _ = sg.generate(w["n_traj"], seed=20260106)
+    t_gen = time.perf_counter() - t0
+    model = sg.MDN(seed=0)
+    t0 = time.perf_counter()
+    model.fit(x, y, epochs=w["epochs"], batch=w["batch"], lr=w["lr"])
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    sur = sg.Surrogate(model, tol=0.01)
+    val = sur.validate(w["n_points"], w["n_ssa"], seed=7)
+    big = sg.Surrogate(model, tol=0.01).validate(w["n_points_big"], w["n_ssa_big"], seed=8)
+    # throughput: queries answered by the surrogate (one forward pass and `draws`
+    # samples each) against queries answered by the SSA engine (`draws` trajectories)
+    rng = np.random.default_rng(9)
+    q = np.concatenate([rng.uniform(-1, 1, (w["n_queries"], 5)), rng.integers(1, 101, (w["n_queries"], 1)) / 100],
+                       axis=1).astype(np.float32)
+    Q = torch.from_numpy(q).cuda()
+    chunk = 8192
+    for s in range(0, 3 * chunk, chunk):  # warm-up
+        model.sample_counts(Q[s:s + chunk], w["draws"])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n_q = 131072
+    e0.record()
+    for s in range(0, n_q, chunk):
+        model.sample_counts(Q[s:s + chunk], w["draws"])
+    e1.record()
+    torch.cuda.synchronize()
+    sur_qps = n_q / (e0.elapsed_time(e1) / 1e3)
+    e0.record()
+    for s in range(0, w["n_queries"], 65536):
+        model.predict_params(Q[s:s + 65536])
+    e1.record()
+    torch.cuda.synchronize()
+    param_qps = w["n_queries"] / (e0.elapsed_time(e1) / 1e3)
+    ssa_qps = w["n_points"] / (val["ssa_kernel_ms"] / 1e3)
+    answered = sur.answer(q[:100000]).mean()
+    med = lambda a: float(np.median(a))  # noqa: E731
+    line = {
+        "metric": "surrogate queries/s (1000 draws each) vs plain GPU SSA queries/s (1000 trajectories each)",
+        "value": sur_qps, "unit": "queries/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": 1e3 * n_q / sur_qps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 weights, fp32 accumulation", "data": "synthetic (engine-generated)",
+        "config": {"workload": w["desc"], "training_tuples": int(x.shape[0]), "epochs": w["epochs"],
+                   "generate_s": t_gen, "train_s": t_train},
+        "ssa_queries_per_s": ssa_qps, "speedup_vs_ssa": sur_qps / ssa_qps, "params_only_queries_per_s": param_qps,
+        "accuracy_1e3": {
+            "points": w["n_points"], "median_w1_rel": [med(val["w1"][:, 0]), med(val["w1"][:, 1])],
+            "median_w1_rel_ssa_vs_ssa": [med(val["w1_floor"][:, 0]), med(val["w1_floor"][:, 1])],
+            "fraction_w1_within_1pct": float(np.mean((val["w1"] <= 0.01).all(axis=1))),
+            "fraction_w1_within_1pct_ssa_vs_ssa": float(np.mean((val["w1_floor"] <= 0.01).all(axis=1))),
+            "median_ks": [med(val["ks"][:, 0]), med(val["ks"][:, 1])]},
+        "accuracy_1e4": {
+            "points": w["n_points_big"], "median_w1_rel": [med(big["w1"][:, 0]), med(big["w1"][:, 1])],
+            "median_w1_rel_ssa_vs_ssa": [med(big["w1_floor"][:, 0]), med(big["w1_floor"][:, 1])],
+            "fraction_w1_within_1pct": float(np.mean((big["w1"] <= 0.01).all(axis=1))),
+            "median_ks": [med(big["ks"][:, 0]), med(big["ks"][:, 1])]},
+        "answered_by_surrogate": float(answered),
+        "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch"], default="dimer")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch", "surrogate"], default="dimer")
     ap.add_argument("--n-traj", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "surrogate":
+        run_surrogate(args)
         return
     w = WORKLOADS[args.workload]
     if args.impl == "reference":

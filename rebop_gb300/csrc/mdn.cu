@@ -206,11 +206,12 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     return z ^ (z >> 31);
 }
 
-// One draw per row: component by its weight, then two Gaussians (Box-Muller).
-__global__ void mdn_sample_kernel(const float *O, int B, int K, uint64_t seed, float *out) {
+// Draws: row r of out takes query r / per_query's mixture; component by its
+// weight, then two Gaussians (Box-Muller).
+__global__ void mdn_sample_kernel(const float *O, int B, int K, uint64_t seed, float *out, int per_query) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= B) return;
-    const float *o = O + (size_t)row * 5 * K;
+    const float *o = O + (size_t)(row / per_query) * 5 * K;
     const uint64_t h = mix64(seed ^ mix64((uint64_t)row + 0x9E3779B97F4A7C15ull));
     const float u0 = (float)(h >> 40) * 0x1p-24f, u1 = ((float)((h >> 16) & 0xFFFFFF) + 0.5f) * 0x1p-24f;
     const uint64_t h2 = mix64(h);
@@ -289,8 +290,10 @@ int rbg_mdn_adam(float *w, void *wb, const float *g, float *m, float *v, int n, 
     return (int)cudaGetLastError();
 }
 
-int rbg_mdn_sample(const float *O, int B, int K, uint64_t seed, float *out, void *stream) {
-    rbg::mdn_sample_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, B, K, seed, out);
+int rbg_mdn_sample(const float *O, int B, int K, uint64_t seed, float *out, int per_query, void *stream) {
+    if (per_query < 1) return (int)cudaErrorInvalidValue;
+    rbg::mdn_sample_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, B, K, seed, out,
+                                                                                          per_query);
     return (int)cudaGetLastError();
 }
 

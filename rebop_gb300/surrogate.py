@@ -35,22 +35,28 @@ def dimer_network(rates=RATES0):
     return net
 
 
-def generate(n_traj: int, seed: int, nb_steps: int = 100, net=None):
+def generate(n_traj: int, seed: int, nb_steps: int = 100, net=None, per_traj: int = 1, chunk: int = 1 << 17):
     """SSA training data: per-trajectory rate factors 10^u, u ~ U[-1, 1]^5, and
-    every trajectory's samples at t = i / nb_steps.  Returns inputs [n*(nb+1)][6]
-    (u, t), targets [n*(nb+1)][2] (log1p protein, log1p dimer) and the raw counts."""
+    `per_traj` sample times per trajectory drawn from the grid t = i / nb_steps
+    (one by default, so every tuple is an independent draw of its
+    distribution).  Returns inputs [n*per_traj][6] (u, t) and targets
+    [n*per_traj][2] (log1p protein, log1p dimer)."""
     rng = np.random.default_rng(seed)
-    u = rng.uniform(-1.0, 1.0, size=(n_traj, 5))
-    rates = np.asarray(RATES0) * 10.0 ** u
-    seeds = rng.integers(np.iinfo(np.uint64).max, size=n_traj, dtype=np.uint64)
     net = net or dimer_network()
-    res = net.run_ensemble(list(X0), seeds, 1.0, nb_steps, save=[2, 3], rates=rates, want_events=False)
-    c = res.counts  # [nb+1][2][n]
-    t = np.arange(nb_steps + 1) / nb_steps
-    x = np.concatenate([np.repeat(u[None], nb_steps + 1, 0), np.broadcast_to(t[:, None, None], (nb_steps + 1, n_traj, 1))],
-                       axis=2).reshape(-1, 6)
-    y = np.log1p(np.transpose(c, (0, 2, 1)).reshape(-1, 2).astype(np.float64))
-    return x.astype(np.float32), y.astype(np.float32), c
+    xs, ys = [], []
+    for c0 in range(0, n_traj, chunk):
+        n = min(chunk, n_traj - c0)
+        u = rng.uniform(-1.0, 1.0, size=(n, 5))
+        rates = np.asarray(RATES0) * 10.0 ** u
+        seeds = rng.integers(np.iinfo(np.uint64).max, size=n, dtype=np.uint64)
+        res = net.run_ensemble(list(X0), seeds, 1.0, nb_steps, save=[2, 3], rates=rates, want_events=False)
+        c = res.counts  # [nb+1][2][n]
+        ti = rng.integers(0, nb_steps + 1, size=(n, per_traj))
+        j = np.repeat(np.arange(n), per_traj)
+        t = ti.reshape(-1)
+        xs.append(np.concatenate([u[j], (t / nb_steps)[:, None]], axis=1))
+        ys.append(np.log1p(np.stack([c[t, 0, j], c[t, 1, j]], axis=1).astype(np.float64)))
+    return np.concatenate(xs).astype(np.float32), np.concatenate(ys).astype(np.float32), None
 
 
 class MDN:
@@ -178,21 +184,84 @@ class MDN:
                 log(f"epoch {ep}: loss {tot / max(cnt, 1):.4f}")
 
     def sample_counts(self, x, n_draws: int, seed: int = 1):
-        """n_draws samples of (protein, dimer) counts at each query row of x [Q][6]."""
+        """n_draws samples of (protein, dimer) counts at each query row of x [Q][6]:
+        one forward pass per query, then n_draws draws from its mixture."""
+        X = self._queries(x)
         torch = self.torch
-        X = torch.as_tensor(np.ascontiguousarray(x), device=self.dev)
-        rep = X.repeat_interleave(n_draws, dim=0).contiguous()
-        o = self.forward(rep)
-        z = torch.empty(rep.shape[0], 2, dtype=torch.float32, device=self.dev)
-        check(lib.rbg_mdn_sample(o.data_ptr(), rep.shape[0], K, int(seed), z.data_ptr(), self._s()))
+        o = self.forward(X)
+        z = torch.empty(X.shape[0] * n_draws, 2, dtype=torch.float32, device=self.dev)
+        check(lib.rbg_mdn_sample(o.data_ptr(), z.shape[0], K, int(seed), z.data_ptr(), int(n_draws), self._s()))
         c = torch.clamp(torch.round(torch.expm1(z)), min=0)
         return c.view(X.shape[0], n_draws, 2)
 
     def predict_params(self, x):
         """Mixture parameters at each query row (one forward pass): [Q][40]."""
+        return self.forward(self._queries(x))
+
+    def _queries(self, x):
         torch = self.torch
-        X = torch.as_tensor(np.ascontiguousarray(x), device=self.dev)
-        return self.forward(X.contiguous())
+        if isinstance(x, torch.Tensor):
+            return x.to(self.dev, torch.float32).contiguous()
+        return torch.as_tensor(np.ascontiguousarray(x, dtype=np.float32), device=self.dev)
+
+
+class Surrogate:
+    """A trained MDN plus the validation that says where it may answer.
+
+    `validate` compares the MDN with fresh SSA batches at held-out points; a
+    query then takes the MDN's answer when the nearest validation point (in
+    (u, t) space) met the tolerance, and falls back to the SSA engine
+    otherwise."""
+
+    def __init__(self, model: MDN, tol: float = 0.01):
+        self.model = model
+        self.tol = tol
+        self.points = None
+        self.ok = None
+
+    def validate(self, n_points: int, n_ssa: int, seed: int, net=None):
+        """Per held-out point: relative W1 and KS of the MDN against a fresh SSA
+        batch of n_ssa trajectories, and the same for a second independent SSA
+        batch (the sampling-noise floor of the comparison)."""
+        rng = np.random.default_rng(seed)
+        u = rng.uniform(-1, 1, size=(n_points, 5))
+        ti = rng.integers(1, 101, size=n_points)
+        t = ti / 100.0
+        net = net or dimer_network()
+        rates = np.repeat(np.asarray(RATES0) * 10.0 ** u, n_ssa, axis=0)
+        runs = []
+        import time
+
+        for rep in range(2):
+            seeds = rng.integers(np.iinfo(np.uint64).max, size=n_points * n_ssa, dtype=np.uint64)
+            t0 = time.perf_counter()
+            res = net.run_ensemble(list(X0), seeds, 1.0, 100, save=[2, 3], rates=rates, want_events=False)
+            runs.append((res.counts, time.perf_counter() - t0, res.stats["kernel_ms"]))
+        x = np.concatenate([u, t[:, None]], axis=1).astype(np.float32)
+        draws = self.model.sample_counts(x, n_ssa, seed=seed + 1).cpu().numpy()
+        out = {"w1": np.zeros((n_points, 2)), "ks": np.zeros((n_points, 2)), "w1_floor": np.zeros((n_points, 2)),
+               "mean": np.zeros((n_points, 2))}
+        for p in range(n_points):
+            sl = slice(p * n_ssa, (p + 1) * n_ssa)
+            for s in range(2):
+                a = runs[0][0][ti[p], s, sl].astype(np.float64)
+                b = runs[1][0][ti[p], s, sl].astype(np.float64)
+                m = draws[p, :, s]
+                mean = max(a.mean(), 1.0)
+                out["mean"][p, s] = a.mean()
+                out["w1"][p, s] = wasserstein1(m, a) / mean
+                out["w1_floor"][p, s] = wasserstein1(b, a) / mean
+                out["ks"][p, s] = ks_distance(m, a)
+        self.points = x
+        self.ok = (out["w1"] <= self.tol).all(axis=1)
+        out["ssa_seconds"] = runs[0][1]
+        out["ssa_kernel_ms"] = runs[0][2]
+        return out
+
+    def answer(self, x):
+        """Which queries of x [Q][6] the MDN answers (True) and which fall back."""
+        d = ((x[:, None, :] - self.points[None, :, :]) ** 2).sum(-1)
+        return self.ok[np.argmin(d, axis=1)]
 
 
 def wasserstein1(a: np.ndarray, b: np.ndarray) -> float:

@@ -59,7 +59,7 @@ def test_mdn_gradients_match_oracle(torch):
 def test_mdn_training_lowers_the_loss(torch):
     from rebop_gb300 import surrogate as sg
 
-    x, y, _ = sg.generate(400, seed=5, nb_steps=50)
+    x, y, _ = sg.generate(20000, seed=5, nb_steps=50)
     model = sg.MDN(seed=1)
     X, Y = torch.tensor(x).cuda(), torch.tensor(y).cuda()
     model.x_mean, model.x_std = X.mean(0), X.std(0) + 1e-6
