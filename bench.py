@@ -567,6 +567,27 @@ def run_surrogate(args):
     torch.cuda.synchronize()
     param_qps = w["n_queries"] / (e0.elapsed_time(e1) / 1e3)
     ssa_qps = w["n_points"] / (val["ssa_kernel_ms"] / 1e3)
+    # the training GEMM shape (4096 x 256 x 256, BF16 in, FP32 out) on both tensor-core kernels
+    from rebop_gb300._lib import check, lib
+
+    ga = torch.randn(4096, 256, device="cuda").to(torch.bfloat16)
+    gb = torch.randn(256, 256, device="cuda").to(torch.bfloat16)
+    gc = torch.empty(4096, 256, device="cuda")
+    gemm_tflops = {}
+    st = torch.cuda.current_stream().cuda_stream
+    for name in ("tc05", "mma"):
+        for rep in range(60):
+            if rep == 10:
+                e0.record()
+            if name == "tc05":
+                check(lib.rbg_mdn_gemm_tc05(ga.data_ptr(), 256, 0, gb.data_ptr(), 256, 1, gc.data_ptr(), 256, 4096, 256,
+                                            256, 0.0, model.tc_err.data_ptr(), st))
+            else:
+                check(lib.rbg_mdn_gemm(ga.data_ptr(), 256, 0, gb.data_ptr(), 256, 1, gc.data_ptr(), 256, 4096, 256, 256,
+                                       0.0, st))
+        e1.record()
+        torch.cuda.synchronize()
+        gemm_tflops[name] = 50 * 2 * 4096 * 256 * 256 / (e0.elapsed_time(e1) / 1e3) / 1e12
     answered = sur.answer(q[:100000]).mean()
     med = lambda a: float(np.median(a))  # noqa: E731
     line = {
@@ -589,6 +610,7 @@ def run_surrogate(args):
             "fraction_w1_within_1pct": float(np.mean((big["w1"] <= 0.01).all(axis=1))),
             "median_ks": [med(big["ks"][:, 0]), med(big["ks"][:, 1])]},
         "answered_by_surrogate": float(answered),
+        "gemm_4096x256x256_tflops": gemm_tflops,
         "gpu_launches": None,
     }
     print(json.dumps(line), flush=True)

@@ -118,6 +118,8 @@ _f32 = C.c_float
 for _name, _args in {
     "rbg_mdn_gemm": [_vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _f32,
                      _vp],
+    "rbg_mdn_gemm_tc05": [_vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int,
+                          _f32, _vp, _vp],
     "rbg_mdn_bias_act": [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp],
     "rbg_mdn_silu_backward": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp],
     "rbg_mdn_head_backward": [_vp, _vp, _vp, C.c_int, C.c_int, _vp],

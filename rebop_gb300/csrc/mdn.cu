@@ -105,6 +105,174 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
             }
 }
 
+// ---------------------------------------------------------------- tcgen05
+// The same product on the 5th-generation tensor cores: one CTA of four warps
+// owns a 128 x 32 tile of C in tensor memory (32 columns of 32-bit
+// accumulators); K advances in chunks of 64 staged in shared memory in the
+// canonical K-major layout without swizzle (8 x 16-byte core matrices,
+// adjacent along K at 128 B, along M/N at 1 KiB); one thread issues four
+// tcgen05.mma (K = 16 each) per chunk and commits them to an mbarrier that
+// every thread waits on, with an iteration limit, before the next chunk
+// overwrites the operands.  Each warp then reads its 32 rows from its own
+// tensor-memory lane quadrant.  A wait that runs out sets *err and the tile
+// is left unwritten; tensor memory is always freed.
+constexpr int kTcM = 128, kTcN = 32, kTcK = 64;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start >> 4, leading (K) byte offset >> 4,
+// stride (M/N) byte offset >> 4, descriptor version 1 (bits 46-48), no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__restrict__ A, int lda,
+                                                        const __nv_bfloat16 *__restrict__ B, int ldb,
+                                                        float *__restrict__ C, int ldc, int M, int N, int K,
+                                                        float beta, int *err) {
+    __shared__ __align__(1024) __nv_bfloat16 As[kTcM * kTcK];
+    __shared__ __align__(1024) __nv_bfloat16 Bs[kTcN * kTcK];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int failed;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+    const uint32_t mb = smem_u32(&mbar);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "r"(kTcN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb));
+        failed = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_base;
+    // idesc: F32 accumulator, BF16 A and B, both K-major, N >> 3, M >> 4
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                           ((uint32_t)(kTcM >> 4) << 24);
+    const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+    uint32_t parity = 0;
+    int chunk = 0;
+    for (int k0 = 0; k0 < K; k0 += kTcK, ++chunk) {
+        // operands -> canonical layout: (r, k) at ((r/8)*(kTcK/8) + k/8)*64 + (r%8)*8 + k%8 elements
+        // K-contiguous rows with 16-byte aligned starts move 8 elements at a
+        // time (one core-matrix row); anything else element by element
+        const bool a_vec = !TA && (lda % 8) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+        const bool b_vec = TB && (ldb % 8) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
+        if (a_vec) {
+            for (int e = tid; e < kTcM * kTcK / 8; e += 128) {
+                const int r = e / (kTcK / 8), k8 = e % (kTcK / 8), m = m0 + r, kk = k0 + k8 * 8;
+                uint4 v = make_uint4(0, 0, 0, 0);
+                if (m < M && kk + 8 <= K) v = *reinterpret_cast<const uint4 *>(A + (size_t)m * lda + kk);
+                else if (m < M)
+                    for (int j = 0; j < 8; ++j)
+                        reinterpret_cast<__nv_bfloat16 *>(&v)[j] = kk + j < K ? A[(size_t)m * lda + kk + j] : zero;
+                *reinterpret_cast<uint4 *>(&As[((r >> 3) * (kTcK / 8) + k8) * 64 + (r & 7) * 8]) = v;
+            }
+        } else {
+            for (int e = tid; e < kTcM * kTcK; e += 128) {
+                const int r = e / kTcK, k = e % kTcK, m = m0 + r, kk = k0 + k;
+                const __nv_bfloat16 v =
+                    (m < M && kk < K) ? (TA ? A[(size_t)kk * lda + m] : A[(size_t)m * lda + kk]) : zero;
+                As[((r >> 3) * (kTcK / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7)] = v;
+            }
+        }
+        if (b_vec) {
+            for (int e = tid; e < kTcN * kTcK / 8; e += 128) {
+                const int r = e / (kTcK / 8), k8 = e % (kTcK / 8), n = n0 + r, kk = k0 + k8 * 8;
+                uint4 v = make_uint4(0, 0, 0, 0);
+                if (n < N && kk + 8 <= K) v = *reinterpret_cast<const uint4 *>(B + (size_t)n * ldb + kk);
+                else if (n < N)
+                    for (int j = 0; j < 8; ++j)
+                        reinterpret_cast<__nv_bfloat16 *>(&v)[j] = kk + j < K ? B[(size_t)n * ldb + kk + j] : zero;
+                *reinterpret_cast<uint4 *>(&Bs[((r >> 3) * (kTcK / 8) + k8) * 64 + (r & 7) * 8]) = v;
+            }
+        } else {
+            for (int e = tid; e < kTcN * kTcK; e += 128) {
+                const int r = e / kTcK, k = e % kTcK, n = n0 + r, kk = k0 + k;
+                const __nv_bfloat16 v =
+                    (n < N && kk < K) ? (TB ? B[(size_t)n * ldb + kk] : B[(size_t)kk * ldb + n]) : zero;
+                Bs[((r >> 3) * (kTcK / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7)] = v;
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0 && !failed) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            for (int s = 0; s < kTcK / 16; ++s) {
+                const uint64_t ad = smem_desc(smem_u32(As) + s * 256, 128, (kTcK / 8) * 128);
+                const uint64_t bd = smem_desc(smem_u32(Bs) + s * 256, 128, (kTcK / 8) * 128);
+                const uint32_t acc = (chunk > 0 || s > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
+                         : "memory");
+        }
+        __syncthreads();
+        if (!failed) {
+            if (!mbar_wait(mb, parity)) failed = 1;
+        }
+        parity ^= 1u;
+        __syncthreads();
+        if (failed) break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    if (!failed) {
+        // warp w reads tensor-memory lanes 32w .. 32w+31 = rows of its quadrant
+        const int row = m0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < kTcN; c0 += 16) {
+            uint32_t v[16];
+            const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(addr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (row < M)
+                for (int j = 0; j < 16; ++j) {
+                    const int n = n0 + c0 + j;
+                    if (n < N) {
+                        float *c = C + (size_t)row * ldc + n;
+                        const float x = __uint_as_float(v[j]);
+                        *c = beta == 0.0f ? x : __fmaf_rn(beta, *c, x);
+                    }
+                }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTcN));
+}
+
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + __expf(-x)); }
 
 // Z[m][n] += b[n]; H = bf16(silu(Z)) (act = 1) or bf16(Z) (act = 0).
@@ -254,6 +422,22 @@ int rbg_mdn_gemm(const void *A, int lda, int ta, const void *B, int ldb, int tb,
     else if (ta) gemm_bf16_kernel<true, false><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta);
     else if (tb) gemm_bf16_kernel<false, true><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta);
     else gemm_bf16_kernel<false, false><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta);
+    return (int)cudaGetLastError();
+}
+
+// The same product on tcgen05 (see gemm_tc05_kernel); *err (device int) is set
+// if a completion wait ran out.
+int rbg_mdn_gemm_tc05(const void *A, int lda, int ta, const void *B, int ldb, int tb, float *C, int ldc, int M,
+                      int N, int K, float beta, int *err, void *stream) {
+    using namespace rbg;
+    const dim3 grid((N + kTcN - 1) / kTcN, (M + kTcM - 1) / kTcM);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto a = static_cast<const __nv_bfloat16 *>(A);
+    auto b = static_cast<const __nv_bfloat16 *>(B);
+    if (ta && tb) gemm_tc05_kernel<true, true><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
+    else if (ta) gemm_tc05_kernel<true, false><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
+    else if (tb) gemm_tc05_kernel<false, true><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
+    else gemm_tc05_kernel<false, false><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
     return (int)cudaGetLastError();
 }
 

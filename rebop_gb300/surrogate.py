@@ -5,8 +5,8 @@ in [0, 1]).
 A multilayer perceptron (6 inputs -> 4 x 256 SiLU -> 40) maps
 (log10 rate factors, t) to an 8-component diagonal Gaussian mixture over
 (log1p protein, log1p dimer) counts.  Weights are BF16 with FP32 master
-copies; every forward and backward GEMM runs in the engine's tensor-core
-kernel with FP32 accumulation, and the loss, its gradient, the optimiser and
+copies; every forward and backward GEMM runs on the 5th-generation tensor
+cores (tcgen05.mma into tensor memory, FP32 accumulation), and the loss, its gradient, the optimiser and
 the sampler are the engine's own kernels (rebop_gb300/csrc/mdn.cu).  PyTorch
 only holds the device memory.  Training data, the validation that decides
 where the surrogate is trusted, and the fallback for the rest all come from
@@ -81,6 +81,10 @@ class MDN:
         self.mb = [torch.zeros_like(b) for b in self.b]
         self.vb = [torch.zeros_like(b) for b in self.b]
         self.step = 0
+        import os
+
+        self.use_tc05 = os.environ.get("RB_GEMM", "tc05") != "mma"
+        self.tc_err = torch.zeros(1, dtype=torch.int32, device=device)
         # input and target normalisation (set from the training data)
         self.x_mean = torch.zeros(N_IN, device=device)
         self.x_std = torch.ones(N_IN, device=device)
@@ -90,8 +94,19 @@ class MDN:
         return self.torch.cuda.current_stream().cuda_stream
 
     def _gemm(self, A, ta, B, tb, C, M, N, K_, lda, ldb, beta=0.0):
-        check(lib.rbg_mdn_gemm(A.data_ptr(), lda, int(ta), B.data_ptr(), ldb, int(tb), C.data_ptr(), N, M, N, K_,
-                               float(beta), self._s()))
+        # tcgen05 with tensor-memory accumulators; RB_GEMM=mma selects the
+        # mma.sync kernel instead
+        if self.use_tc05:
+            check(lib.rbg_mdn_gemm_tc05(A.data_ptr(), lda, int(ta), B.data_ptr(), ldb, int(tb), C.data_ptr(), N, M,
+                                        N, K_, float(beta), self.tc_err.data_ptr(), self._s()))
+        else:
+            check(lib.rbg_mdn_gemm(A.data_ptr(), lda, int(ta), B.data_ptr(), ldb, int(tb), C.data_ptr(), N, M, N,
+                                   K_, float(beta), self._s()))
+
+    def check_errors(self):
+        """Raise if a tensor-core completion wait ran out since construction."""
+        if self.use_tc05 and int(self.tc_err.item()):
+            raise RuntimeError("tcgen05 GEMM: a completion wait ran out")
 
     def forward(self, x):
         """x [B][6] float (unnormalised u, t) -> head outputs [B][40]; keeps the
@@ -182,6 +197,7 @@ class MDN:
                 k += 1
             if log:
                 log(f"epoch {ep}: loss {tot / max(cnt, 1):.4f}")
+        self.check_errors()
 
     def sample_counts(self, x, n_draws: int, seed: int = 1):
         """n_draws samples of (protein, dimer) counts at each query row of x [Q][6]:

@@ -69,3 +69,27 @@ def test_mdn_training_lowers_the_loss(torch):
     assert after < before - 1.0, (before, after)
     c = model.sample_counts(x[:16], 200).cpu().numpy()
     assert c.shape == (16, 200, 2) and (c >= 0).all()
+
+
+def test_gemm_tcgen05_matches_float64(torch):
+    # the tcgen05 / tensor-memory kernel against float64, all transposes
+    from rebop_gb300._lib import check, lib
+
+    rng = np.random.default_rng(2)
+    err_flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for (M, N, K) in [(128, 64, 64), (200, 100, 80), (4096, 256, 256), (40, 256, 4096), (256, 40, 256)]:
+        for ta in (0, 1):
+            for tb in (0, 1):
+                a = torch.tensor(rng.standard_normal((K, M) if ta else (M, K)), dtype=torch.bfloat16).cuda()
+                b = torch.tensor(rng.standard_normal((N, K) if tb else (K, N)), dtype=torch.bfloat16).cuda()
+                c = torch.empty(M, N, dtype=torch.float32, device="cuda")
+                check(lib.rbg_mdn_gemm_tc05(a.data_ptr(), a.shape[1], ta, b.data_ptr(), b.shape[1], tb, c.data_ptr(),
+                                            N, M, N, K, 0.0, err_flag.data_ptr(),
+                                            torch.cuda.current_stream().cuda_stream))
+                torch.cuda.synchronize()
+                assert int(err_flag.item()) == 0
+                A = a.double().cpu().numpy()
+                B = b.double().cpu().numpy()
+                ref = (A.T if ta else A) @ (B.T if tb else B)
+                err = np.abs(c.cpu().numpy() - ref).max() / (np.abs(ref).max() + 1e-30)
+                assert err < 1e-5, (M, N, K, ta, tb, err)
