@@ -7,25 +7,31 @@
 // The random stream consumed follows from those decisions too.  And at every
 // sample time the clock is reset to T exactly (gillespie.rs:328-330).
 //
-// So each step here evaluates propensities, their running sum, the Exp1
-// abscissa, Exp1/total, the clock and total*U in float pairs (hi + lo,
-// about 46 bits) on the FP32 pipe -- the widest pipe of the SM -- together
-// with a bound on the distance of every quantity from the value rebop's
-// binary64 arithmetic produces.  A decision whose operands lie farther apart
-// than their bounds is the reference's decision.  When a decision falls inside
-// the margin (or a value leaves the float-pair range), the lane restores the
-// state it saved at the start of the sample interval and re-runs that interval
-// with the exact step of ssa_exact.cuh, so every recorded count, event count
-// and random draw equals rebop's bit for bit.  Intervals of trajectories whose
-// rates are outside the float-pair range always run exactly.
+// So each step here evaluates propensities and their running sum in float
+// pairs (hi + lo, about 46 bits), the clock as a float triple, Exp1/total in
+// float pairs and the choice in float32, all on the FP32 and integer pipes,
+// together with a bound on the distance of every quantity from the value
+// rebop's binary64 arithmetic produces.  A decision whose operands lie farther
+// apart than their bounds is the reference's decision:
+//   * a float32 choice comparison inside its margin (2^-21 of the total) is
+//     redone in binary64 for that step alone (Ops::exact_choice);
+//   * a clock comparison inside its margin, a count outside [0, 2^23) or a
+//     total outside 2^-90 .. 2^90 makes the lane restore the state it saved at
+//     the start of the sample interval and re-run that interval with the exact
+//     step of ssa_exact.cuh.
+// So every recorded count, event count and random draw equals rebop's bit for
+// bit.  Trajectories whose rates lie outside 2^-60 .. 2^60 run exactly.
 //
 // Error model: every float-pair operation (including the reference's own
 // binary64 rounding of the same operation) moves a value by at most
 // gamma = 2^-44 relative (the float-pair errors are near 2^-46, binary64's
-// 2^-53).  With M reactant factors per reaction at most and R reactions,
-// running sums are within G = (M + R + 2) gamma of the reference, the clock
-// increment within (G + 6 gamma) q plus the Exp1 abscissa's absolute error
-// over total, and each clock add adds 2 gamma t.
+// 2^-53).  With M reactant factors per reaction at most and R reactions, the
+// total is within G = (M + R + 2) gamma of the reference's and Exp1/total
+// within (G + 6 gamma) q plus the Exp1 abscissa's absolute error over the
+// total.  The triple-float clock add is exact up to its low part's rounding,
+// and the reference's own rounding of t + q adds at most 2^-53 (t + q): the
+// bound grows by 2^-52 t per event, accumulated with upward rounding.
+//
 // This header holds the device side, templated on the network operations of
 // the float-pair step: TableOps below walks the packed descriptor; a network
 // compiled at run time supplies the same members unrolled, with its counts in
