@@ -84,7 +84,38 @@ LARGE = dict(
           "tmax = 1.5 (~1e5 events per trajectory), nb_steps = 100"),
     S=200, reactions=_LR, x0=_LX0, tmax=1.5, nb_steps=100, n_traj=10_000, cpu_sample=32, sparse=True,
 )
-WORKLOADS = {"dimer": DIMER, "sir": SIR, "large": LARGE}
+
+
+def vilar_workload() -> dict:
+    """The reference's Vilar oscillator benchmark (benchmarks/benches/vilar/vilar.py:1-41),
+    read from the committed golden extract: 9 species in the order the run-time API
+    names them (first appearance), 16 mass-action reactions, x0 Da = Dr = 1,
+    tmax 200, nb_steps 200.  The reference times 100 trajectories of it."""
+    d = json.loads((ROOT / "tests/golden/reference_goldens.json").read_text())["vilar"]
+    names: list[str] = []
+    for r in d["reactions"]:
+        for s in r["reactants"] + r["products"]:
+            if s not in names:
+                names.append(s)
+    reactions = []
+    for r in d["reactions"]:
+        e = [r["reactants"].count(s) for s in names]
+        reactions.append((r["rate"], e, [r["products"].count(s) - x for s, x in zip(names, e)]))
+    run = d["run"]
+    return dict(
+        name="vilar",
+        desc=(f"Vilar oscillator ({len(names)} species, {len(reactions)} reactions, parameters of the "
+              f"reference benchmark), x0 Da=Dr=1, tmax={run['tmax']:g}, nb_steps={run['nb_steps']}"),
+        S=len(names), species=names, reactions=reactions,
+        x0=[run["init"].get(s, 0) for s in names], tmax=run["tmax"], nb_steps=run["nb_steps"],
+        n_traj=65_536, cpu_sample=256, calib_n=run["n_traj"],
+        # published wall time of the reference's own 100-trajectory run (rebopy, run-time API)
+        calib_published_s=5.811,
+    )
+
+
+VILAR = vilar_workload()
+WORKLOADS = {"dimer": DIMER, "sir": SIR, "large": LARGE, "vilar": VILAR}
 
 BATCH = dict(
     name="batch",
@@ -384,6 +415,27 @@ def run_ours(args, w):
                "sample": f"{nb} trajectories of the same workload, oracle port of the reference CPU path, "
                          f"{threads} threads"}
 
+    calib = None
+    if rank == 0 and w.get("calib_n"):
+        # the reference's own benchmark size: calib_n trajectories through the
+        # host API (host buffers, copies inside the timed region)
+        nc = int(w["calib_n"])
+        cs = seeds_for(rank, 900, nc)
+        net.run_ensemble(x0_host, cs, w["tmax"], w["nb_steps"], want_events=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = net.run_ensemble(x0_host, cs, w["tmax"], w["nb_steps"], want_events=True)
+        c_s = time.perf_counter() - t0
+        calib = {"n_traj": nc, "seconds": c_s, "events": int(rc.total_events),
+                 "published_reference_s": w["calib_published_s"],
+                 "note": "wall time of the reference's own run size through the host API on one GPU; "
+                         "the published figure is the reference's rebopy run on its authors' CPU"}
+        if not args.no_cpu_baseline:
+            # single-thread slope of the oracle port, the unit the reference's
+            # benchmark quotes (ms per trajectory on one core)
+            r1 = cpu_reference(w, 16, 1, 0, 1)
+            calib["cpu_port_1thread_ms_per_traj"] = 1e3 * r1["seconds"] / 16
+
     if rank == 0:
         line = {
             "metric": "SSA reaction events/sec", "value": value, "unit": "events/s", "n_gpus": world,
@@ -408,6 +460,8 @@ def run_ours(args, w):
             "cpu_baseline": cpu,
             "clocks": clk,
         }
+        if calib is not None:
+            line["config"]["reference_benchmark_run"] = calib
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -109,7 +109,37 @@ def extract(ref: Path) -> dict:
                                  "numpy_seed": int(np.random.default_rng(seed).integers(
                                      np.iinfo(np.uint64).max, dtype=np.uint64)),
                                  "where": f"tests/test_rebop.py:{i}"}
+    out["vilar"] = extract_vilar(ref)
     return out
+
+
+def extract_vilar(ref: Path) -> dict:
+    """Parameters, reactions and run arguments of the Vilar oscillator benchmark
+    as the run-time API builds it (benchmarks/benches/vilar/vilar.py)."""
+    path = "benchmarks/benches/vilar/vilar.py"
+    lines = (ref / path).read_text().splitlines()
+    params, reactions, run = {}, [], None
+    for i, line in enumerate(lines, 1):
+        m = re.match(r"^(\w+) = ([-\d.eE]+)\s*$", line)
+        if m:
+            params[m.group(1)] = float(m.group(2))
+            continue
+        m = re.search(r"\.add_reaction\((\w+), \[([^\]]*)\], \[([^\]]*)\]\)", line)
+        if m:
+            reactions.append({"rate_param": m.group(1), "rate": params[m.group(1)],
+                              "reactants": re.findall(r'"(\w+)"', m.group(2)),
+                              "products": re.findall(r'"(\w+)"', m.group(3)),
+                              "where": f"{path}:{i}"})
+            continue
+        m = re.search(r"for _ in range\((\d+)\):", line)
+        if m:
+            n_traj = int(m.group(1))
+        m = re.search(r"\.run\(\{([^}]*)\}, tmax=([-\d.eE]+), nb_steps=(\d+)\)", line)
+        if m:
+            run = {"init": {k: int(v) for k, v in re.findall(r'"(\w+)": (\d+)', m.group(1))},
+                   "tmax": float(m.group(2)), "nb_steps": int(m.group(3)),
+                   "n_traj": n_traj, "where": f"{path}:{i}"}
+    return {"params": params, "reactions": reactions, "run": run}
 
 
 if __name__ == "__main__":

@@ -115,6 +115,23 @@ def test_dsl_lowering(rb):
             rb.Network.from_dsl(bad)
 
 
+def test_vilar_dsl_agrees_with_runtime_extract(rb, goldens):
+    # The reference states the Vilar benchmark twice: define_system! in
+    # benchmarks/benches/vilar/vilar.rs and the run-time API in vilar.py.  The
+    # DSL lowering with the extracted parameter values must give the extracted
+    # reactions, in the same order, with the same rates and net changes.
+    vil = goldens["vilar"]
+    greek = {"α": "alpha", "β": "beta", "γ": "gamma", "δ": "delta", "θ": "theta"}
+    net = rb.Network.from_dsl(VILAR)
+    for p in net.params:
+        net.set_param(p, vil["params"]["".join(greek.get(c, c) for c in p)])
+    assert net.nb_reactions == len(vil["reactions"]) == 16
+    for i, r in enumerate(vil["reactions"]):
+        assert net.reaction_rate(i) == r["rate"]
+    assert vil["run"]["n_traj"] == 100 and vil["run"]["nb_steps"] == 200 and vil["run"]["tmax"] == 200.0
+    assert vil["run"]["init"] == {"Da": 1, "Dr": 1}
+
+
 def test_expr_parser_goldens(rb, goldens):
     from rebop_gb300 import expr
 
