@@ -271,6 +271,17 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
         set_error(std::string("RB_SSA_KERNEL=") + pref + " does not cover this network or sample grid");
         return false;
     }
+    // Ensembles too small to fill every SM scheduler with a full warp spread
+    // out: `lanes` trajectories per warp, one 4-warp block per SM, so each
+    // trajectory's step latency is close to a lone lane's (RB_SPEC_LANES=k
+    // sets k lanes per warp; 32 turns the spreading off).
+    int lanes = 0;
+    if (spec) {
+        const int64_t sched = (int64_t)ctx->sm_count * 4;
+        if (const char *e = std::getenv("RB_SPEC_LANES")) lanes = std::max(1, std::min(32, std::atoi(e)));
+        else if (r.n_traj < sched * 32) lanes = (int)((r.n_traj + sched - 1) / sched);
+        if (lanes >= 32) lanes = 0;
+    }
     int block, per_sm;
     size_t smem;
     if (warp) {
@@ -296,10 +307,11 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
         return true;
     }
     if (spec) {
-        block = ssa_spec_block();
-        a.n_slots = spec_slots;
+        block = lanes ? 128 : ssa_spec_block();
+        a.n_slots = lanes ? 128 : spec_slots;
+        a.lanes = lanes;
         if (const char *ph = std::getenv("RB_SPEC_PHASE")) a.phase_steps = std::atoi(ph);
-        smem = ssa_spec_smem(a, spec_slots);
+        smem = ssa_spec_smem(a, a.n_slots);
         per_sm = ssa_spec_occupancy(a, block, smem);
     } else if (fast) {
         block = 128;
@@ -316,29 +328,38 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
         per_sm = ssa_thread_occupancy(a, block, smem);
     }
     if (per_sm < 1) per_sm = 1;
-    int64_t want = (r.n_traj + block - 1) / block;
+    int64_t want = lanes ? (r.n_traj + 4 * lanes - 1) / (4 * lanes) : (r.n_traj + block - 1) / block;
     int64_t cap = (int64_t)ctx->sm_count * per_sm;
     int grid = (int)std::max<int64_t>(1, std::min(want, cap));
-    // A network the generator covers runs on its own compiled kernel when the
-    // ensemble is large enough to repay the compilation (RB_JIT=0 never,
-    // RB_JIT=1 always); results are the same either way.
+    // A network the generator covers runs on its own compiled kernel (RB_JIT=0
+    // never, RB_JIT=1 always; results are the same either way).  By default
+    // the kernel is compiled when the ensemble is large enough to repay the
+    // compilation or the network runs a second time, and used whenever it is
+    // already loaded or in the disk cache.
     const void *jk = nullptr;
+    const int64_t run_no = ++dn.runs;
     if (spec && jit_supported(p)) {
         const char *jit = std::getenv("RB_JIT");
-        const bool want = jit ? std::strcmp(jit, "0") != 0 : r.n_traj >= 4096;
-        if (want) {
+        // RB_SSA_KERNEL=spec asks for the packed-descriptor kernel itself
+        const bool off = (jit && std::strcmp(jit, "0") == 0) || (pref && std::strcmp(pref, "spec") == 0);
+        const bool compile = jit ? !off : (r.n_traj >= 4096 || run_no >= 2);
+        if (!off) {
             // generated kernels may run larger blocks (fewer registers per lane)
-            int jb = 512;
-            if (const char *e = std::getenv("RB_JIT_BLOCK")) jb = std::max(32, std::min(1024, std::atoi(e) / 32 * 32));
-            const int jgrid = (int)std::max<int64_t>(1, std::min<int64_t>(ctx->sm_count, (r.n_traj + jb - 1) / jb));
-            const int jslots = ssa_spec_slots(a, jgrid, ctx->smem_optin, jb);
+            int kb = 512;
+            if (const char *e = std::getenv("RB_JIT_BLOCK")) kb = std::max(32, std::min(1024, std::atoi(e) / 32 * 32));
+            const bool spread = lanes && kb >= 128;  // spread launches run 128 lanes of the same kernel
+            const int jb = spread ? 128 : kb;
+            const int jgrid = spread ? grid
+                                     : (int)std::max<int64_t>(1, std::min<int64_t>(ctx->sm_count, (r.n_traj + jb - 1) / jb));
+            const int jslots = spread ? 128 : ssa_spec_slots(a, jgrid, ctx->smem_optin, jb);
             if (jslots > 0) {
-                jk = jit_kernel(p, jb);
+                jk = jit_kernel(p, kb, compile);
                 if (!jk && jit && std::strcmp(jit, "1") == 0) return false;
                 if (jk) {
                     block = jb;
                     grid = jgrid;
                     a.n_slots = jslots;
+                    a.lanes = spread ? lanes : 0;
                     smem = ssa_spec_smem(a, jslots);
                 }
             }

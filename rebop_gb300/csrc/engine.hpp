@@ -52,6 +52,7 @@ struct DeviceNet {
     cudaStream_t stream = nullptr;      // library stream of host-pointer calls
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaStream_t last_stream = nullptr; // stream of the last device-pointer run
+    int64_t runs = 0;                   // sampled launches of this network
     ~DeviceNet();
 };
 

@@ -79,6 +79,10 @@ struct SsaArgs {
     // Speculative kernel: steps between two compactions of a warp's slots
     // (0: the default).
     int32_t phase_steps;
+    // Speculative kernel: lanes of a warp that hold trajectories (0: all 32).
+    // Small ensembles spread over more warps and SMs with fewer lanes each,
+    // which shortens every trajectory's step latency.
+    int32_t lanes;
 
     // Warp-per-trajectory kernel: [grid * warps per block][R] doubles of
     // scratch for its exact steps.

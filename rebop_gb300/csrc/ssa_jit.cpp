@@ -285,11 +285,12 @@ uint64_t image_key(const std::string &src, Nvrtc *nv) {
 }
 
 // Compiled image of the network's kernel, from the disk cache or NVRTC.
-bool compile_image(const std::string &src, uint64_t key, Nvrtc *nv, std::string &image) {
+bool compile_image(const std::string &src, uint64_t key, Nvrtc *nv, std::string &image, bool compile = true) {
     char hex[17];
     std::snprintf(hex, sizeof hex, "%016llx", (unsigned long long)key);
     const std::string dir = cache_dir(), path = dir + "/net_" + hex + ".cubin";
     if (read_file(path, image)) return true;
+    if (!compile) return false;
     if (!nv) {
         set_error("run-time network compilation unavailable: " + g_nvrtc.why);
         return false;
@@ -334,7 +335,7 @@ bool jit_compile(const Packed &p, int block, size_t *image_bytes) {
     return true;
 }
 
-const void *jit_kernel(const Packed &p, int block) {
+const void *jit_kernel(const Packed &p, int block, bool compile) {
     std::lock_guard<std::mutex> lk(g_mu);
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -348,7 +349,7 @@ const void *jit_kernel(const Packed &p, int block) {
     auto it = g_loaded.find({dev, key});
     if (it != g_loaded.end()) return (const void *)it->second.kern;
     std::string image;
-    if (!compile_image(src, key, nv, image)) return nullptr;
+    if (!compile_image(src, key, nv, image, compile)) return nullptr;
     Loaded l;
     if (cudaLibraryLoadData(&l.lib, image.data(), nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess ||
         cudaLibraryGetKernel(&l.kern, l.lib, "rbg_net_kernel") != cudaSuccess) {

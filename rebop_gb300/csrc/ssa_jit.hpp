@@ -20,8 +20,10 @@ std::string jit_net_source(const Packed &p, int block);
 // loading it; false with the error set on failure.
 bool jit_compile(const Packed &p, int block, size_t *image_bytes);
 // The compiled kernel for the current device (compiled on first use); null
-// with the error set on failure.
-const void *jit_kernel(const Packed &p, int block);
+// with the error set on failure.  With `compile` false only a kernel already
+// loaded or in the disk cache is returned (null, no error, otherwise).  A
+// kernel built for `block` lanes also runs blocks of fewer lanes.
+const void *jit_kernel(const Packed &p, int block, bool compile = true);
 int launch_ssa_jit(const void *kern, const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st);
 
 }  // namespace rbg

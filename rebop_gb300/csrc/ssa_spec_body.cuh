@@ -424,8 +424,9 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
             const DF d = spec_rate_ok(rb) ? df_from_double(__longlong_as_double((long long)rb)) : DF{0.f, 0.f};
             rdf[r] = make_float2(d.h, d.l);
         }
-    // every slot starts live and empty (no trajectory taken yet)
-    for (int k = tid; k < NS; k += BD) stflag[k] = kLive;
+    // every slot a lane may hold starts live and empty (no trajectory taken yet)
+    const int lanes = a.lanes > 0 && a.lanes < 32 ? a.lanes : 32;
+    for (int k = tid; k < NS; k += BD) stflag[k] = (k % SPW) < lanes ? kLive : 0u;
     if (tid < 128) ctr[tid] = 0;
     __syncthreads();
     const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
@@ -441,14 +442,14 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     // ---- this lane's slot; the hot state sits in registers during a phase,
     // the cold words (interval start t0, sample time T, trajectory, event
     // count at the interval start, sample index) stay in the slot's columns
-    int slot = wbase + lane;
+    int slot = lane < lanes ? wbase + lane : -1;
     int32_t *const wlist = slot_list + wbase;
     typename Ops::Counts c{};
     Xoshiro g{0, 0, 0, 0};
     TF Tc{0.f, 0.f, 0.f}, tc{0.f, 0.f, 0.f};  // sample time, clock
     float err_t = 0.f;                         // bound on |clock - reference clock|
     unsigned long long ev = 0;
-    bool live = true, have = false, nat = false, exact_traj = false, begin = false, abort_run = false;
+    bool live = slot >= 0, have = false, nat = false, exact_traj = false, begin = false, abort_run = false;
 
     for (;;) {
         // ---------------------------------------------------------- phase
