@@ -347,8 +347,11 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
             // generated kernels may run larger blocks (fewer registers per lane)
             int kb = 512;
             if (const char *e = std::getenv("RB_JIT_BLOCK")) kb = std::max(32, std::min(1024, std::atoi(e) / 32 * 32));
-            const bool spread = lanes && kb >= 128;  // spread launches run 128 lanes of the same kernel
-            const int jb = spread ? 128 : kb;
+            // spread launches run 128 lanes of a kernel built for 128 (all
+            // registers to the few lanes that hold trajectories)
+            const bool spread = lanes != 0;
+            if (spread) kb = 128;
+            const int jb = kb;
             const int jgrid = spread ? grid
                                      : (int)std::max<int64_t>(1, std::min<int64_t>(ctx->sm_count, (r.n_traj + jb - 1) / jb));
             const int jslots = spread ? 128 : ssa_spec_slots(a, jgrid, ctx->smem_optin, jb);

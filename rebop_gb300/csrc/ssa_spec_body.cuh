@@ -426,7 +426,7 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
         }
     // every slot a lane may hold starts live and empty (no trajectory taken yet)
     const int lanes = a.lanes > 0 && a.lanes < 32 ? a.lanes : 32;
-    for (int k = tid; k < NS; k += BD) stflag[k] = (k % SPW) < lanes ? kLive : 0u;
+    for (int k = tid; k < NS; k += BD) stflag[k] = lanes == 32 || (k % SPW) < lanes ? kLive : 0u;
     if (tid < 128) ctr[tid] = 0;
     __syncthreads();
     const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
