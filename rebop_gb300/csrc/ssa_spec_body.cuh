@@ -153,8 +153,9 @@ __device__ __forceinline__ TF tf_add(TF t, DF q) {
 }
 
 // Exp1 draw as a float pair, consuming the stream exactly as the reference
-// does (the wedge test is decided exactly, see wedge_accept).  xerr bounds
-// |x - rebop's binary64 draw|.
+// does: every accept/reject decision is the binary64 one (the wedge test in
+// float32 outside a margin, exactly inside it).  xerr bounds |x - rebop's
+// binary64 draw|.
 __device__ __forceinline__ DF exp1_df(Xoshiro &g, const ExactTables &ex, const float2 *xdf, float &xerr) {
     for (;;) {
         const uint64_t b = xo_next(g);
@@ -162,21 +163,37 @@ __device__ __forceinline__ DF exp1_df(Xoshiro &g, const ExactTables &ex, const f
         const uint64_t k = b >> 12;
         const ulonglong2 e = ex.zxk[i];
         const float2 X = xdf[i];
+        const DF x = df_mul(df_u53(2 * k + 1), DF{X.x, X.y});
         if (k < e.y) {
             xerr = kGamma * X.x;
-            return df_mul(df_u53(2 * k + 1), DF{X.x, X.y});
+            return x;
         }
         if (i == 0) {
             const double xd = __dsub_rn(kZigR, log(xo_uniform(g)));
-            const DF x = df_from_double(xd);
-            xerr = kGamma * x.h;
-            return x;
+            const DF t = df_from_double(xd);
+            xerr = kGamma * t.h;
+            return t;
         }
-        bool bad = false;
-        const uint64_t xb = b64::mul_u64(e.x, 2 * k + 1, 53, bad);
-        if (wedge_accept(ex, i, xb, xo_next(g) >> 11, bad)) {
+        // Wedge test f[i+1] - |f[i] - f[i+1]| U < exp(-x), first in float32:
+        // the float copies of the tables and U are within 2^-23 (2^-20.2 of
+        // the left side at the steepest layer, f[2]/f[1] < 2.2), x.h within
+        // 2^-24 x (x < 7.7: 2^-21 on exp(-x)) and expf within 2 ulp, so a
+        // side more than 2^-17 apart decides as binary64 would; inside that
+        // band the exact operands decide.
+        const uint64_t mu = xo_next(g) >> 11;
+        const float u = __fmul_rn(f23((uint32_t)(mu >> 30)), 0x1p-23f);
+        const float wf = __fmaf_rn(-f32_rz(ex.zd[i]), u, f32_rz(ex.zf[i + 1]));
+        const float ef = expf(-x.h);
+        bool acc;
+        if (wf < __fmul_rn(ef, 1.0f - 0x1p-17f)) acc = true;
+        else if (wf > __fmul_rn(ef, 1.0f + 0x1p-17f)) acc = false;
+        else {
+            bool bad = false;
+            acc = wedge_accept(ex, i, b64::mul_u64(e.x, 2 * k + 1, 53, bad), mu, bad);
+        }
+        if (acc) {
             xerr = kGamma * X.x;
-            return df_from_double(__longlong_as_double((long long)xb));
+            return x;
         }
     }
 }
