@@ -152,50 +152,65 @@ __device__ __forceinline__ TF tf_add(TF t, DF q) {
     return TF{h, __fsub_rn(m2, __fsub_rn(h, s)), l};
 }
 
+// Wedge test of the ziggurat, f[i+1] - |f[i] - f[i+1]| U < exp(-x), for the
+// candidate x = X_i (2k + 1) 2^-53 (xh its float within 2^-24 x) and U = mu
+// 2^-53.  First in float32: the float copies of the tables and U are within
+// 2^-23 (2^-20.2 of the left side at the steepest layer, f[2]/f[1] < 2.2),
+// xh within 2^-24 x (x < 7.7: 2^-21 on exp(-x)) and expf within 2 ulp, so a
+// side more than 2^-17 apart decides as binary64 would; inside that band the
+// exact operands decide (wedge_accept).
+__device__ __forceinline__ bool wedge_df(const ExactTables &ex, int i, uint64_t k, float xh, uint64_t mu) {
+    const float u = __fmul_rn(f23((uint32_t)(mu >> 30)), 0x1p-23f);
+    const float wf = __fmaf_rn(-f32_rz(ex.zd[i]), u, f32_rz(ex.zf[i + 1]));
+    const float ef = expf(-xh);
+    if (wf < __fmul_rn(ef, 1.0f - 0x1p-17f)) return true;
+    if (wf > __fmul_rn(ef, 1.0f + 0x1p-17f)) return false;
+    bool bad = false;
+    return wedge_accept(ex, i, b64::mul_u64(ex.zxk[i].x, 2 * k + 1, 53, bad), mu, bad);
+}
+
 // Exp1 draw as a float pair, consuming the stream exactly as the reference
-// does: every accept/reject decision is the binary64 one (the wedge test in
-// float32 outside a margin, exactly inside it).  xerr bounds |x - rebop's
-// binary64 draw|.
+// does: every accept/reject decision is the binary64 one.  xerr bounds
+// |x - rebop's binary64 draw|.
 __device__ __forceinline__ DF exp1_df(Xoshiro &g, const ExactTables &ex, const float2 *xdf, float &xerr) {
     for (;;) {
         const uint64_t b = xo_next(g);
         const int i = (int)(b & 0xff);
         const uint64_t k = b >> 12;
-        const ulonglong2 e = ex.zxk[i];
         const float2 X = xdf[i];
         const DF x = df_mul(df_u53(2 * k + 1), DF{X.x, X.y});
-        if (k < e.y) {
+        if (k < ex.zxk[i].y) {
             xerr = kGamma * X.x;
             return x;
         }
         if (i == 0) {
-            const double xd = __dsub_rn(kZigR, log(xo_uniform(g)));
-            const DF t = df_from_double(xd);
+            const DF t = df_from_double(__dsub_rn(kZigR, log(xo_uniform(g))));
             xerr = kGamma * t.h;
             return t;
         }
-        // Wedge test f[i+1] - |f[i] - f[i+1]| U < exp(-x), first in float32:
-        // the float copies of the tables and U are within 2^-23 (2^-20.2 of
-        // the left side at the steepest layer, f[2]/f[1] < 2.2), x.h within
-        // 2^-24 x (x < 7.7: 2^-21 on exp(-x)) and expf within 2 ulp, so a
-        // side more than 2^-17 apart decides as binary64 would; inside that
-        // band the exact operands decide.
-        const uint64_t mu = xo_next(g) >> 11;
-        const float u = __fmul_rn(f23((uint32_t)(mu >> 30)), 0x1p-23f);
-        const float wf = __fmaf_rn(-f32_rz(ex.zd[i]), u, f32_rz(ex.zf[i + 1]));
-        const float ef = expf(-x.h);
-        bool acc;
-        if (wf < __fmul_rn(ef, 1.0f - 0x1p-17f)) acc = true;
-        else if (wf > __fmul_rn(ef, 1.0f + 0x1p-17f)) acc = false;
-        else {
-            bool bad = false;
-            acc = wedge_accept(ex, i, b64::mul_u64(e.x, 2 * k + 1, 53, bad), mu, bad);
-        }
-        if (acc) {
+        if (wedge_df(ex, i, k, x.h, xo_next(g) >> 11)) {
             xerr = kGamma * X.x;
             return x;
         }
     }
+}
+
+// Exp1 draw whose first candidate (draw b, float pair x) failed the fast
+// test, when the next draw b2 is already taken (g is past it): b2 is the
+// wedge's or the tail's uniform, as in the reference.
+__device__ __forceinline__ DF exp1_df_cont(Xoshiro &g, uint64_t b, uint64_t b2, DF x, const ExactTables &ex,
+                                           const float2 *xdf, float &xerr) {
+    const int i = (int)(b & 0xff);
+    if (i == 0) {
+        const DF t = df_from_double(__dsub_rn(kZigR, log(uniform53(b2))));
+        xerr = kGamma * t.h;
+        return t;
+    }
+    if (wedge_df(ex, i, b >> 12, x.h, b2 >> 11)) {
+        xerr = kGamma * xdf[i].x;
+        return x;
+    }
+    return exp1_df(g, ex, xdf, xerr);
 }
 
 // Rate in the float-pair range (0, or 2^-60 .. 2^60), also inside the exact
@@ -574,11 +589,10 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                     uint64_t bu = b2;
                     if (tot.h > 0.0f) {
                         if (slow) {
-                            // ziggurat rejection or tail: redo the draws in order
-                            Xoshiro gs = g;
-                            x = exp1_df(gs, ex, xdf, xerr);
-                            bu = xo_next(gs);
-                            g2 = gs;
+                            // wedge or tail: b2 was its uniform, the choice
+                            // takes the draw after the Exp1 is settled
+                            x = exp1_df_cont(g2, b1, b2, x, ex, xdf, xerr);
+                            bu = xo_next(g2);
                         }
                         amb |= tot.h < 0x1p-90f || tot.h > 0x1p90f;
                         const float r = rcp_approx(tot.h);
