@@ -222,6 +222,7 @@ std::string jit_net_source(const Packed &p, int block) {
     // (a jump moves it by less than 2^23, so floats stay exact in between)
     o << "    __device__ static bool props(const SsaArgs &, const ExactTables &, const Counts &c, const int64_t *, int,\n"
          "                                 const float2 *rf, int RS, float *cum, DF &tot) {\n";
+    o << "        RunSum sum;\n";
     o << "        float lo = c.n[0], hi = c.n[0];\n";
     for (int s = 1; s < S; s++) o << "        lo = fminf(lo, c.n[" << s << "]); hi = fmaxf(hi, c.n[" << s << "]);\n";
     for (int r = 0; r < R; r++) {
@@ -238,11 +239,12 @@ std::string jit_net_source(const Packed &p, int block) {
             }
         }
         if (r == 0)
-            o << "            tot = acc;\n";
+            o << "            sum = RunSum{acc.h, acc.l};\n";
         else
-            o << "            tot = df_add(tot, acc);\n";
-        o << "            cum[" << r << "] = tot.h;\n        }\n";
+            o << "            rs_add(sum, acc);\n";
+        o << "            cum[" << r << "] = sum.s;\n        }\n";
     }
+    o << "        tot = rs_total(sum);\n";
     o << "        return !(lo >= 0.0f && hi < 8388608.0f);\n    }\n";
     o << "    __device__ static int exact_choice(const SsaArgs &, const ExactTables &, const Counts &c, const int64_t "
          "*, int,\n                                       const uint64_t *rl, int RS, uint64_t u53) {\n";

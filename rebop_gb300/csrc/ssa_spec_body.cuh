@@ -7,14 +7,15 @@
 // The random stream consumed follows from those decisions too.  And at every
 // sample time the clock is reset to T exactly (gillespie.rs:328-330).
 //
-// So each step here evaluates propensities and their running sum in float
-// pairs (hi + lo, about 46 bits), the clock as a float triple, Exp1/total in
-// float pairs and the choice in float32, all on the FP32 and integer pipes,
+// So each step here evaluates propensities and their total in float pairs
+// (hi + lo, about 46 bits), the clock as a float triple, Exp1/total in float
+// pairs and the choice in float32, all on the FP32 and integer pipes,
 // together with a bound on the distance of every quantity from the value
 // rebop's binary64 arithmetic produces.  A decision whose operands lie farther
 // apart than their bounds is the reference's decision:
-//   * a float32 choice comparison inside its margin (2^-21 of the total) is
-//     redone in binary64 for that step alone (Ops::exact_choice);
+//   * a float32 choice comparison inside its margin ((R + M + 6) 2^-24 of
+//     the total) is redone in binary64 for that step alone
+//     (Ops::exact_choice);
 //   * a clock comparison inside its margin, a count outside [0, 2^23) or a
 //     total outside 2^-90 .. 2^90 makes the lane restore the state it saved at
 //     the start of the sample interval and re-run that interval with the exact
@@ -26,7 +27,9 @@
 // binary64 rounding of the same operation) moves a value by at most
 // gamma = 2^-44 relative (the float-pair errors are near 2^-46, binary64's
 // 2^-53).  With M reactant factors per reaction at most and R reactions, the
-// total is within G = (M + R + 2) gamma of the reference's and Exp1/total
+// total (a float32 running sum of the high parts plus a float32 sum of the
+// two-sum errors and low parts) is within G = (M + R + 2 + (R (R + 1) / 2 +
+// R (M + 2)) / 16) gamma of the reference's and Exp1/total
 // within (G + 6 gamma) q plus the Exp1 abscissa's absolute error over the
 // total.  The triple-float clock add is exact up to its low part's rounding,
 // and the reference's own rounding of t + q adds at most 2^-53 (t + q): the
@@ -85,6 +88,25 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
     e = __fadd_rn(e, __fadd_rn(a.l, b.l));
     return fast2sum(s, e);
 }
+
+// Running sum of non-negative float pairs: s is the float32 running sum of the
+// high parts, e collects the two-sum errors and the low parts, so s + e is
+// the pair.  After r terms of at most M factors each, s is within
+// (r + M + 2) 2^-24 of the exact running sum (a rate's low part is below
+// 2^-23 of its high part, each factor adds 2^-24; one rounding per add).
+struct RunSum {
+    float s, e;
+};
+
+__device__ __forceinline__ void rs_add(RunSum &a, DF b) {
+    const float s = __fadd_rn(a.s, b.h);
+    const float bb = __fsub_rn(s, a.s);
+    const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    a.e = __fadd_rn(a.e, __fadd_rn(err, b.l));
+    a.s = s;
+}
+
+__device__ __forceinline__ DF rs_total(RunSum a) { return fast2sum(a.s, a.e); }
 
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;
@@ -359,7 +381,7 @@ struct TableOps {
     __device__ static bool props(const SsaArgs &a, const ExactTables &ex, const Counts &, const int64_t *sp,
                                  int NS, const float2 *rf, int RS, float *cum, DF &tot) {
         bool amb = false;
-        tot = DF{0.f, 0.f};
+        RunSum sum{0.f, 0.f};
 #pragma unroll
         for (int r = 0; r < MAXR; ++r) {
             if (r < a.R) {
@@ -380,10 +402,11 @@ struct TableOps {
                         acc = df_mul_fu(acc, f23((uint32_t)x & 0x7FFFFFu));
                     }
                 }
-                tot = df_add(tot, acc);
-                cum[r] = tot.h;
+                rs_add(sum, acc);
+                cum[r] = sum.s;
             }
         }
+        tot = rs_total(sum);
         return amb;
     }
     // The reference's choice for this state and uniform draw, in binary64.
@@ -463,9 +486,16 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     __syncthreads();
     const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
 
-    const float G = (float)(a.max_mults + R + 2) * kGamma;  // running-sum bound
+    // running-sum bound: the products and the reference's own roundings
+    // (M + R + 2 gamma), plus the float32 accumulation of the low parts,
+    // (r + M + 2) 2^-48 of the total at add r (1/16 gamma each)
+    const float G = ((float)(a.max_mults + R + 2) +
+                     (float)(R * (R + 1) / 2 + R * (a.max_mults + 2)) * 0.0625f) * kGamma;
     const float c_q = G + 6.0f * kGamma;                     // relative bound of Exp1/total
-    const float c_sel = 0x1p-21f;                            // float32 choice margin / total
+    // float32 choice margin / total: running sums within (R + M + 2) 2^-24,
+    // U truncated to 2^-23, the product rounded (2^-24), the total's high
+    // part within 2^-24
+    const float c_sel = (float)(a.max_mults + R + 6) * 0x1p-24f * 1.001f;
     const int64_t t_start = global_ns();
     const int phase_steps = a.phase_steps > 0 ? a.phase_steps : kSpecPhase;
     unsigned int tick = 0, rot = 0;
