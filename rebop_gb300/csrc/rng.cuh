@@ -54,6 +54,19 @@ __device__ __forceinline__ uint64_t xo_next(Xoshiro &g) {
     return out;
 }
 
+// The state before the last xo_next: the update is invertible; s1 ^ s2 after
+// it is b ^ (b << 17) of the old s1 = b, undone by three more shifts.
+__device__ __forceinline__ void xo_prev(Xoshiro &g) {
+    const uint64_t d1 = rotl64(g.s3, 19);
+    const uint64_t y = g.s1 ^ g.s2;
+    const uint64_t b = y ^ (y << 17) ^ (y << 34) ^ (y << 51);
+    const uint64_t a = g.s0 ^ d1;
+    g.s2 = g.s1 ^ b ^ a;
+    g.s0 = a;
+    g.s1 = b;
+    g.s3 = d1 ^ b;
+}
+
 // k * 2^-53 for the top 53 bits k of a draw (exact: k < 2^53).
 __device__ __forceinline__ double uniform53(uint64_t bits) {
     return __dmul_rn((double)(bits >> 11), 0x1.0p-53);

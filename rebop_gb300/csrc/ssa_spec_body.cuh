@@ -598,14 +598,13 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                 int idx = 0;
                 if (!replay) {
                     // Float-pair step.  Both draws the step may make are taken
-                    // ahead from a copy of the generator (the reference draws
-                    // Exp1 only when total > 0 and the uniform only when the
-                    // reaction fires), so they overlap the propensities; the
-                    // generator moves on only by the draws the step commits.
-                    // An undecided step re-runs the interval from its saved state.
-                    Xoshiro g2 = g;
-                    const uint64_t b1 = xo_next(g2);
-                    const uint64_t b2 = xo_next(g2);
+                    // ahead (the reference draws Exp1 only when total > 0 and
+                    // the uniform only when the reaction fires), so they
+                    // overlap the propensities; a step that commits fewer
+                    // draws steps the generator back.  An undecided step
+                    // re-runs the interval from its saved state.
+                    const uint64_t b1 = xo_next(g);
+                    const uint64_t b2 = xo_next(g);
                     const int i1 = (int)(b1 & 0xff);
                     const uint64_t k1 = b1 >> 12;
                     const uint64_t K1 = ex.zxk[i1].y;
@@ -621,8 +620,8 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                         if (slow) {
                             // wedge or tail: b2 was its uniform, the choice
                             // takes the draw after the Exp1 is settled
-                            x = exp1_df_cont(g2, b1, b2, x, ex, xdf, xerr);
-                            bu = xo_next(g2);
+                            x = exp1_df_cont(g, b1, b2, x, ex, xdf, xerr);
+                            bu = xo_next(g);
                         }
                         amb |= tot.h < 0x1p-90f || tot.h > 0x1p90f;
                         const float r = rcp_approx(tot.h);
@@ -661,15 +660,17 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                         if (!amb) {
                             if (fire) {
                                 if (close) idx = Ops::exact_choice(a, ex, c, sp, NS, rl, RS, bu >> 11);
-                                g = g2;
                                 tc = tn;
                                 err_t = err_tn;
                             } else {
                                 // the sample records: the Exp1 draw alone was made
-                                if (slow) exp1_df(g, ex, xdf, xerr);
-                                else xo_next(g);
+                                xo_prev(g);
                             }
                         }
+                    } else {
+                        // no reaction can fire: no draw is made
+                        xo_prev(g);
+                        xo_prev(g);
                     }
                     replay = amb;
                 }
