@@ -13,7 +13,7 @@
 // together with a bound on the distance of every quantity from the value
 // rebop's binary64 arithmetic produces.  A decision whose operands lie farther
 // apart than their bounds is the reference's decision:
-//   * a float32 choice comparison inside its margin ((R + M + 8) 2^-24 of
+//   * a float32 choice comparison inside its margin ((R + M + 6) 2^-24 of
 //     the total) is redone in binary64 for that step alone
 //     (Ops::exact_choice);
 //   * a clock comparison inside its margin, a count outside [0, 2^23) or a
@@ -48,10 +48,6 @@ namespace rbg {
 extern __shared__ __align__(16) unsigned char g_spec_smem[];
 
 constexpr float kGamma = 0x1p-44f;
-// Bound on |Exp1 draw - rebop's binary64 draw| per unit of the layer's
-// abscissa X[i] (or of the tail draw): gamma, with a 1.001 margin that also
-// covers the reciprocal's error when the bound is divided by the total.
-constexpr float kXerr = kGamma * 1.001f;
 
 struct DF {
     float h, l;
@@ -206,16 +202,16 @@ __device__ __forceinline__ DF exp1_df(Xoshiro &g, const ExactTables &ex, const f
         const float2 X = xdf[i];
         const DF x = df_mul(df_u53(2 * k + 1), DF{X.x, X.y});
         if (k < ex.zxk[i].y) {
-            xerr = kXerr * X.x;
+            xerr = kGamma * X.x;
             return x;
         }
         if (i == 0) {
             const DF t = df_from_double(__dsub_rn(kZigR, log(xo_uniform(g))));
-            xerr = kXerr * t.h;
+            xerr = kGamma * t.h;
             return t;
         }
         if (wedge_df(ex, i, k, x.h, xo_next(g) >> 11)) {
-            xerr = kXerr * X.x;
+            xerr = kGamma * X.x;
             return x;
         }
     }
@@ -229,11 +225,11 @@ __device__ __forceinline__ DF exp1_df_cont(Xoshiro &g, uint64_t b, uint64_t b2, 
     const int i = (int)(b & 0xff);
     if (i == 0) {
         const DF t = df_from_double(__dsub_rn(kZigR, log(uniform53(b2))));
-        xerr = kXerr * t.h;
+        xerr = kGamma * t.h;
         return t;
     }
     if (wedge_df(ex, i, b >> 12, x.h, b2 >> 11)) {
-        xerr = kXerr * xdf[i].x;
+        xerr = kGamma * xdf[i].x;
         return x;
     }
     return exp1_df(g, ex, xdf, xerr);
@@ -498,8 +494,8 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     const float c_q = G + 6.0f * kGamma;                     // relative bound of Exp1/total
     // float32 choice margin / total: running sums within (R + M + 2) 2^-24,
     // U truncated to 2^-23, the product rounded (2^-24), the total's high
-    // part within 2^-24, ch -+ margin rounded (2^-23)
-    const float c_sel = (float)(a.max_mults + R + 8) * 0x1p-24f * 1.001f;
+    // part within 2^-24
+    const float c_sel = (float)(a.max_mults + R + 6) * 0x1p-24f * 1.001f;
     const int64_t t_start = global_ns();
     const int phase_steps = a.phase_steps > 0 ? a.phase_steps : kSpecPhase;
     unsigned int tick = 0, rot = 0;
@@ -614,7 +610,7 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                     const uint64_t K1 = ex.zxk[i1].y;
                     const float2 X1 = xdf[i1];
                     DF x = df_mul(df_u53(2 * k1 + 1), DF{X1.x, X1.y});
-                    float xerr = kXerr * X1.x;
+                    float xerr = kGamma * X1.x;
                     float cum[MAXR];
                     DF tot;
                     bool amb = Ops::props(a, ex, c, sp, NS, rf, RS, cum, tot);
@@ -632,37 +628,35 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                         const DF q = df_div(x, tot, r);
                         const TF tn = tf_add(tc, q);
                         // error bound, rounded up: previous bound, Exp1/total
-                        // against the reference's quotient (c_q q, and the
-                        // draw's error over the total), the reference's
+                        // against the reference's quotient, the reference's
                         // rounding of its clock add, the low part's roundings
-                        const float e_q = __fmaf_ru(c_q, q.h, __fmul_ru(xerr, r));
-                        const float e_t = __fmaf_ru(0x1p-52f, tn.h, __fmul_ru(0x1p-23f, fabsf(tn.l)));
-                        const float err_tn = __fadd_ru(__fadd_ru(err_t, e_q), e_t);
+                        float err_tn = __fadd_ru(err_t, __fmul_ru(c_q, q.h));
+                        err_tn = __fadd_ru(err_tn, __fmul_ru(__fmul_ru(xerr, r), 1.001f));
+                        err_tn = __fadd_ru(err_tn, __fmul_ru(0x1p-52f, tn.h));
+                        err_tn = __fadd_ru(err_tn, __fmul_ru(0x1p-23f, fabsf(tn.l)));
                         // T - tn: the high difference is exact near T, the
                         // rest is below 2^-46 max(T, tn) off
                         const float d = __fadd_rn(__fsub_rn(Tc.h, tn.h),
                                                   __fadd_rn(__fsub_rn(Tc.m, tn.m), __fsub_rn(Tc.l, tn.l)));
-                        const float mt = __fmaf_ru(0x1p-44f, fmaxf(Tc.h, tn.h), err_tn);
+                        const float mt = __fadd_ru(err_tn, __fmul_ru(0x1p-44f, fmaxf(Tc.h, tn.h)));
                         const float dd = __fmul_rn(d, 1.0f - 0x1p-22f);
                         fire = dd > mt;
                         amb |= !(fire || dd < -mt) || !(err_tn < 1.0e30f) || q.h < 0x1p-100f;
-                        // choice #{r : cum_r < total * U} in float32: the
-                        // running sums are nondecreasing, so with none of them
-                        // in [ch - msel, ch + msel] the count below ch - msel
-                        // is the reference's choice; otherwise a comparison
-                        // inside the margin is redone exactly in binary64
+                        // choice #{r : cum_r < total * U} in float32: the high
+                        // parts are within 2^-23.9 of the exact sums, U and the
+                        // product add 2^-23 each; a comparison inside that
+                        // margin is redone exactly in binary64
                         const float ch = __fmul_rn(tot.h, f23((uint32_t)(bu >> 41)) * 0x1p-23f);
                         const float msel = c_sel * tot.h;
-                        const float lo_t = __fsub_rn(ch, msel), hi_t = __fadd_rn(ch, msel);
-                        int hi = 0;
+                        bool close = false;
 #pragma unroll
                         for (int rr = 0; rr < MAXR; ++rr) {
                             if (rr < R) {
-                                idx += cum[rr] < lo_t ? 1 : 0;
-                                hi += cum[rr] <= hi_t ? 1 : 0;
+                                const float dr = __fsub_rn(cum[rr], ch);
+                                idx += dr < 0.0f ? 1 : 0;
+                                close |= fabsf(dr) <= msel;
                             }
                         }
-                        const bool close = idx != hi;
                         if (!amb) {
                             if (fire) {
                                 if (close) idx = Ops::exact_choice(a, ex, c, sp, NS, rl, RS, bu >> 11);
