@@ -3,6 +3,7 @@
 
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <random>
 
@@ -327,6 +328,17 @@ int rb_network_reaction_rate(const rb_network *net, int32_t r, double *rate) {
 }
 
 // ---------------------------------------------------------------- ensemble
+// Device address of a page-locked host buffer, or null for any other memory.
+static void *mapped_host(void *h) {
+    if (!h) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, int32_t x0_per_traj,
                     const double *rates, int32_t rates_per_traj, const uint64_t *seeds, double tmax,
                     int64_t nb_steps, const int32_t *save_idx, int32_t n_save, int64_t *out, double *times,
@@ -379,29 +391,42 @@ int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, i
     r.n_samples = (int64_t)NT;
     r.save_idx = reinterpret_cast<int32_t *>(b + o_save);
     r.n_save = (int32_t)NS;
-    r.out = reinterpret_cast<int64_t *>(b + o_out);
-    r.events = reinterpret_cast<uint64_t *>(b + o_ev);
+    // Page-locked result buffers can be written by the kernel itself, over
+    // the host link, while it runs.  That pays when the samples trickle out
+    // (a few GB/s at most: the kernel's scattered 8-byte stores then cost
+    // nothing), while a launch that writes faster runs better against device
+    // memory and one copy back at the end; the network's previous run
+    // decides (RB_ZERO_COPY=1 always, 0 never).
+    const char *zc = std::getenv("RB_ZERO_COPY");
+    const bool zero_copy = zc ? std::strcmp(zc, "0") != 0 : dn.out_gbs > 0 && dn.out_gbs < 4.0;
+    int64_t *out_host = zero_copy ? static_cast<int64_t *>(mapped_host(out)) : nullptr;
+    uint64_t *ev_host = zero_copy ? static_cast<uint64_t *>(mapped_host(events)) : nullptr;
+    r.out = out_host ? out_host : reinterpret_cast<int64_t *>(b + o_out);
+    r.events = ev_host ? ev_host : reinterpret_cast<uint64_t *>(b + o_ev);
     r.fin_species = final_species ? reinterpret_cast<int64_t *>(b + o_fin) : nullptr;
     r.times_ok = std::isfinite(tmax) && tmax >= 0;
     r.t_last = tmax;
     int mapping = 0;
     if (!rbg::launch_sampled(net, dn, r, dn.stream, true, &mapping)) return RB_ERR_CUDA;
+    if (out_host) d2h += NT * NS * N * 8;
+    if (ev_host) d2h += N * 8;
     auto d2h_copy = [&](void *dst, size_t off, size_t bytes) {
         if (!bytes || !dst) return true;
         d2h += bytes;
         return cuda_check(cudaMemcpyAsync(dst, b + off, bytes, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync");
     };
     unsigned long long sc[3] = {0, 0, 0};  // total events, timeout flag, exact re-runs
-    if (!d2h_copy(out, o_out, NT * NS * N * 8) || !d2h_copy(events, o_ev, N * 8) ||
+    if ((!out_host && !d2h_copy(out, o_out, NT * NS * N * 8)) || (!ev_host && !d2h_copy(events, o_ev, N * 8)) ||
         !d2h_copy(final_species, o_fin, final_species ? N * S * 8 : 0) ||
         !cuda_check(cudaMemcpyAsync(sc, dn.scratch + 1, 24, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync") ||
         !cuda_check(cudaStreamSynchronize(dn.stream), "ssa_thread_kernel"))
         return RB_ERR_CUDA;
     if (sc[1]) return fail(RB_ERR_TIMEOUT, "ensemble run ran out of its time budget (RB_KERNEL_BUDGET_S)");
     const uint64_t total_events = sc[0];
+    float ms = 0.f;
+    if (N) cudaEventElapsedTime(&ms, dn.ev_start, dn.ev_stop);
+    if (ms > 0.f) dn.out_gbs = (double)(NT * NS * N * 8) / ((double)ms * 1e6);
     if (stats) {
-        float ms = 0.f;
-        if (N) cudaEventElapsedTime(&ms, dn.ev_start, dn.ev_stop);
         stats->events = total_events;
         stats->kernel_ms = ms;
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();

@@ -356,7 +356,16 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
                                      : (int)std::max<int64_t>(1, std::min<int64_t>(ctx->sm_count, (r.n_traj + jb - 1) / jb));
             const int jslots = spread ? 128 : ssa_spec_slots(a, jgrid, ctx->smem_optin, jb);
             if (jslots > 0) {
-                jk = jit_kernel(p, kb, compile);
+                if (dn.jit_k && dn.jit_block == kb && dn.jit_version == dn.version) {
+                    jk = dn.jit_k;
+                } else {
+                    jk = jit_kernel(p, kb, compile);
+                    if (jk) {
+                        dn.jit_k = jk;
+                        dn.jit_block = kb;
+                        dn.jit_version = dn.version;
+                    }
+                }
                 if (!jk && jit && std::strcmp(jit, "1") == 0) return false;
                 if (jk) {
                     block = jb;

@@ -53,6 +53,10 @@ struct DeviceNet {
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaStream_t last_stream = nullptr; // stream of the last device-pointer run
     int64_t runs = 0;                   // sampled launches of this network
+    double out_gbs = 0;                 // sample bytes / kernel time of the last host-pointer run
+    const void *jit_k = nullptr;        // generated kernel last used, for
+    int jit_block = 0;                  //   blocks of jit_block lanes and
+    uint64_t jit_version = 0;           //   descriptor version jit_version
     ~DeviceNet();
 };
 

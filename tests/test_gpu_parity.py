@@ -260,6 +260,27 @@ def test_device_entry_point_matches_host_entry_point(rb, O):
     assert total == tot
 
 
+def test_page_locked_results_written_in_place(rb, O):
+    # Page-locked result buffers written by the kernel directly (no staging
+    # copy): the results and the byte counts match the staged path.
+    torch = pytest.importorskip("torch")
+    net = _dimer(rb)
+    n = 1234
+    seeds = _seeds(n, 8)
+    pin_out = torch.empty((21, 4, n), dtype=torch.int64, pin_memory=True).numpy()
+    pin_ev = torch.empty(n, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    pin_out[...] = -7
+    res = _with_env("RB_ZERO_COPY", "1",
+                    lambda: net.run_ensemble([1, 0, 0, 0], seeds, 0.5, 20, out=pin_out, events=pin_ev))
+    ref, ev, tot, _ = O.dimer_net().run_ensemble([1, 0, 0, 0], seeds, 0.5, 20)
+    np.testing.assert_array_equal(pin_out, ref)
+    np.testing.assert_array_equal(pin_ev, ev)
+    assert res.total_events == tot
+    staged = _with_env("RB_ZERO_COPY", "0", lambda: net.run_ensemble([1, 0, 0, 0], seeds, 0.5, 20))
+    np.testing.assert_array_equal(staged.counts, ref)
+    assert res.stats["d2h_bytes"] == staged.stats["d2h_bytes"]
+
+
 def _with_kernel(kind, fn):
     import os
 
