@@ -101,6 +101,7 @@ DeviceNet::~DeviceNet() {
     if (desc) cudaFree(desc);
     if (scratch) cudaFree(scratch);
     if (warp_scratch) cudaFree(warp_scratch);
+    if (dep) cudaFree(dep);
     if (io) cudaFree(io);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_stop) cudaEventDestroy(ev_stop);
@@ -108,6 +109,35 @@ DeviceNet::~DeviceNet() {
 }
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+bool warp_dep_lists(const Packed &p, std::vector<int32_t> &off, std::vector<int32_t> &pos) {
+    const int R = p.R, P = p.P, Q = p.Q;
+    const int C = (R + 31) / 32;
+    off.assign(1, 0);
+    pos.clear();
+    if (R < 1 || C > 256) return false;
+    // reactions reading each species
+    std::vector<std::vector<int32_t>> readers((size_t)p.S);
+    for (int r = 0; r < R; r++)
+        for (int k = 0; k < P; k++)
+            if (p.fac_ord[(size_t)r * P + k] > 0) {
+                auto &v = readers[(size_t)p.fac_sp[(size_t)r * P + k]];
+                if (v.empty() || v.back() != r) v.push_back(r);
+            }
+    std::vector<int32_t> mark((size_t)R, -1);
+    for (int j = 0; j < R; j++) {
+        for (int k = 0; k < Q; k++) {
+            if (p.jmp_d[(size_t)j * Q + k] == 0) continue;
+            for (int32_t r : readers[(size_t)p.jmp_sp[(size_t)j * Q + k]])
+                if (mark[(size_t)r] != j) {
+                    mark[(size_t)r] = j;
+                    pos.push_back((r % C) * 32 + r / C);
+                }
+        }
+        off.push_back((int32_t)pos.size());
+    }
+    return true;
+}
 
 bool ensure_device(const Network &net) {
     DeviceCtx *ctx = device_ctx();
@@ -299,6 +329,31 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
             dn.warp_scratch_bytes = need;
         }
         a.warp_scratch = dn.warp_scratch;
+        // dependency lists: only the propensities a reaction's jump touches
+        // are re-evaluated after it fires (RB_WARP_DEPS=0: all, every step)
+        if (dn.dep_version != dn.version) {
+            if (dn.dep) cudaFree(dn.dep);
+            dn.dep = nullptr;
+            std::vector<int32_t> off, pos;
+            dn.dep_ok = warp_dep_lists(p, off, pos);
+            if (dn.dep_ok) {
+                const size_t bytes = sizeof(int32_t) * (off.size() + std::max<size_t>(pos.size(), 1));
+                if (!cuda_ok(cudaMalloc(&dn.dep, bytes), "cudaMalloc(dependency lists)") ||
+                    !cuda_ok(cudaMemcpy(dn.dep, off.data(), sizeof(int32_t) * off.size(), cudaMemcpyHostToDevice),
+                             "cudaMemcpy(dependency lists)") ||
+                    (!pos.empty() &&
+                     !cuda_ok(cudaMemcpy(dn.dep + off.size(), pos.data(), sizeof(int32_t) * pos.size(),
+                                         cudaMemcpyHostToDevice),
+                              "cudaMemcpy(dependency lists)")))
+                    return false;
+            }
+            dn.dep_version = dn.version;
+        }
+        const char *wd = std::getenv("RB_WARP_DEPS");
+        if (dn.dep_ok && !(wd && std::strcmp(wd, "0") == 0)) {
+            a.dep_off = dn.dep;
+            a.dep_pos = dn.dep + p.R + 1;
+        }
         if (timed && !cuda_ok(cudaEventRecord(dn.ev_start, stream), "cudaEventRecord")) return false;
         const int err = launch_ssa_warp(a, warp_w, (int)blocks, smem, stream);
         if (err != 0) return cuda_ok((cudaError_t)err, "SSA kernel launch");

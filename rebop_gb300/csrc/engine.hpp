@@ -54,11 +54,21 @@ struct DeviceNet {
     cudaStream_t last_stream = nullptr; // stream of the last device-pointer run
     int64_t runs = 0;                   // sampled launches of this network
     double out_gbs = 0;                 // sample bytes / kernel time of the last host-pointer run
+    int32_t *dep = nullptr;             // warp kernel dependency lists: offsets, then positions
+    uint64_t dep_version = 0;           //   for this descriptor version (0: none built)
+    bool dep_ok = false;                //   false: the network is beyond the lists' reach
     const void *jit_k = nullptr;        // generated kernel last used, for
     int jit_block = 0;                  //   blocks of jit_block lanes and
     uint64_t jit_version = 0;           //   descriptor version jit_version
     ~DeviceNet();
 };
+
+// Dependency lists of the warp kernel for a packed network: off gets R + 1
+// offsets into pos, which holds the lane-major positions (reaction l*C + i at
+// i*32 + l, C = ceil(R / 32)) of the reactions whose propensity reads a
+// species the reaction changes.  False when the kernel's update groups cannot
+// cover the network (more than 8192 reactions).
+bool warp_dep_lists(const Packed &p, std::vector<int32_t> &off, std::vector<int32_t> &pos);
 
 // Make net.dev current for the active device and descriptor version.
 // Caller holds net.mu.  Returns false (error set) on failure.

@@ -87,6 +87,13 @@ struct SsaArgs {
     // Warp-per-trajectory kernel: [grid * warps per block][R] doubles of
     // scratch for its exact steps.
     double *warp_scratch;
+    // Warp-per-trajectory kernel, one network: for each reaction j, the
+    // lane-major positions (see batch below) of the reactions whose
+    // propensity reads a species that j changes, dep_pos[dep_off[j] ..
+    // dep_off[j+1]).  After j fires only those are re-evaluated.  Null: every
+    // propensity is re-evaluated at every step.
+    const int32_t *dep_off;
+    const int32_t *dep_pos;
 
     // Warp kernel over a batch of networks (batch != null): item k is
     // batch[k], its trajectories are the tickets batch_start[k] ..

@@ -42,6 +42,11 @@ struct WarpLayout {
 // i*32 + l -- so one step of the walk touches 32 consecutive words.
 __host__ __device__ inline int warp_chunk(int R) { return (R + 31) / 32; }
 
+// A lane's chunk is summed in groups of warp_group(C) reactions (at most 32
+// groups), so that re-evaluating a few propensities re-sums only their groups.
+__host__ __device__ inline int warp_group(int C) { return C > 256 ? (C + 31) / 32 : 8; }
+__host__ __device__ inline int warp_ngroups(int C) { return (C + warp_group(C) - 1) / warp_group(C); }
+
 // Shared memory: block tables (Exp1 tables, float-pair rates when shared,
 // reactant factors in both layouts, jumps), then per warp: counts, counts at
 // the interval start, float-pair propensities (and float-pair rates when per
@@ -62,6 +67,7 @@ __host__ __device__ inline WarpLayout warp_layout(const SsaArgs &a) {
     w += 4 * ((size_t)a.S + 1);                         // counts as floats, plus the constant 1
     w += 8 * RP + 8;                                    // propensities (lane-major), alignment
     if (a.rate_stride) w += 8 * RP;                     // per-trajectory float-pair rates
+    if (!a.batch) w += 8 * 32 * (size_t)warp_ngroups(warp_chunk(a.R)) + 4 * 32;  // group sums, dirty masks
     l.warp_bytes = (w + 15) & ~(size_t)15;
     return l;
 }
@@ -225,6 +231,8 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
     float *cntf = reinterpret_cast<float *>(cnt0 + a.S);  // [S + 1]
     float2 *prop = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(cntf + a.S + 1) + 7) & ~(uintptr_t)7);
     float2 *rdf_w = prop + RP0;  // per-trajectory float-pair rates (single-network mode)
+    float2 *gsum = rdf_w + (a.rate_stride ? RP0 : 0);  // group sums [NG][32] (single-network mode)
+    uint32_t *dmask = reinterpret_cast<uint32_t *>(gsum + 32 * (size_t)warp_ngroups(C0));  // dirty groups per lane
     double *scr = a.warp_scratch + ((size_t)blockIdx.x * nw + warp) * (size_t)a.R;
     const int64_t t_start = global_ns();
     unsigned long long warp_events = 0;
@@ -262,9 +270,54 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
         const int r_lo = min(R, lane * C), r_hi = min(R, r_lo + C);
         const int n_own = r_hi - r_lo;
         const int mm = use_shape ? 2 : it.max_mults;  // multiplies per propensity
-        const float c_tot = (float)(mm + 1 + C + 5) * kGamma + (float)(R + mm + 4) * 0x1p-53f;
+        const int GS = warp_group(C), NG = warp_ngroups(C);
+        // dependency lists (one network only); a step whose list is longer
+        // than a third of the network re-evaluates everything
+        const bool deps = !BATCH && a.dep_off != nullptr;
+        // the chunk sum is a sum of group sums: at most GS + NG adds deep
+        const float c_tot = (float)(mm + 1 + GS + NG + 5) * kGamma + (float)(R + mm + 4) * 0x1p-53f;
         const float c_q = c_tot + 6.0f * kGamma;
         const float c_sel = 2.0f * (c_tot + (float)(C + 4) * kGamma);
+        // float-pair propensity of the reaction at lane-major position pos;
+        // bad is set when a count it reads lies outside [0, 2^23)
+        auto eval_prop = [&](int pos, bool &bad) -> DF {
+            const float2 k = rdf[pos];
+            if (use_shape) {
+                const uint32_t w = shape[pos];
+                const float n1 = cntf[w & 0x7FFFu], n2 = cntf[(w >> 16) & 0x7FFFu];
+                bad |= !(n1 >= 0.0f && n1 < 8388608.0f && n2 >= 0.0f && n2 < 8388608.0f);
+                const float f1 = fmaxf(__fsub_rn(n1, (float)((w >> 15) & 1u)), 0.0f);
+                const float f2 = fmaxf(__fsub_rn(n2, (float)(w >> 31)), 0.0f);
+                return df_mul_fu(df_mul_fu(DF{k.x, k.y}, f1), f2);
+            }
+            const int i2 = pos >> 5, l = pos & 31;
+            DF acc{k.x, k.y};
+            for (int p = 0; p < P; ++p) {
+                const int f = facl[(i2 * P + p) * 32 + l];
+                const int o = f >> 16;
+                if (o == 0) continue;
+                const int64_t n = cnt[f & 0xFFFF];
+                bad |= (uint64_t)n >= (1ull << 23);
+                for (int j = 0; j < o; ++j) {
+                    const int64_t x = n - j > 0 ? n - j : 0;
+                    acc = df_mul_fu(acc, f23((uint32_t)x & 0x7FFFFFu));
+                }
+            }
+            return acc;
+        };
+        // sum of this lane's group g (its propensities already in prop)
+        auto group_sum = [&](int g) -> DF {
+            DF s{0.f, 0.f};
+            const int e = min(n_own, (g + 1) * GS);
+            for (int i2 = g * GS; i2 < e; ++i2) {
+                const float2 v = prop[i2 * 32 + lane];
+                s = df_add(s, DF{v.x, v.y});
+            }
+            return s;
+        };
+        bool need_full = true;  // every propensity to be evaluated
+        bool amb_next = false;  // a re-evaluated propensity read a count out of range
+        DF ls{0.f, 0.f};        // this lane's chunk sum
 
         // ---- start (or resume) the trajectory
         Xoshiro g{0, 0, 0, 0};
@@ -316,38 +369,24 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                     }
                 }
                 // ---- float-pair propensities of this lane's chunk and their sum
-                DF ls{0.f, 0.f};
-                bool amb = false;
-                if (use_shape) {
-                    for (int i2 = 0; i2 < n_own; ++i2) {
-                        const float2 k = rdf[i2 * 32 + lane];
-                        const uint32_t w = shape[i2 * 32 + lane];
-                        const float n1 = cntf[w & 0x7FFFu], n2 = cntf[(w >> 16) & 0x7FFFu];
-                        amb |= !(n1 >= 0.0f && n1 < 8388608.0f && n2 >= 0.0f && n2 < 8388608.0f);
-                        const float f1 = fmaxf(__fsub_rn(n1, (float)((w >> 15) & 1u)), 0.0f);
-                        const float f2 = fmaxf(__fsub_rn(n2, (float)(w >> 31)), 0.0f);
-                        const DF acc = df_mul_fu(df_mul_fu(DF{k.x, k.y}, f1), f2);
-                        prop[i2 * 32 + lane] = make_float2(acc.h, acc.l);
-                        ls = df_add(ls, acc);
-                    }
-                } else {
-                    for (int i2 = 0; i2 < n_own; ++i2) {
-                        const float2 k = rdf[i2 * 32 + lane];
-                        DF acc{k.x, k.y};
-                        for (int p = 0; p < P; ++p) {
-                            const int f = facl[(i2 * P + p) * 32 + lane];
-                            const int o = f >> 16;
-                            if (o == 0) continue;
-                            const int64_t n = cnt[f & 0xFFFF];
-                            amb |= (uint64_t)n >= (1ull << 23);
-                            for (int j = 0; j < o; ++j) {
-                                const int64_t x = n - j > 0 ? n - j : 0;
-                                acc = df_mul_fu(acc, f23((uint32_t)x & 0x7FFFFFu));
-                            }
+                bool amb = amb_next;
+                amb_next = false;
+                if (need_full || BATCH) {
+                    ls = DF{0.f, 0.f};
+                    for (int g = 0; g < NG; ++g) {
+                        DF gs{0.f, 0.f};
+                        const int e = min(n_own, (g + 1) * GS);
+                        for (int i2 = g * GS; i2 < e; ++i2) {
+                            const DF acc = eval_prop(i2 * 32 + lane, amb);
+                            prop[i2 * 32 + lane] = make_float2(acc.h, acc.l);
+                            gs = df_add(gs, acc);
                         }
-                        prop[i2 * 32 + lane] = make_float2(acc.h, acc.l);
-                        ls = df_add(ls, acc);
+                        if (!BATCH) gsum[g * 32 + lane] = make_float2(gs.h, gs.l);
+                        ls = df_add(ls, gs);
                     }
+                    if (!BATCH) dmask[lane] = 0u;
+                    need_full = !deps;
+                    __syncwarp();
                 }
                 // inclusive scan of the chunk sums
                 DF incl = ls;
@@ -450,6 +489,38 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                         }
                     }
                 __syncwarp();
+                // ---- re-evaluate the propensities the jump touched, re-sum
+                // their groups and the chunks holding them
+                if (deps && idx < R) {
+                    const int d0 = a.dep_off[idx], d1 = a.dep_off[idx + 1];
+                    if (3 * (d1 - d0) > R) {
+                        need_full = true;
+                    } else {
+                        for (int e = d0 + lane; e < d1; e += 32) {
+                            const int pos = a.dep_pos[e];
+                            const DF acc = eval_prop(pos, amb_next);
+                            prop[pos] = make_float2(acc.h, acc.l);
+                            atomicOr(&dmask[pos & 31], 1u << ((pos >> 5) / GS));
+                        }
+                        __syncwarp();
+                        uint32_t m = dmask[lane];
+                        if (m) {
+                            dmask[lane] = 0u;
+                            while (m) {
+                                const int g = __ffs(m) - 1;
+                                m &= m - 1u;
+                                const DF gs = group_sum(g);
+                                gsum[g * 32 + lane] = make_float2(gs.h, gs.l);
+                            }
+                            ls = DF{0.f, 0.f};
+                            for (int g = 0; g < NG; ++g) {
+                                const float2 v = gsum[g * 32 + lane];
+                                ls = df_add(ls, DF{v.x, v.y});
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
             }
             if (abort_run) break;
             if (replay) {
@@ -480,6 +551,8 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                 }
                 if (abort_run) break;
                 for (int s = lane; s < S; s += 32) cntf[s] = (float)cnt[s];
+                need_full = true;
+                amb_next = false;
                 __syncwarp();
             }
             // ---- record sample i at t = T

@@ -453,6 +453,35 @@ def _random_net(rb, O, seed, S, R, x0_mean):
     return net, onet, x0
 
 
+def test_warp_kernel_dependency_updates_match_full_passes(rb, O):
+    # After a reaction fires the warp kernel re-evaluates only the propensities
+    # that read a species it changed; results equal full re-evaluation and the
+    # oracle, over networks whose lists are short (64 x 400) and long (a
+    # species read by every reaction makes some lists cover the network).
+    for seed, S, R, tmax in ((71, 64, 400, 2e-2), (72, 30, 300, 1e-2)):
+        net, onet, x0 = _random_net(rb, O, seed, S, R, 80.0)
+        if seed == 72:  # species 0 becomes a catalyst of every reaction
+            net = rb.Network(S + 1)
+            onet = O.OracleNet(S + 1)
+            import bench
+
+            reactions, x0 = bench.random_network(seed, S, R, x0_mean=80.0)
+            for k, e, d in reactions:
+                net.add_reaction(rb.Rate.lma(k, list(e) + [1]), list(d) + [0])
+                onet.add_lma_sparse(k, [(i, x) for i, x in enumerate(list(e) + [1]) if x], list(d) + [0])
+            net.add_reaction(rb.Rate.lma(5.0, [0] * S + [0]), [0] * S + [1])
+            onet.add_lma_sparse(5.0, [], [0] * S + [1])
+            x0 = list(x0) + [3]
+        seeds = _seeds(96, seed)
+        res = _with_kernel("warp", lambda: net.run_ensemble(x0, seeds, tmax, 10))
+        full = _with_env("RB_WARP_DEPS", "0", lambda: _with_kernel("warp", lambda: net.run_ensemble(x0, seeds, tmax, 10)))
+        ref, ev, _, _ = onet.run_ensemble(x0, seeds, tmax, 10)
+        assert res.stats["mapping"] == 5 and ev.min() > 100
+        np.testing.assert_array_equal(res.counts, ref)
+        np.testing.assert_array_equal(res.events, ev)
+        np.testing.assert_array_equal(full.counts, ref)
+
+
 def test_warp_kernel_matches_oracle(rb, O):
     # Warp per trajectory: a random network beyond the thread kernels (chosen
     # by the dispatcher), then small networks forced onto it.
