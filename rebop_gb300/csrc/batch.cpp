@@ -355,9 +355,6 @@ bool Batch::build(cudaStream_t st) {
         const int per_sm = std::max(1, ssa_warp_occupancy(warp_args, warp_warps, ssa_warp_smem(warp_args, warp_warps)));
         warp_grid = (int)std::max<int64_t>(
             1, std::min<int64_t>((acc + warp_warps - 1) / warp_warps, (int64_t)ctx->sm_count * per_sm));
-        const size_t scr = (size_t)warp_grid * warp_warps * maxR * sizeof(double);
-        if (!cuda_ok(cudaMalloc(&warp_scratch, scr), "cudaMalloc(batch warp scratch)")) return false;
-        warp_args.warp_scratch = warp_scratch;
     }
 
     // ---------------- every class's network on the device, kernels compiled
@@ -564,8 +561,6 @@ void Batch::free_device() {
     dev = nullptr;
     if (host) cudaFreeHost(host);
     host = nullptr;
-    if (warp_scratch) cudaFree(warp_scratch);
-    warp_scratch = nullptr;
     if (side) cudaStreamDestroy(side);
     side = nullptr;
     for (cudaEvent_t *e : {&fork, &join, &t0, &t1})

@@ -69,7 +69,6 @@ struct Batch {
     SsaArgs warp_args{};
     int warp_warps = 0, warp_grid = 0;
     int64_t warp_traj = 0;
-    double *warp_scratch = nullptr;
     cudaStream_t stream = nullptr, side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, t0 = nullptr, t1 = nullptr;
     cudaGraphExec_t exec = nullptr;

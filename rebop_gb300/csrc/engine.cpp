@@ -100,7 +100,6 @@ DeviceNet::~DeviceNet() {
     // are ignored here.
     if (desc) cudaFree(desc);
     if (scratch) cudaFree(scratch);
-    if (warp_scratch) cudaFree(warp_scratch);
     if (dep) cudaFree(dep);
     if (io) cudaFree(io);
     if (ev_start) cudaEventDestroy(ev_start);
@@ -110,12 +109,12 @@ DeviceNet::~DeviceNet() {
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-bool warp_dep_lists(const Packed &p, std::vector<int32_t> &off, std::vector<int32_t> &pos) {
+bool warp_dep_table(const Packed &p, std::vector<uint16_t> &tab) {
     const int R = p.R, P = p.P, Q = p.Q;
     const int C = (R + 31) / 32;
-    off.assign(1, 0);
-    pos.clear();
+    tab.clear();
     if (R < 1 || C > 256) return false;
+    tab.assign((size_t)R * 32, 0);
     // reactions reading each species
     std::vector<std::vector<int32_t>> readers((size_t)p.S);
     for (int r = 0; r < R; r++)
@@ -126,15 +125,17 @@ bool warp_dep_lists(const Packed &p, std::vector<int32_t> &off, std::vector<int3
             }
     std::vector<int32_t> mark((size_t)R, -1);
     for (int j = 0; j < R; j++) {
+        int n = 0;
+        uint16_t *row = tab.data() + (size_t)j * 32;
         for (int k = 0; k < Q; k++) {
             if (p.jmp_d[(size_t)j * Q + k] == 0) continue;
             for (int32_t r : readers[(size_t)p.jmp_sp[(size_t)j * Q + k]])
                 if (mark[(size_t)r] != j) {
                     mark[(size_t)r] = j;
-                    pos.push_back((r % C) * 32 + r / C);
+                    if (++n <= 31) row[n] = (uint16_t)((r % C) * 32 + r / C);
                 }
         }
-        off.push_back((int32_t)pos.size());
+        row[0] = n <= 31 ? (uint16_t)n : (uint16_t)0xFFFF;
     }
     return true;
 }
@@ -320,40 +321,22 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
         per_sm = std::max(1, ssa_warp_occupancy(a, warp_w, smem));
         const int64_t blocks = std::max<int64_t>(
             1, std::min<int64_t>((r.n_traj + warp_w - 1) / warp_w, (int64_t)ctx->sm_count * per_sm));
-        const size_t need = (size_t)blocks * warp_w * std::max<int32_t>(p.R, 1) * sizeof(double);
-        if (dn.warp_scratch_bytes < need) {
-            if (dn.warp_scratch) cudaFree(dn.warp_scratch);
-            dn.warp_scratch = nullptr;
-            dn.warp_scratch_bytes = 0;
-            if (!cuda_ok(cudaMalloc(&dn.warp_scratch, need), "cudaMalloc(warp scratch)")) return false;
-            dn.warp_scratch_bytes = need;
-        }
-        a.warp_scratch = dn.warp_scratch;
         // dependency lists: only the propensities a reaction's jump touches
         // are re-evaluated after it fires (RB_WARP_DEPS=0: all, every step)
         if (dn.dep_version != dn.version) {
             if (dn.dep) cudaFree(dn.dep);
             dn.dep = nullptr;
-            std::vector<int32_t> off, pos;
-            dn.dep_ok = warp_dep_lists(p, off, pos);
-            if (dn.dep_ok) {
-                const size_t bytes = sizeof(int32_t) * (off.size() + std::max<size_t>(pos.size(), 1));
-                if (!cuda_ok(cudaMalloc(&dn.dep, bytes), "cudaMalloc(dependency lists)") ||
-                    !cuda_ok(cudaMemcpy(dn.dep, off.data(), sizeof(int32_t) * off.size(), cudaMemcpyHostToDevice),
-                             "cudaMemcpy(dependency lists)") ||
-                    (!pos.empty() &&
-                     !cuda_ok(cudaMemcpy(dn.dep + off.size(), pos.data(), sizeof(int32_t) * pos.size(),
-                                         cudaMemcpyHostToDevice),
-                              "cudaMemcpy(dependency lists)")))
-                    return false;
-            }
+            std::vector<uint16_t> tab;
+            dn.dep_ok = warp_dep_table(p, tab);
+            if (dn.dep_ok &&
+                (!cuda_ok(cudaMalloc(&dn.dep, sizeof(uint16_t) * tab.size()), "cudaMalloc(dependency table)") ||
+                 !cuda_ok(cudaMemcpy(dn.dep, tab.data(), sizeof(uint16_t) * tab.size(), cudaMemcpyHostToDevice),
+                          "cudaMemcpy(dependency table)")))
+                return false;
             dn.dep_version = dn.version;
         }
         const char *wd = std::getenv("RB_WARP_DEPS");
-        if (dn.dep_ok && !(wd && std::strcmp(wd, "0") == 0)) {
-            a.dep_off = dn.dep;
-            a.dep_pos = dn.dep + p.R + 1;
-        }
+        if (dn.dep_ok && !(wd && std::strcmp(wd, "0") == 0)) a.dep_tab = dn.dep;
         if (timed && !cuda_ok(cudaEventRecord(dn.ev_start, stream), "cudaEventRecord")) return false;
         const int err = launch_ssa_warp(a, warp_w, (int)blocks, smem, stream);
         if (err != 0) return cuda_ok((cudaError_t)err, "SSA kernel launch");

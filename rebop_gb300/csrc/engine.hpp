@@ -45,8 +45,6 @@ struct DeviceNet {
     int32_t *ex_off = nullptr, *ex_code = nullptr;  // ex_off null: no Rate::Expr reaction
     double *ex_const = nullptr;
     unsigned long long *scratch = nullptr;  // [4]: trajectory ticket, event total, timeout flag
-    double *warp_scratch = nullptr;         // exact steps of the warp-per-trajectory kernel
-    size_t warp_scratch_bytes = 0;
     void *io = nullptr;                 // staging for rb_ensemble_run & friends
     size_t io_bytes = 0;
     cudaStream_t stream = nullptr;      // library stream of host-pointer calls
@@ -54,7 +52,7 @@ struct DeviceNet {
     cudaStream_t last_stream = nullptr; // stream of the last device-pointer run
     int64_t runs = 0;                   // sampled launches of this network
     double out_gbs = 0;                 // sample bytes / kernel time of the last host-pointer run
-    int32_t *dep = nullptr;             // warp kernel dependency lists: offsets, then positions
+    uint16_t *dep = nullptr;            // warp kernel dependency table [R][32]
     uint64_t dep_version = 0;           //   for this descriptor version (0: none built)
     bool dep_ok = false;                //   false: the network is beyond the lists' reach
     const void *jit_k = nullptr;        // generated kernel last used, for
@@ -63,12 +61,12 @@ struct DeviceNet {
     ~DeviceNet();
 };
 
-// Dependency lists of the warp kernel for a packed network: off gets R + 1
-// offsets into pos, which holds the lane-major positions (reaction l*C + i at
-// i*32 + l, C = ceil(R / 32)) of the reactions whose propensity reads a
-// species the reaction changes.  False when the kernel's update groups cannot
+// Dependency table of the warp kernel for a packed network ([R][32], see
+// SsaArgs::dep_tab): row j lists the lane-major positions (reaction l*C + i
+// at i*32 + l, C = ceil(R / 32)) of the reactions whose propensity reads a
+// species reaction j changes.  False when the kernel's update groups cannot
 // cover the network (more than 8192 reactions).
-bool warp_dep_lists(const Packed &p, std::vector<int32_t> &off, std::vector<int32_t> &pos);
+bool warp_dep_table(const Packed &p, std::vector<uint16_t> &tab);
 
 // Make net.dev current for the active device and descriptor version.
 // Caller holds net.mu.  Returns false (error set) on failure.

@@ -84,16 +84,13 @@ struct SsaArgs {
     // which shortens every trajectory's step latency.
     int32_t lanes;
 
-    // Warp-per-trajectory kernel: [grid * warps per block][R] doubles of
-    // scratch for its exact steps.
-    double *warp_scratch;
-    // Warp-per-trajectory kernel, one network: for each reaction j, the
-    // lane-major positions (see batch below) of the reactions whose
-    // propensity reads a species that j changes, dep_pos[dep_off[j] ..
-    // dep_off[j+1]).  After j fires only those are re-evaluated.  Null: every
-    // propensity is re-evaluated at every step.
-    const int32_t *dep_off;
-    const int32_t *dep_pos;
+    // Warp-per-trajectory kernel, one network: row j of dep_tab ([R][32])
+    // holds the number n of reactions whose propensity reads a species that
+    // reaction j changes, then their lane-major positions (see batch below)
+    // in entries 1 .. n; n = 0xFFFF when there are more than 31.  After j
+    // fires only those are re-evaluated (one coalesced load per step).  Null:
+    // every propensity is re-evaluated at every step.
+    const uint16_t *dep_tab;
 
     // Warp kernel over a batch of networks (batch != null): item k is
     // batch[k], its trajectories are the tickets batch_start[k] ..

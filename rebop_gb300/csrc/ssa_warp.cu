@@ -107,49 +107,69 @@ __device__ __forceinline__ double exact_propensity(const SsaArgs &it, const int6
 
 // One exact step of the whole warp from the committed state (lane 0 holds the
 // generator).  Returns 1 when a reaction fires (its index in idx, the clock in
-// t), 0 when the step records the sample.  scr is this warp's [R] scratch.
+// t), 0 when the step records the sample.  scr is this warp's shared-memory
+// scratch of 32 * ceil(R / 32) doubles, lane-major like the chunks: lane l
+// evaluates and folds its own reactions l*C .. l*C + C - 1, in order, starting
+// from the running sum lane l - 1 hands over, so the sums are the reference's
+// sequential fold (make_cumrates, gillespie.rs:357-364) while every lane reads
+// only its own column.
 template <bool MACRO>
 __device__ __noinline__ int warp_exact_step(const SsaArgs &it, const int64_t *cnt, const double *rates,
                                             const double *zig, double *scr, Xoshiro &g, double &t, double T,
                                             int &idx) {
-    const int lane = threadIdx.x & 31, R = it.R;
-    for (int r = lane; r < R; r += 32) scr[r] = exact_propensity<MACRO>(it, cnt, rates[r], r);
-    __syncwarp();
-    int fire = 0;
-    double chosen = 0.0;
-    int midx = R;
-    if (lane == 0) {
-        double total = 0.0;
-        for (int r = 0; r < R; ++r) {
-            total = __dadd_rn(total, scr[r]);
-            scr[r] = total;
-        }
-        if (0.0 < total) {
-            const double tn = __dadd_rn(t, __ddiv_rn(xo_exp1(g, zig, zig + kZigOffF), total));
-            if (!(tn > T)) {
-                fire = 1;
-                t = tn;
-                chosen = __dmul_rn(total, xo_uniform(g));
-                if (MACRO)  // first r with chosen < cum_r (gillespie_macro.rs:150-171)
-                    for (int r = 0; r < R; ++r)
-                        if (chosen < scr[r]) {
-                            midx = r;
-                            break;
-                        }
+    const int lane = threadIdx.x & 31, R = it.R, C = warp_chunk(R);
+    const int r_lo = min(R, lane * C), n_own = min(R, r_lo + C) - r_lo;
+    for (int i = 0; i < n_own; ++i) scr[i * 32 + lane] = exact_propensity<MACRO>(it, cnt, rates[r_lo + i], r_lo + i);
+    // the fold, one lane's chunk after the other; loads go ahead in blocks of 8
+    double run = 0.0;
+    for (int l = 0; l < 32; ++l) {
+        if (lane == l) {
+            for (int i0 = 0; i0 < n_own; i0 += 8) {
+                double v[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) v[j] = i0 + j < n_own ? scr[(i0 + j) * 32 + lane] : 0.0;
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    if (i0 + j < n_own) {
+                        run = __dadd_rn(run, v[j]);
+                        scr[(i0 + j) * 32 + lane] = run;
+                    }
             }
         }
+        run = shfl_d(run, l);
     }
-    __syncwarp();
+    const double total = run;
+    int fire = 0;
+    double chosen = 0.0;
+    if (lane == 0 && 0.0 < total) {
+        const double tn = __dadd_rn(t, __ddiv_rn(xo_exp1(g, zig, zig + kZigOffF), total));
+        if (!(tn > T)) {
+            fire = 1;
+            t = tn;
+            chosen = __dmul_rn(total, xo_uniform(g));
+        }
+    }
     fire = __shfl_sync(0xffffffffu, fire, 0);
     t = shfl_d(t, 0);
     if (!fire) return 0;
+    chosen = shfl_d(chosen, 0);
     if (MACRO) {
-        idx = __shfl_sync(0xffffffffu, midx, 0);
+        // first r with chosen < cum_r (gillespie_macro.rs:150-171): the first
+        // lane holding one, at its first position
+        int first = n_own;
+        for (int i = n_own - 1; i >= 0; --i)
+            if (chosen < scr[i * 32 + lane]) first = i;
+        const unsigned int has = __ballot_sync(0xffffffffu, first < n_own);
+        if (!has) {
+            idx = R;
+        } else {
+            const int l = __ffs((int)has) - 1;
+            idx = l * C + __shfl_sync(0xffffffffu, first, l);
+        }
     } else {
         // #{r : cum_r < chosen} (gillespie.rs:402-407), counted by all lanes
-        chosen = shfl_d(chosen, 0);
         int c = 0;
-        for (int r = lane; r < R; r += 32) c += scr[r] < chosen ? 1 : 0;
+        for (int i = 0; i < n_own; ++i) c += scr[i * 32 + lane] < chosen ? 1 : 0;
         for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
         idx = c;
     }
@@ -177,7 +197,7 @@ __host__ __device__ inline uint32_t shape_word(const int32_t *fac_sp, const int3
 // memory, lane-major); otherwise the one network of `a`, whose tables the
 // block copies to shared memory.
 template <bool MACRO, bool BATCH>
-__global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __grid_constant__ SsaArgs a) {
+__global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const __grid_constant__ SsaArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
     const WarpLayout L = warp_layout(a);  // sized for the largest network of the launch
 
@@ -233,7 +253,8 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
     float2 *rdf_w = prop + RP0;  // per-trajectory float-pair rates (single-network mode)
     float2 *gsum = rdf_w + (a.rate_stride ? RP0 : 0);  // group sums [NG][32] (single-network mode)
     uint32_t *dmask = reinterpret_cast<uint32_t *>(gsum + 32 * (size_t)warp_ngroups(C0));  // dirty groups per lane
-    double *scr = a.warp_scratch + ((size_t)blockIdx.x * nw + warp) * (size_t)a.R;
+    // exact steps use the propensity array as their scratch (32 * C doubles)
+    double *scr = reinterpret_cast<double *>(prop);
     const int64_t t_start = global_ns();
     unsigned long long warp_events = 0;
     bool abort_run = false;
@@ -273,7 +294,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
         const int GS = warp_group(C), NG = warp_ngroups(C);
         // dependency lists (one network only); a step whose list is longer
         // than a third of the network re-evaluates everything
-        const bool deps = !BATCH && a.dep_off != nullptr;
+        const bool deps = !BATCH && a.dep_tab != nullptr;
         // the chunk sum is a sum of group sums: at most GS + NG adds deep
         const float c_tot = (float)(mm + 1 + GS + NG + 5) * kGamma + (float)(R + mm + 4) * 0x1p-53f;
         const float c_q = c_tot + 6.0f * kGamma;
@@ -305,13 +326,42 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
             }
             return acc;
         };
-        // sum of this lane's group g (its propensities already in prop)
+        // sum of this lane's group g (its propensities already in prop), as
+        // a pairwise tree for groups of 8
         auto group_sum = [&](int g) -> DF {
+            const int b = g * GS, e = min(n_own, b + GS);
+            if (GS == 8) {
+                DF v[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const float2 q = b + t < e ? prop[(b + t) * 32 + lane] : make_float2(0.f, 0.f);
+                    v[t] = DF{q.x, q.y};
+                }
+                return df_add(df_add(df_add(v[0], v[1]), df_add(v[2], v[3])),
+                              df_add(df_add(v[4], v[5]), df_add(v[6], v[7])));
+            }
             DF s{0.f, 0.f};
-            const int e = min(n_own, (g + 1) * GS);
-            for (int i2 = g * GS; i2 < e; ++i2) {
-                const float2 v = prop[i2 * 32 + lane];
-                s = df_add(s, DF{v.x, v.y});
+            for (int i2 = b; i2 < e; ++i2) {
+                const float2 q = prop[i2 * 32 + lane];
+                s = df_add(s, DF{q.x, q.y});
+            }
+            return s;
+        };
+        // this lane's chunk sum from its group sums (pairwise up to 4 groups)
+        auto chunk_sum = [&]() -> DF {
+            if (NG <= 4) {
+                DF v[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const float2 q = t < NG ? gsum[t * 32 + lane] : make_float2(0.f, 0.f);
+                    v[t] = DF{q.x, q.y};
+                }
+                return df_add(df_add(v[0], v[1]), df_add(v[2], v[3]));
+            }
+            DF s{0.f, 0.f};
+            for (int g = 0; g < NG; ++g) {
+                const float2 q = gsum[g * 32 + lane];
+                s = df_add(s, DF{q.x, q.y});
             }
             return s;
         };
@@ -371,20 +421,25 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                 // ---- float-pair propensities of this lane's chunk and their sum
                 bool amb = amb_next;
                 amb_next = false;
-                if (need_full || BATCH) {
+                if (BATCH) {
                     ls = DF{0.f, 0.f};
+                    for (int i2 = 0; i2 < n_own; ++i2) {
+                        const DF acc = eval_prop(i2 * 32 + lane, amb);
+                        prop[i2 * 32 + lane] = make_float2(acc.h, acc.l);
+                        ls = df_add(ls, acc);
+                    }
+                } else if (need_full) {
                     for (int g = 0; g < NG; ++g) {
-                        DF gs{0.f, 0.f};
                         const int e = min(n_own, (g + 1) * GS);
                         for (int i2 = g * GS; i2 < e; ++i2) {
                             const DF acc = eval_prop(i2 * 32 + lane, amb);
                             prop[i2 * 32 + lane] = make_float2(acc.h, acc.l);
-                            gs = df_add(gs, acc);
                         }
-                        if (!BATCH) gsum[g * 32 + lane] = make_float2(gs.h, gs.l);
-                        ls = df_add(ls, gs);
+                        const DF gs = group_sum(g);
+                        gsum[g * 32 + lane] = make_float2(gs.h, gs.l);
                     }
-                    if (!BATCH) dmask[lane] = 0u;
+                    ls = chunk_sum();
+                    dmask[lane] = 0u;
                     need_full = !deps;
                     __syncwarp();
                 }
@@ -492,31 +547,27 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps) ssa_warp_kernel(const __gr
                 // ---- re-evaluate the propensities the jump touched, re-sum
                 // their groups and the chunks holding them
                 if (deps && idx < R) {
-                    const int d0 = a.dep_off[idx], d1 = a.dep_off[idx + 1];
-                    if (3 * (d1 - d0) > R) {
+                    const int v = a.dep_tab[(size_t)idx * 32 + lane];
+                    const int nd = __shfl_sync(0xffffffffu, v, 0);
+                    if (nd > 31) {
                         need_full = true;
                     } else {
-                        for (int e = d0 + lane; e < d1; e += 32) {
-                            const int pos = a.dep_pos[e];
-                            const DF acc = eval_prop(pos, amb_next);
-                            prop[pos] = make_float2(acc.h, acc.l);
-                            atomicOr(&dmask[pos & 31], 1u << ((pos >> 5) / GS));
+                        if (lane >= 1 && lane <= nd) {
+                            const DF acc = eval_prop(v, amb_next);
+                            prop[v] = make_float2(acc.h, acc.l);
+                            atomicOr(&dmask[v & 31], 1u << ((v >> 5) / GS));
                         }
                         __syncwarp();
                         uint32_t m = dmask[lane];
                         if (m) {
                             dmask[lane] = 0u;
                             while (m) {
-                                const int g = __ffs(m) - 1;
+                                const int g = __ffs((int)m) - 1;
                                 m &= m - 1u;
                                 const DF gs = group_sum(g);
                                 gsum[g * 32 + lane] = make_float2(gs.h, gs.l);
                             }
-                            ls = DF{0.f, 0.f};
-                            for (int g = 0; g < NG; ++g) {
-                                const float2 v = gsum[g * 32 + lane];
-                                ls = df_add(ls, DF{v.x, v.y});
-                            }
+                            ls = chunk_sum();
                         }
                         __syncwarp();
                     }
