@@ -337,6 +337,7 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
         }
         const char *wd = std::getenv("RB_WARP_DEPS");
         if (dn.dep_ok && !(wd && std::strcmp(wd, "0") == 0)) a.dep_tab = dn.dep;
+        if (const char *xc = std::getenv("RB_WARP_EXACT_CHOICE")) a.exact_choice = std::strcmp(xc, "0") != 0;
         if (timed && !cuda_ok(cudaEventRecord(dn.ev_start, stream), "cudaEventRecord")) return false;
         const int err = launch_ssa_warp(a, warp_w, (int)blocks, smem, stream);
         if (err != 0) return cuda_ok((cudaError_t)err, "SSA kernel launch");

@@ -91,6 +91,9 @@ struct SsaArgs {
     // fires only those are re-evaluated (one coalesced load per step).  Null:
     // every propensity is re-evaluated at every step.
     const uint16_t *dep_tab;
+    // Warp-per-trajectory kernel: decide every choice with the exact fold, as
+    // for a close float-pair comparison (RB_WARP_EXACT_CHOICE=1; tests).
+    int32_t exact_choice;
 
     // Warp kernel over a batch of networks (batch != null): item k is
     // batch[k], its trajectories are the tickets batch_start[k] ..

@@ -15,12 +15,17 @@
 // The reference's sums are a sequential binary64 fold, within (R + M + 2)
 // 2^-53 of the exact sums; the float pairs are within a few 2^-44 of them.
 // A decision whose operands lie farther apart than both bounds together is
-// the reference's decision.  Anything else -- a close choice or clock
-// comparison, a count outside [0, 2^23), a rate outside 2^-60 .. 2^60 --
-// re-runs the sample interval from its saved start with the exact step below:
-// lanes compute the binary64 propensities in the reference's multiply order,
-// lane 0 folds them in order and draws in native binary64, so counts, event
+// the reference's decision.  A close choice is redone for that step alone
+// with the exact fold below; anything else -- a close clock comparison, a
+// count outside [0, 2^23), a rate outside 2^-60 .. 2^60 -- re-runs the sample
+// interval from its saved start with the exact step: lanes compute the
+// binary64 propensities in the reference's multiply order and fold them in
+// order lane after lane, lane 0 draws in native binary64, so counts, event
 // numbers and the random stream equal rebop's bit for bit.
+//
+// After a reaction fires only the propensities reading a species it changed
+// are re-evaluated (SsaArgs::dep_tab); a lane's chunk is summed in groups, so
+// only the groups holding them are re-summed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -105,22 +110,19 @@ __device__ __forceinline__ double exact_propensity(const SsaArgs &it, const int6
     return acc;
 }
 
-// One exact step of the whole warp from the committed state (lane 0 holds the
-// generator).  Returns 1 when a reaction fires (its index in idx, the clock in
-// t), 0 when the step records the sample.  scr is this warp's shared-memory
-// scratch of 32 * ceil(R / 32) doubles, lane-major like the chunks: lane l
-// evaluates and folds its own reactions l*C .. l*C + C - 1, in order, starting
-// from the running sum lane l - 1 hands over, so the sums are the reference's
-// sequential fold (make_cumrates, gillespie.rs:357-364) while every lane reads
-// only its own column.
+// Exact binary64 propensities and their running sums, in scr: this warp's
+// shared-memory scratch of 32 * ceil(R / 32) doubles, lane-major like the
+// chunks.  Lane l evaluates and folds its own reactions l*C .. l*C + C - 1, in
+// order, starting from the running sum lane l - 1 hands over, so the sums are
+// the reference's sequential fold (make_cumrates, gillespie.rs:357-364) while
+// every lane reads only its own column.  Returns the total on every lane.
 template <bool MACRO>
-__device__ __noinline__ int warp_exact_step(const SsaArgs &it, const int64_t *cnt, const double *rates,
-                                            const double *zig, double *scr, Xoshiro &g, double &t, double T,
-                                            int &idx) {
+__device__ __forceinline__ double warp_exact_fold(const SsaArgs &it, const int64_t *cnt, const double *rates,
+                                                  double *scr) {
     const int lane = threadIdx.x & 31, R = it.R, C = warp_chunk(R);
     const int r_lo = min(R, lane * C), n_own = min(R, r_lo + C) - r_lo;
     for (int i = 0; i < n_own; ++i) scr[i * 32 + lane] = exact_propensity<MACRO>(it, cnt, rates[r_lo + i], r_lo + i);
-    // the fold, one lane's chunk after the other; loads go ahead in blocks of 8
+    // one lane's chunk after the other; loads go ahead in blocks of 8
     double run = 0.0;
     for (int l = 0; l < 32; ++l) {
         if (lane == l) {
@@ -138,7 +140,40 @@ __device__ __noinline__ int warp_exact_step(const SsaArgs &it, const int64_t *cn
         }
         run = shfl_d(run, l);
     }
-    const double total = run;
+    return run;
+}
+
+// The reaction the reference picks for `chosen` from the running sums in scr:
+// #{r : cum_r < chosen} (gillespie.rs:402-407), or for define_system! the
+// first r with chosen < cum_r (gillespie_macro.rs:150-171); R if none.
+template <bool MACRO>
+__device__ __forceinline__ int warp_exact_pick(const SsaArgs &it, const double *scr, double chosen) {
+    const int lane = threadIdx.x & 31, R = it.R, C = warp_chunk(R);
+    const int r_lo = min(R, lane * C), n_own = min(R, r_lo + C) - r_lo;
+    if (MACRO) {
+        int first = n_own;
+        for (int i = n_own - 1; i >= 0; --i)
+            if (chosen < scr[i * 32 + lane]) first = i;
+        const unsigned int has = __ballot_sync(0xffffffffu, first < n_own);
+        if (!has) return R;
+        const int l = __ffs((int)has) - 1;
+        return l * C + __shfl_sync(0xffffffffu, first, l);
+    }
+    int c = 0;
+    for (int i = 0; i < n_own; ++i) c += scr[i * 32 + lane] < chosen ? 1 : 0;
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+    return c;
+}
+
+// One exact step of the whole warp from the committed state (lane 0 holds the
+// generator).  Returns 1 when a reaction fires (its index in idx, the clock in
+// t), 0 when the step records the sample.
+template <bool MACRO>
+__device__ __noinline__ int warp_exact_step(const SsaArgs &it, const int64_t *cnt, const double *rates,
+                                            const double *zig, double *scr, Xoshiro &g, double &t, double T,
+                                            int &idx) {
+    const int lane = threadIdx.x & 31;
+    const double total = warp_exact_fold<MACRO>(it, cnt, rates, scr);
     int fire = 0;
     double chosen = 0.0;
     if (lane == 0 && 0.0 < total) {
@@ -152,28 +187,20 @@ __device__ __noinline__ int warp_exact_step(const SsaArgs &it, const int64_t *cn
     fire = __shfl_sync(0xffffffffu, fire, 0);
     t = shfl_d(t, 0);
     if (!fire) return 0;
-    chosen = shfl_d(chosen, 0);
-    if (MACRO) {
-        // first r with chosen < cum_r (gillespie_macro.rs:150-171): the first
-        // lane holding one, at its first position
-        int first = n_own;
-        for (int i = n_own - 1; i >= 0; --i)
-            if (chosen < scr[i * 32 + lane]) first = i;
-        const unsigned int has = __ballot_sync(0xffffffffu, first < n_own);
-        if (!has) {
-            idx = R;
-        } else {
-            const int l = __ffs((int)has) - 1;
-            idx = l * C + __shfl_sync(0xffffffffu, first, l);
-        }
-    } else {
-        // #{r : cum_r < chosen} (gillespie.rs:402-407), counted by all lanes
-        int c = 0;
-        for (int i = 0; i < n_own; ++i) c += scr[i * 32 + lane] < chosen ? 1 : 0;
-        for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
-        idx = c;
-    }
+    idx = warp_exact_pick<MACRO>(it, scr, shfl_d(chosen, 0));
     return 1;
+}
+
+// The exact choice alone, for a step whose clock the float pairs decided
+// (the reaction fires) but whose choice they left close: the reference's
+// total, chosen = total * U for the uniform's top 53 bits u53, and the pick.
+// Overwrites scr.
+template <bool MACRO>
+__device__ __noinline__ int warp_exact_choice(const SsaArgs &it, const int64_t *cnt, const double *rates,
+                                              double *scr, uint64_t u53) {
+    const double total = warp_exact_fold<MACRO>(it, cnt, rates, scr);
+    const double chosen = __dmul_rn(total, __dmul_rn((double)u53, 0x1.0p-53));
+    return warp_exact_pick<MACRO>(it, scr, chosen);
 }
 
 // Two-slot shape of reaction r (reactant order <= 2): slots (species, offset)
@@ -456,6 +483,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                 // ---- lane 0: Exp1 draw, clock, decision; then the uniform
                 int state = 0;  // 0 record, 1 fire, 2 undecided
                 DF ch{0.f, 0.f};
+                uint64_t u53 = 0;  // the choice uniform's top 53 bits (lane 0)
                 if (lane == 0 && !amb && tot.h > 0.0f) {
                     float xerr;
                     Xoshiro gt = g;
@@ -475,7 +503,8 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                         state = 2;
                     } else if (dd > mt) {
                         state = 1;
-                        ch = df_mul(tot, df_u53(xo_next(gt) >> 11));
+                        u53 = xo_next(gt) >> 11;
+                        ch = df_mul(tot, df_u53(u53));
                         g = gt;
                         tc = tn;
                         err_t = err_tn;
@@ -528,9 +557,11 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                     }
                     idx = k * C + count;
                 }
-                if (__any_sync(0xffffffffu, close)) {
-                    replay = true;
-                    break;
+                if (__any_sync(0xffffffffu, close) || a.exact_choice) {
+                    // the clock is decided: only the choice is redone, exactly
+                    // (the float-pair propensities are overwritten)
+                    idx = warp_exact_choice<MACRO>(it, cnt, rates, scr, __shfl_sync(0xffffffffu, u53, 0));
+                    need_full = true;
                 }
                 // ---- jump
                 ++ev;
@@ -546,7 +577,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                 __syncwarp();
                 // ---- re-evaluate the propensities the jump touched, re-sum
                 // their groups and the chunks holding them
-                if (deps && idx < R) {
+                if (deps && idx < R && !need_full) {
                     const int v = a.dep_tab[(size_t)idx * 32 + lane];
                     const int nd = __shfl_sync(0xffffffffu, v, 0);
                     if (nd > 31) {

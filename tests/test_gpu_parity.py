@@ -482,6 +482,31 @@ def test_warp_kernel_dependency_updates_match_full_passes(rb, O):
         np.testing.assert_array_equal(full.counts, ref)
 
 
+def test_warp_kernel_exact_choice_path(rb, O):
+    # Every choice taken by the exact lane-by-lane fold (the path of a close
+    # float-pair comparison), with dependency updates resuming after it, in
+    # both arithmetics.
+    net, onet, x0 = _random_net(rb, O, 73, 48, 200, 60.0)
+    seeds = _seeds(64, 73)
+    res = _with_env("RB_WARP_EXACT_CHOICE", "1",
+                    lambda: _with_kernel("warp", lambda: net.run_ensemble(x0, seeds, 5e-3, 5)))
+    ref, ev, _, _ = onet.run_ensemble(x0, seeds, 5e-3, 5)
+    assert res.stats["mapping"] == 5 and ev.min() > 50
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+    D = rb.define_system(DIMER_DSL)
+    d = D.with_parameters(25.0, 1000.0, 0.001, 0.1, 1.0)
+    d.gene = 1
+    res = _with_env("RB_WARP_EXACT_CHOICE", "1",
+                    lambda: _with_kernel("warp", lambda: d.run_ensemble(seeds, 0.2, 4)))
+    o = (O.OracleNet(4, macro=True).add_macro(25.0, [(0, 1)], [0, 1, 0, 0])
+         .add_macro(1000.0, [(1, 1)], [0, 0, 1, 0]).add_macro(0.001, [(2, 2)], [0, 0, -2, 1])
+         .add_macro(0.1, [(1, 1)], [0, -1, 0, 0]).add_macro(1.0, [(2, 1)], [0, 0, -1, 0]))
+    ref, ev, _, _ = o.run_ensemble([1, 0, 0, 0], seeds, 0.2, 4)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+
+
 def test_warp_kernel_matches_oracle(rb, O):
     # Warp per trajectory: a random network beyond the thread kernels (chosen
     # by the dispatcher), then small networks forced onto it.
