@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
     float *cntf = reinterpret_cast<float *>(cnt0 + a.S);  // [S + 1]
     float2 *prop = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(cntf + a.S + 1) + 7) & ~(uintptr_t)7);
     float2 *rdf_w = prop + RP0;  // per-trajectory float-pair rates (single-network mode)
-    float2 *gsum = rdf_w + (a.rate_stride ? RP0 : 0);  // group sums [NG][32] (single-network mode)
+    float2 *gsum = rdf_w + (a.rate_stride ? RP0 : 0);  // group sums [NG][32] (one network only)
     uint32_t *dmask = reinterpret_cast<uint32_t *>(gsum + 32 * (size_t)warp_ngroups(C0));  // dirty groups per lane
     // exact steps use the propensity array as their scratch (32 * C doubles)
     double *scr = reinterpret_cast<double *>(prop);
@@ -319,8 +319,9 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
         const int n_own = r_hi - r_lo;
         const int mm = use_shape ? 2 : it.max_mults;  // multiplies per propensity
         const int GS = warp_group(C), NG = warp_ngroups(C);
-        // dependency lists (one network only); a step whose list is longer
-        // than a third of the network re-evaluates everything
+        // dependency table (one network only: a batch's small networks gain
+        // nothing from it); a reaction with more than 31 dependents
+        // re-evaluates everything after it fires
         const bool deps = !BATCH && a.dep_tab != nullptr;
         // the chunk sum is a sum of group sums: at most GS + NG adds deep
         const float c_tot = (float)(mm + 1 + GS + NG + 5) * kGamma + (float)(R + mm + 4) * 0x1p-53f;
