@@ -411,9 +411,13 @@ def run_ours(args, w):
         threads = os.cpu_count() or 1
         nb = args.cpu_sample or w["cpu_sample"]
         r = cpu_reference(w, nb, 1, 0, threads)
+        # one core as well, on a sample of about a second
+        n1 = max(1, min(nb, int(nb * 1.0 / max(r["seconds"] * threads, 1e-9))))
+        r1 = cpu_reference(w, n1, 1, 0, 1)
         cpu = {"value": r["value"], "unit": "events/s", "cores": threads, "kind": "port",
                "sample": f"{nb} trajectories of the same workload, oracle port of the reference CPU path, "
-                         f"{threads} threads"}
+                         f"{threads} threads",
+               "value_1core": r1["value"], "sample_1core": f"{n1} trajectories on one thread"}
 
     calib = None
     if rank == 0 and w.get("calib_n"):
