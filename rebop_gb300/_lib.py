@@ -133,6 +133,8 @@ lib.rbg_internal_jit_source.argtypes = [_vp, _cp, _sz]
 lib.rbg_internal_jit_source.restype = C.c_int
 lib.rbg_internal_jit_compile.argtypes = [_vp, P(_u64)]
 lib.rbg_internal_jit_compile.restype = C.c_int
+lib.rbg_internal_warp_dep_table.argtypes = [_vp, P(C.c_uint16), _sz]
+lib.rbg_internal_warp_dep_table.restype = C.c_int
 
 
 def last_error() -> str:

@@ -655,6 +655,22 @@ int rbg_internal_jit_source(const rb_network *net, char *buf, size_t len) {
     return copy_name(rbg::jit_net_source(p, 512), buf, len);
 }
 
+// The warp kernel's dependency table for the network ([R][32] entries into
+// out, which holds cap entries); RB_ERR_UNSUPPORTED beyond its reach.
+int rbg_internal_warp_dep_table(const rb_network *net, uint16_t *out, size_t cap) {
+    if (!net || !out) return fail(RB_ERR_INVALID, "null argument");
+    std::vector<uint16_t> tab;
+    bool ok;
+    {
+        std::lock_guard<std::mutex> lk(net->net.mu);
+        ok = rbg::warp_dep_table(net->net.pack(), tab);
+    }
+    if (!ok) return fail(RB_ERR_UNSUPPORTED, "network beyond the dependency table's reach");
+    if (tab.size() > cap) return fail(RB_ERR_INVALID, "buffer too small");
+    std::memcpy(out, tab.data(), 2 * tab.size());
+    return RB_OK;
+}
+
 int rbg_internal_jit_compile(const rb_network *net, uint64_t *image_bytes) {
     if (!net) return fail(RB_ERR_INVALID, "null network");
     rbg::Packed p;

@@ -285,3 +285,31 @@ def test_batch_plan_groups_by_structure(rb):
         del os.environ["RB_BATCH_MIN_THREAD"]
     with pytest.raises(ValueError):
         b.add(mm, [1, 2, 3], seeds, 1.0, 2)
+
+
+def test_warp_dependency_table(rb):
+    # Row j of the warp kernel's dependency table lists, at lane-major
+    # positions, exactly the reactions whose propensity reads a species that
+    # reaction j changes; more than 31 of them mark the row for a full pass.
+    import bench
+    from rebop_gb300._lib import lib as L
+
+    for seed, S, R in ((3, 20, 90), (4, 200, 1000), (5, 6, 300)):
+        reactions, _ = bench.random_network(seed, S, R)
+        net = rb.Network(S)
+        for k, e, d in reactions:
+            net.add_reaction(rb.Rate.lma(k, e), d)
+        tab = np.zeros(R * 32, dtype=np.uint16)
+        assert L.rbg_internal_warp_dep_table(net._h, tab.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)),
+                                             tab.size) == 0
+        tab = tab.reshape(R, 32)
+        C = (R + 31) // 32
+        readers = [{r for r, (_, e, _) in enumerate(reactions) if e[s] > 0} for s in range(S)]
+        for j, (_, _, d) in enumerate(reactions):
+            deps = set().union(*[readers[s] for s in range(S) if d[s] != 0]) if any(d) else set()
+            pos = {(r % C) * 32 + r // C for r in deps}
+            if len(pos) > 31:
+                assert tab[j, 0] == 0xFFFF
+            else:
+                assert tab[j, 0] == len(pos)
+                assert set(tab[j, 1:1 + len(pos)].tolist()) == pos
