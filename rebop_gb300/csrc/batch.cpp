@@ -362,7 +362,7 @@ bool Batch::build(cudaStream_t st) {
         const Item &it0 = items[c.items[0]];
         std::lock_guard<std::mutex> lk(it0.net->mu);
         if (!ensure_device(*it0.net)) return false;
-        if (c.kind == Class::Merged && jit_supported(it0.packed) && !jit_kernel(it0.packed, ssa_spec_block()))
+        if (c.kind == Class::Merged && jit_supported(it0.packed) && !jit_kernel(it0.packed, jit_block()))
             cudaGetLastError();  // the descriptor kernel runs instead
     }
     if (!cuda_ok(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "cudaStreamCreate") ||

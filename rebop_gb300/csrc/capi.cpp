@@ -652,7 +652,7 @@ int rbg_internal_jit_source(const rb_network *net, char *buf, size_t len) {
     std::lock_guard<std::mutex> lk(net->net.mu);
     const rbg::Packed p = net->net.pack();
     if (!rbg::jit_supported(p)) return fail(RB_ERR_UNSUPPORTED, "network not covered by the generator");
-    return copy_name(rbg::jit_net_source(p, 512), buf, len);
+    return copy_name(rbg::jit_net_source(p, rbg::jit_block()), buf, len);
 }
 
 // The warp kernel's dependency table for the network ([R][32] entries into
@@ -680,7 +680,7 @@ int rbg_internal_jit_compile(const rb_network *net, uint64_t *image_bytes) {
     }
     if (!rbg::jit_supported(p)) return fail(RB_ERR_UNSUPPORTED, "network not covered by the generator");
     size_t n = 0;
-    if (!rbg::jit_compile(p, 512, &n)) return RB_ERR_UNSUPPORTED;
+    if (!rbg::jit_compile(p, rbg::jit_block(), &n)) return RB_ERR_UNSUPPORTED;
     if (image_bytes) *image_bytes = n;
     return RB_OK;
 }

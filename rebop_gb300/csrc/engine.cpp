@@ -384,8 +384,7 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
         const bool compile = jit ? !off : (r.n_traj >= 4096 || run_no >= 2);
         if (!off) {
             // generated kernels may run larger blocks (fewer registers per lane)
-            int kb = 512;
-            if (const char *e = std::getenv("RB_JIT_BLOCK")) kb = std::max(32, std::min(1024, std::atoi(e) / 32 * 32));
+            int kb = jit_block();
             // spread launches run 128 lanes of a kernel built for 128 (all
             // registers to the few lanes that hold trajectories)
             const bool spread = lanes != 0;

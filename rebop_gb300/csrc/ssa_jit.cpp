@@ -18,6 +18,7 @@
 #include <dlfcn.h>
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -361,6 +362,11 @@ const void *jit_kernel(const Packed &p, int block, bool compile) {
     }
     g_loaded[{dev, key}] = l;
     return (const void *)l.kern;
+}
+
+int jit_block() {
+    if (const char *e = std::getenv("RB_JIT_BLOCK")) return std::max(32, std::min(1024, std::atoi(e) / 32 * 32));
+    return 384;
 }
 
 int launch_ssa_jit(const void *kern, const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st) {

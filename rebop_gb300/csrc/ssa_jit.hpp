@@ -25,5 +25,9 @@ bool jit_compile(const Packed &p, int block, size_t *image_bytes);
 // kernel built for `block` lanes also runs blocks of fewer lanes.
 const void *jit_kernel(const Packed &p, int block, bool compile = true);
 int launch_ssa_jit(const void *kern, const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st);
+// Lanes per block of a generated kernel for a full-size ensemble: 384 (12
+// warps per SM at up to 168 registers a lane; fastest measured on the dimer and
+// Vilar networks), or RB_JIT_BLOCK rounded to a multiple of 32.
+int jit_block();
 
 }  // namespace rbg
