@@ -62,9 +62,9 @@ __host__ __device__ inline WarpLayout warp_layout(const SsaArgs &a) {
     size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;  // zxk, zf, zd, xdf
     if (!a.batch) {  // a batch's networks stay in global memory
         b += 8 * RP;                                        // shared float-pair rates (lane-major)
-        b += 4 * (size_t)a.R * a.P + 4 * RP * a.P;          // factors: reaction-major, lane-major
+        b += 4 * RP * a.P;                                  // factors (lane-major)
         b += 4 * RP;                                        // two-slot reaction shapes (lane-major)
-        b += 4 * (size_t)a.R * a.Q + 8 * (size_t)a.R * a.Q; // jumps (exact tables' layout)
+        b += 2 * (size_t)a.R * a.Q + 4 * (size_t)a.R * a.Q; // jumps: species (16 bit), deltas (32 bit)
         b += 16;                                            // alignment of the jump deltas
     }
     l.block_bytes = (b + 15) & ~(size_t)15;
@@ -238,19 +238,25 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
     const int C0 = warp_chunk(a.R), RP0 = 32 * C0;
     int32_t *facl_sh = reinterpret_cast<int32_t *>(rdf_sh + RP0);
     uint32_t *shape_sh = reinterpret_cast<uint32_t *>(facl_sh + (size_t)RP0 * a.P);
-    int32_t *fac_sh = reinterpret_cast<int32_t *>(shape_sh + RP0);
-    int32_t *jsp_sh = fac_sh + (size_t)a.R * a.P;
-    int64_t *jd_sh = reinterpret_cast<int64_t *>(
-        (reinterpret_cast<uintptr_t>(jsp_sh + (size_t)a.R * a.Q) + 7) & ~(uintptr_t)7);
-    if (BATCH) {
-        for (int k = tid; k < 256; k += blockDim.x) {
-            zxk[k] = make_ulonglong2((uint64_t)__double_as_longlong(a.zig[k]),
-                                     (uint64_t)__double_as_longlong(a.zig[kZigOffK + k]));
-            zd[k] = (uint64_t)__double_as_longlong(a.zig[kZigOffD + k]) & ~(1ull << 63);
+    // jumps of the one network: species as 16-bit indices (S < 65536), deltas
+    // as 32-bit values when every one fits (else read from the descriptor)
+    uint16_t *jsp_sh = reinterpret_cast<uint16_t *>(shape_sh + RP0);
+    int32_t *jd_sh = reinterpret_cast<int32_t *>(
+        (reinterpret_cast<uintptr_t>(jsp_sh + (size_t)a.R * a.Q) + 15) & ~(uintptr_t)15);
+    for (int k = tid; k < 256; k += blockDim.x) {
+        zxk[k] = make_ulonglong2((uint64_t)__double_as_longlong(a.zig[k]),
+                                 (uint64_t)__double_as_longlong(a.zig[kZigOffK + k]));
+        zd[k] = (uint64_t)__double_as_longlong(a.zig[kZigOffD + k]) & ~(1ull << 63);
+    }
+    for (int k = tid; k < 257; k += blockDim.x) zf[k] = (uint64_t)__double_as_longlong(a.zig[kZigOffF + k]);
+    bool jd_wide = false;
+    if (!BATCH) {
+        for (int k = tid; k < a.R * a.Q; k += blockDim.x) {
+            const int64_t dlt = a.jmp_d[k];
+            jsp_sh[k] = (uint16_t)a.jmp_sp[k];
+            jd_sh[k] = (int32_t)dlt;
+            jd_wide |= dlt != (int64_t)(int32_t)dlt;
         }
-        for (int k = tid; k < 257; k += blockDim.x) zf[k] = (uint64_t)__double_as_longlong(a.zig[kZigOffF + k]);
-    } else {
-        load_exact_tables(a, zxk, zf, zd, fac_sh, jsp_sh, jd_sh);
         const bool shape2 = a.max_mults <= 2 && a.S < 32767;
         for (int q = tid; q < RP0; q += blockDim.x) {
             const int i = q >> 5, l = q & 31, r = l * C0 + i;
@@ -268,8 +274,9 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
         const double v = a.zig[kZigOffXdf + k];
         xdf[k] = *reinterpret_cast<const float2 *>(&v);
     }
-    __syncthreads();
-    const ExactTables ex{zxk, zf, zd, fac_sh, jsp_sh, jd_sh};
+    jd_wide = __syncthreads_or(jd_wide);
+    // the Exp1 draws use the ziggurat tables only
+    const ExactTables ex{zxk, zf, zd, nullptr, nullptr, nullptr};
 
     // ---- this warp's region (sized for the largest network)
     unsigned char *wbase = g_spec_smem + L.block_bytes + (size_t)warp * L.warp_bytes;
@@ -312,8 +319,9 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
         const int32_t *facl = BATCH ? it.lm_fac : facl_sh;
         const uint32_t *shape = BATCH ? it.lm_shape : shape_sh;
         const bool use_shape = BATCH ? it.lm_shape != nullptr : (it.max_mults <= 2 && it.S < 32767);
-        const int32_t *jsp = BATCH ? it.jmp_sp : jsp_sh;
-        const int64_t *jd = BATCH ? it.jmp_d : jd_sh;
+        // reaction j's k-th jump entry: species, delta
+        auto jump_sp = [&](int e) -> int { return BATCH ? it.jmp_sp[e] : (int)jsp_sh[e]; };
+        auto jump_d = [&](int e) -> int64_t { return BATCH || jd_wide ? it.jmp_d[e] : (int64_t)jd_sh[e]; };
         // lane l owns reactions [l * C, min(R, (l + 1) * C)); local index i sits at i*32 + l
         const int r_lo = min(R, lane * C), r_hi = min(R, r_lo + C);
         const int n_own = r_hi - r_lo;
@@ -568,9 +576,9 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                 ++ev;
                 if (idx < R)
                     for (int q = lane; q < Q; q += 32) {
-                        const int64_t dlt = jd[idx * Q + q];
+                        const int64_t dlt = jump_d(idx * Q + q);
                         if (dlt != 0) {
-                            const int sp = jsp[idx * Q + q];
+                            const int sp = jump_sp(idx * Q + q);
                             cnt[sp] += dlt;
                             cntf[sp] = __fadd_rn(cntf[sp], (float)dlt);
                         }
@@ -627,8 +635,8 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                     ++ev;
                     if (idx < R)
                         for (int q = lane; q < Q; q += 32) {
-                            const int64_t dlt = jd[idx * Q + q];
-                            if (dlt != 0) cnt[jsp[idx * Q + q]] += dlt;
+                            const int64_t dlt = jump_d(idx * Q + q);
+                            if (dlt != 0) cnt[jump_sp(idx * Q + q)] += dlt;
                         }
                     __syncwarp();
                 }
