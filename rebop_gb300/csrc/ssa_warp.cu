@@ -331,8 +331,10 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
         // nothing from it); a reaction with more than 31 dependents
         // re-evaluates everything after it fires
         const bool deps = !BATCH && a.dep_tab != nullptr;
-        // the chunk sum is a sum of group sums: at most GS + NG adds deep
-        const float c_tot = (float)(mm + 1 + GS + NG + 5) * kGamma + (float)(R + mm + 4) * 0x1p-53f;
+        // adds on the way to a chunk sum: a batch sums its chunk in order (C),
+        // one network sums groups and then their sums (at most GS + NG)
+        const int depth = BATCH ? C : GS + NG;
+        const float c_tot = (float)(mm + 1 + depth + 5) * kGamma + (float)(R + mm + 4) * 0x1p-53f;
         const float c_q = c_tot + 6.0f * kGamma;
         const float c_sel = 2.0f * (c_tot + (float)(C + 4) * kGamma);
         // float-pair propensity of the reaction at lane-major position pos;
