@@ -276,7 +276,8 @@ def shard_seeds(rank: int, step: int, n: int) -> np.ndarray:
 # ---------------------------------------------------------------- GPU side
 # Kernel that runs each mapping (rb_run_stats.mapping) and what it is.
 MAPPINGS = {
-    5: ("ssa_warp_kernel", "warp per trajectory: lanes share the reaction list, float-pair scan, exact binary64 "
+    5: ("ssa_warp_kernel", "warp per trajectory: lanes share the reaction list, only the propensities a firing "
+                           "touches re-evaluated, float-pair scan, exact binary64 fold for close choices and "
                            "re-runs of undecided intervals"),
     4: ("rbg_net_kernel", "thread per trajectory, kernel generated for the network and compiled at run time "
                           "(NVRTC); float-pair speculation with exact binary64 re-runs"),
