@@ -104,3 +104,28 @@ def test_batch_merges_parameter_sets(rb, monkeypatch):
     for k, x0, seeds, rates in specs:
         _check(b, k, mm, x0, seeds, 3.0, 12, rates, [1, 3])
         assert b.mapping(k) in (2, 3, 4)
+
+
+def test_batch_of_networks_beyond_256_reactions(rb):
+    # Warp batch items whose lanes own more than 8 reactions each: their chunk
+    # sums are longer sequential chains, which the error bound must count.
+    import bench
+
+    rng = np.random.default_rng(9)
+    b = rb.Batch()
+    specs = []
+    for k, (S, R) in enumerate([(50, 400), (30, 300)]):
+        reactions, _ = bench.random_network(200 + k, S, R)
+        net = rb.Network(S)
+        for kk, e, d in reactions:
+            net.add_reaction(rb.Rate.lma(kk, e), d)
+        x0 = rng.integers(0, 501, size=S).tolist()
+        seeds = rng.integers(np.iinfo(np.uint64).max, size=24, dtype=np.uint64)
+        specs.append((b.add(net, x0, seeds, 1e-3, 5), net, x0, seeds, 1e-3, 5, None, None))
+    n_thread, n_warp = b.plan()
+    assert n_warp == 2 and n_thread == 0
+    st = b.run()
+    assert st["events"] > 0
+    for k, net, x0, seeds, tmax, nb, rates, save in specs:
+        _check(b, k, net, x0, seeds, tmax, nb, rates, save)
+        assert b.mapping(k) == 5
