@@ -168,3 +168,25 @@ def test_advance_until_is_resumable(O):
     sp, t, st, ev2, _, _ = net.advance_until(sp, t, st, 1.0)
     out = net.run_ensemble([1, 0, 0, 0], [99], 1.0, 2)[0]
     assert sp.tolist() == out[-1, :, 0].tolist() and t == 1.0
+
+
+def test_birth_death_matches_poisson_law(O):
+    # Statistical check independent of any stream: for births at k1 and
+    # deaths at k2 * n from n = 0, n(t) is Poisson with mean
+    # k1 / k2 * (1 - exp(-k2 t)) at every t.  Means, variances and the KS
+    # distance to that law, at every sample time, within 5 standard errors.
+    from scipy import stats
+
+    k1, k2, n_traj = 20.0, 1.0, 4000
+    net = O.OracleNet(1).add_lma(k1, [0], [1]).add_lma(k2, [1], [-1])
+    seeds = np.random.default_rng(77).integers(np.iinfo(np.uint64).max, size=n_traj, dtype=np.uint64)
+    out, _, _, _ = net.run_ensemble([0], seeds, 5.0, 10, n_threads=4)
+    for i in range(1, 11):
+        t = 0.5 * i
+        m = k1 / k2 * (1.0 - math.exp(-k2 * t))
+        x = out[i, 0, :].astype(float)
+        assert abs(x.mean() - m) < 5 * math.sqrt(m / n_traj), (t, x.mean(), m)
+        assert abs(x.var() - m) < 5 * math.sqrt((m + 2 * m * m) / n_traj), (t, x.var(), m)
+        vals = np.arange(0, int(x.max()) + 1)
+        ecdf = np.searchsorted(np.sort(x), vals, side="right") / n_traj
+        assert np.max(np.abs(ecdf - stats.poisson.cdf(vals, m))) < 1.63 / math.sqrt(n_traj) * 1.5, t
