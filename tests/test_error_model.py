@@ -77,3 +77,42 @@ def test_running_sums_and_total_within_their_bounds():
             G = (M + R + 2 + (R * (R + 1) / 2 + R * (M + 2)) / 16) * 2.0**-44
             got = Fraction(float(tot[0])) + Fraction(float(tot[1]))
             assert abs(got - total) <= Fraction(G) * total, (R, M)
+
+
+def f32_rz(v):
+    h = np.float32(v)
+    if abs(np.float64(h)) > abs(v):
+        h = np.nextafter(h, f32(0))
+    return h
+
+
+def test_float32_wedge_test_decides_as_binary64(O):
+    # The ziggurat's wedge test f[i+1] + (f[i] - f[i+1]) U < exp(-x), decided
+    # in float32 outside a 2^-17 band (wedge_df in ssa_spec_body.cuh), must
+    # agree with the binary64 test of the oracle's sampler whenever it
+    # decides.  x = (2k + 1) 2^-53 X[i] and U = mu 2^-53 as drawn; exp here is
+    # numpy's float32 exp, within the 2 ulp the band allows for expf.
+    X, F = O.zig_tables()
+    rng = np.random.default_rng(11)
+    decided = band = 0
+    for i in range(1, 256):
+        zd = F[i + 1] - F[i]
+        assert zd > 0
+        for _ in range(400):
+            k = int(rng.integers(0, 1 << 52))
+            mu = int(rng.integers(0, 1 << 53))
+            x = ((2 * k + 1) * 2.0**-53) * X[i]
+            U = mu * 2.0**-53
+            exact = F[i + 1] + (F[i] - F[i + 1]) * U < np.exp(-x)
+            u = f32(f32((mu >> 30) & 0x7FFFFF) * f32(2.0**-23))
+            wf = fma32(-f32_rz(zd), u, f32_rz(F[i + 1]))
+            ef = np.exp(-f32(x), dtype=np.float32)
+            if wf < f32(ef * f32(1 - 2.0**-17)):
+                decided += 1
+                assert exact, (i, k, mu)
+            elif wf > f32(ef * f32(1 + 2.0**-17)):
+                decided += 1
+                assert not exact, (i, k, mu)
+            else:
+                band += 1
+    assert decided > 100 * band
