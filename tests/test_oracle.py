@@ -190,3 +190,44 @@ def test_birth_death_matches_poisson_law(O):
         vals = np.arange(0, int(x.max()) + 1)
         ecdf = np.searchsorted(np.sort(x), vals, side="right") / n_traj
         assert np.max(np.abs(ecdf - stats.poisson.cdf(vals, m))) < 1.63 / math.sqrt(n_traj) * 1.5, t
+
+
+def test_generator_step_back_inverts_the_state_update(O):
+    # The float-pair step draws ahead and steps the generator back when it
+    # commits fewer draws (xo_prev in rebop_gb300/csrc/rng.cuh): restated here
+    # on the oracle's own stream, stepping forward n times and back n times
+    # returns the seeded state, and every output in between is the oracle's.
+    M = (1 << 64) - 1
+
+    def rotl(x, k):
+        return ((x << k) | (x >> (64 - k))) & M
+
+    def step(s):
+        s0, s1, s2, s3 = s
+        out = (rotl((s0 + s3) & M, 23) + s0) & M
+        t = (s1 << 17) & M
+        s2 ^= s0
+        s3 ^= s1
+        s1 ^= s2
+        s0 ^= s3
+        s2 ^= t
+        return out, [s0, s1, s2, rotl(s3, 45)]
+
+    def back(s):
+        d1 = rotl(s[3], 19)
+        y = s[1] ^ s[2]
+        b = (y ^ (y << 17) ^ (y << 34) ^ (y << 51)) & M
+        a = s[0] ^ d1
+        return [a, b, s[1] ^ b ^ a, d1 ^ b]
+
+    for seed in (0, 1, 42, 2**63 + 5):
+        st0 = [int(w) for w in O.seed_state(seed)]
+        ref = O.draw_u64(seed, 64)
+        s, states = st0, [st0]
+        for k in range(64):
+            out, s = step(s)
+            assert out == int(ref[k])
+            states.append(s)
+        for k in range(64, 0, -1):
+            s = back(s)
+            assert s == states[k - 1]
