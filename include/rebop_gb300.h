@@ -143,7 +143,10 @@ int rb_network_reaction_rate(const rb_network *net, int32_t r, double *rate);
  *   events    [n_traj] accepted events per trajectory, may be NULL
  *   final_species [n_traj][S], may be NULL
  *
- * rb_ensemble_run takes host buffers and does the copies itself;
+ * rb_ensemble_run takes host buffers and does the copies itself (page-locked
+ * out/events buffers may be written by the kernel in place, over the host
+ * link, when the network's previous run wrote its samples slowly; the call
+ * returns only once every result is in place either way);
  * rb_ensemble_run_device takes device buffers and a cudaStream_t (NULL:
  * the legacy default stream) and returns once the work is enqueued. */
 int rb_ensemble_run(const rb_network *net, int64_t n_traj, const int64_t *x0, int32_t x0_per_traj,
