@@ -313,3 +313,30 @@ def test_warp_dependency_table(rb):
             else:
                 assert tab[j, 0] == len(pos)
                 assert set(tab[j, 1:1 + len(pos)].tolist()) == pos
+
+
+def _build_cpp_mirror(tmp_path):
+    import shutil
+    import subprocess
+
+    from rebop_gb300 import build
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no g++")
+    exe = tmp_path / "rust_api_mirror"
+    lib = Path(build.LIB)
+    subprocess.run([cxx, "-std=c++17", "-O1", "-I", str(ROOT / "include"), str(ROOT / "tests/cpp/rust_api_mirror.cpp"),
+                    "-o", str(exe), "-L", str(lib.parent), "-l:" + lib.name, "-Wl,-rpath," + str(lib.parent)],
+                   check=True)
+    return exe
+
+
+def test_cpp_mirror_of_the_rust_api(rb, tmp_path):
+    # include/rebop_gb300.hpp: constructors, asserts as exceptions, accessors.
+    import subprocess
+
+    exe = _build_cpp_mirror(tmp_path)
+    r = subprocess.run([str(exe), "cpu"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.strip().endswith("ok")
