@@ -169,10 +169,30 @@ private:
 class Ensemble {
 public:
     explicit Ensemble(size_t n_species) { detail::check(rb_network_create((int32_t)n_species, &net_)); }
+    /* A define_system! body (src/gillespie_macro.rs:50-58), with the macro's
+     * arithmetic; its parameters start as NaN (set_param). */
+    static Ensemble from_dsl(const std::string &text) {
+        rb_network *n = nullptr;
+        detail::check(rb_network_from_dsl(text.c_str(), &n));
+        return Ensemble(n);
+    }
     Ensemble(const Ensemble &) = delete;
     Ensemble &operator=(const Ensemble &) = delete;
+    Ensemble(Ensemble &&o) noexcept : net_(o.net_) { o.net_ = nullptr; }
     ~Ensemble() {
         if (net_) rb_network_destroy(net_);
+    }
+    void set_param(const std::string &name, double value) {
+        detail::check(rb_network_set_param(net_, name.c_str(), value));
+    }
+    std::vector<std::string> params() const { return names(rb_network_nb_params(net_), rb_network_param_name); }
+    std::vector<std::string> species() const {
+        return names(rb_network_nb_species(net_), rb_network_species_name);
+    }
+    double reaction_rate(size_t r) const {
+        double v = 0.0;
+        detail::check(rb_network_reaction_rate(net_, (int32_t)r, &v));
+        return v;
     }
     size_t nb_species() const { return (size_t)rb_network_nb_species(net_); }
     size_t nb_reactions() const { return (size_t)rb_network_nb_reactions(net_); }
@@ -214,6 +234,16 @@ public:
     }
 
 private:
+    explicit Ensemble(rb_network *n) : net_(n) {}
+    std::vector<std::string> names(int32_t n, int (*get)(const rb_network *, int32_t, char *, size_t)) const {
+        std::vector<std::string> out;
+        char buf[256];
+        for (int32_t i = 0; i < n; ++i) {
+            detail::check(get(net_, i, buf, sizeof buf));
+            out.emplace_back(buf);
+        }
+        return out;
+    }
     rb_network *net_ = nullptr;
 };
 

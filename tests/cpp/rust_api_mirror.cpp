@@ -60,6 +60,23 @@ int main(int argc, char **argv) {
     e.add_reaction(rebop::Rate::lma(0.1, {0, 1, 0, 0}), {0, -1, 0, 0});
     e.add_reaction(rebop::Rate::lma(1.0, {0, 0, 1, 0}), {0, 0, -1, 0});
     EXPECT(e.nb_species() == 4 && e.nb_reactions() == 5);
+    // define_system! (gillespie_macro.rs:50-58): parameters start NaN
+    auto d = rebop::Ensemble::from_dsl(
+        "rtx rtl rdi rdm rdp; Dimers { gene, mRNA, protein, dimer } "
+        "transcription: gene => gene + mRNA @ rtx translation: mRNA => mRNA + protein @ rtl "
+        "dimerization: 2 protein => dimer @ rdi decay_mRNA: mRNA => @ rdm decay_prot: protein => @ rdp");
+    EXPECT(d.nb_species() == 4 && d.nb_reactions() == 5 && d.params().size() == 5);
+    EXPECT(d.species()[2] == "protein" && d.params()[1] == "rtl");
+    EXPECT(d.reaction_rate(1) != d.reaction_rate(1));  // NaN
+    d.set_param("rtl", 1000.0);
+    EXPECT(d.reaction_rate(1) == 1000.0);
+    threw = false;
+    try {
+        rebop::Ensemble::from_dsl("k; X { A } r: B => A @ k");
+    } catch (const std::invalid_argument &) {
+        threw = true;
+    }
+    EXPECT(threw);
     if (gpu) {
         for (double tm : {0.1, 0.25, 0.7}) g.advance_until(tm);
         std::printf("traj %.17g %lld %lld %lld %lld\n", g.get_time(), (long long)g.get_species(0),
