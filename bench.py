@@ -690,6 +690,12 @@ def main():
         run_batch(args)
         return
     if args.workload == "surrogate":
+        if args.impl == "reference":
+            if int(os.environ.get("RANK", "0")) == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned surrogate; "
+                                  "its plain SSA answers the same queries in the surrogate line "
+                                  "(ssa_queries_per_s)"}), flush=True)
+            return
         run_surrogate(args)
         return
     w = WORKLOADS[args.workload]
