@@ -142,6 +142,48 @@ def batch_items(seed: int = 20260105):
     return items
 
 
+def batch_seeds(step: int, j: int) -> np.ndarray:
+    """Seeds of batch item j at bench step `step`."""
+    return seeds_for(step, 100000 + j, BATCH["traj"])
+
+
+def make_batch(rb, items, want_events: bool = False):
+    """The heterogeneous batch of `items` (see batch_items) as one rb.Batch:
+    every Michaelis-Menten set shares one network with its own rate constants,
+    every random network is its own; seeds of step 0.  Returns (batch, networks)."""
+    b = rb.Batch()
+    mm = rb.Network(4)
+    for e, d in MM_REACTIONS:
+        mm.add_reaction(rb.Rate.lma(1.0, e), d)
+    nets = [mm]
+    for j, (kind, spec, x0) in enumerate(items):
+        seeds = batch_seeds(0, j)
+        if kind == "mm":
+            b.add(mm, x0, seeds, BATCH["tmax_mm"], BATCH["nb_steps"], rates=spec, want_events=want_events)
+        else:
+            net = rb.Network(len(x0))
+            for k, e, d in spec:
+                net.add_reaction(rb.Rate.lma(k, e), d)
+            nets.append(net)
+            b.add(net, x0, seeds, BATCH["tmax_rand"], BATCH["nb_steps"], want_events=want_events)
+    return b, nets
+
+
+def batch_oracle_net(O, item):
+    """The oracle's copy of a batch item's network (the reference's sparse form
+    for the random networks) and its horizon."""
+    kind, spec, x0 = item
+    if kind == "mm":
+        net = O.OracleNet(4)
+        for (e, d), k in zip(MM_REACTIONS, spec):
+            net.add_lma(k, e, d)
+        return net, BATCH["tmax_mm"]
+    net = O.OracleNet(len(x0))
+    for k, e, d in spec:
+        net.add_lma_sparse(k, [(i, x) for i, x in enumerate(e) if x], d)
+    return net, BATCH["tmax_rand"]
+
+
 def f_event(w) -> int:
     """Algorithmic binary64 operations per event of the direct method with full
     recompute: sum of reactant orders (LMA multiplies) + R (running sum) + R
@@ -477,19 +519,11 @@ def _batch_cpu(items, every: int, traj: int, threads: int):
     from oracle import oracle as O
 
     ev_tot, t_tot = 0, 0.0
-    for j, (kind, spec, x0) in enumerate(items):
+    for j, item in enumerate(items):
         if j % every:
             continue
-        if kind == "mm":
-            net = O.OracleNet(4)
-            for (e, d), k in zip(MM_REACTIONS, spec):
-                net.add_lma(k, e, d)
-            tmax = BATCH["tmax_mm"]
-        else:
-            net = O.OracleNet(len(x0))
-            for k, e, d in spec:
-                net.add_lma_sparse(k, [(i, x) for i, x in enumerate(e) if x], d)
-            tmax = BATCH["tmax_rand"]
+        net, tmax = batch_oracle_net(O, item)
+        x0 = item[2]
         seeds = seeds_for(0, 7000 + j, traj)
         t0 = time.perf_counter()
         _, _, ev, _ = net.run_ensemble(x0, seeds, tmax, BATCH["nb_steps"], n_threads=threads)
@@ -520,21 +554,7 @@ def run_batch(args):
                                   "d2h_bytes_per_step": 0}}), flush=True)
         return
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    b = rb.Batch()
-    mm = rb.Network(4)
-    for e, d in MM_REACTIONS:
-        mm.add_reaction(rb.Rate.lma(1.0, e), d)
-    nets = []
-    for j, (kind, spec, x0) in enumerate(items):
-        seeds = seeds_for(0, 100000 + j, traj)
-        if kind == "mm":
-            b.add(mm, x0, seeds, BATCH["tmax_mm"], BATCH["nb_steps"], rates=spec, want_events=False)
-        else:
-            net = rb.Network(len(x0))
-            for k, e, d in spec:
-                net.add_reaction(rb.Rate.lma(k, e), d)
-            nets.append(net)
-            b.add(net, x0, seeds, BATCH["tmax_rand"], BATCH["nb_steps"], want_events=False)
+    b, nets = make_batch(rb, items)
     n_thread, n_warp = b.plan()
     for s in range(args.warmup):
         b.run()
@@ -543,7 +563,7 @@ def run_batch(args):
     dev_ms, wall, events, h2d, d2h = 0.0, 0.0, 0, 0, 0
     for s in range(args.steps):
         for j in range(len(items)):
-            b.seeds(j)[:] = seeds_for(1 + s, 100000 + j, traj)
+            b.seeds(j)[:] = batch_seeds(1 + s, j)
         t0 = time.perf_counter()
         st = b.run()
         wall += time.perf_counter() - t0

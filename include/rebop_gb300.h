@@ -172,7 +172,10 @@ int rb_ensemble_run_device(const rb_network *net, int64_t n_traj, const int64_t 
  * library keeps until the process exits.  A network and sampling grid that
  * do not fit return RB_ERR_INVALID with the needed size in the message.
  * The first call on a device looks up that array's device address (with the
- * device current); make that first call before any stream capture.  Arguments
+ * device current); make that first call before any stream capture.  The address
+ * is kept for the life of the process, so it is stale after a cudaDeviceReset of
+ * that device.  The call's own data reaches the array as launch parameters of
+ * small staging kernels, so no host buffer is read after the call returns.  Arguments
  * are those of rb_ensemble_run_device (device buffers, host save_idx), plus
  * d_status: NULL or a device pointer to 2 uint64 receiving the run's event
  * total and its time-budget flag (1 = ran out, results incomplete).  Work is

@@ -224,6 +224,10 @@ public:
                int64_t nb_steps) const {
         Result r;
         const size_t n = seeds.size(), S = nb_species();
+        if (x0.size() != S)
+            throw std::invalid_argument("x0 has " + std::to_string(x0.size()) + " counts for " +
+                                        std::to_string(S) + " species");
+        if (nb_steps < 1) throw std::invalid_argument("nb_steps must be >= 1");
         r.counts.resize((size_t)(nb_steps + 1) * S * n);
         r.times.resize((size_t)nb_steps + 1);
         r.events.resize(n);

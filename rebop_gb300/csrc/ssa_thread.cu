@@ -390,6 +390,10 @@ int launch_ssa_events(const EventArgs &a, void *stream) {
 // All calls share the one array: each call clears the counters and rewrites
 // the rest before its kernel starts, and two calls whose work overlaps on the
 // GPU (for instance on two streams) overwrite each other's data and race.
+//
+// The call's own data reaches the array as the by-value parameters of small
+// staging kernels (at most kNoAllocStageChunk bytes each), which the launch
+// itself copies; no host buffer is read after the call returns.
 // ---------------------------------------------------------------------------
 
 #include <cstring>
@@ -406,11 +410,28 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
+// One staging launch: `nbytes` (a multiple of 16) bytes of `data` go to the
+// array at `offset`.  The struct travels as the kernel's parameter block
+// (below the 32 764-byte parameter limit).
+constexpr uint32_t kNoAllocStageChunk = 30720;
+struct NoAllocChunk {
+    uint32_t offset, nbytes;
+    alignas(16) unsigned char data[kNoAllocStageChunk];
+};
+
+__global__ void noalloc_stage_kernel(const __grid_constant__ NoAllocChunk c) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(c.data);
+    uint4 *dst = reinterpret_cast<uint4 *>(g_noalloc_scratch + c.offset);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < c.nbytes / 16; i += gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
 namespace {
 
 std::mutex g_na_mu;
 unsigned char *g_na_dev[kNoAllocMaxDevices];      // device address of the array, per device
 alignas(16) unsigned char g_na_host[kNoAllocScratchBytes];  // host image, built under g_na_mu
+NoAllocChunk g_na_chunk;                                    // parameter block, filled under g_na_mu
 
 size_t na_align(size_t v) { return (v + 15) & ~(size_t)15; }
 
@@ -464,15 +485,18 @@ int noalloc_ensemble_run(const Network &net, int64_t n_traj, const int64_t *d_x0
     std::lock_guard<std::mutex> lk(g_na_mu);
     if (!g_na_dev[dev]) {
         // Once per device, with that device current: the host-side name of
-        // the array is not a device address; ask the runtime for it.
+        // the array is not a device address; ask the runtime for it.  The
+        // address is kept for the life of the process, so it is stale after a
+        // cudaDeviceReset of that device.
         void *p = nullptr;
         ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (ce != cudaSuccess) return err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(ce), 2;
         g_na_dev[dev] = static_cast<unsigned char *>(p);
     }
     unsigned char *dbase = g_na_dev[dev];
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (ce != cudaSuccess) return err = std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(ce), 2;
 
     unsigned char *h = g_na_host;
     zig_tables_host(reinterpret_cast<double *>(h + o_zig), reinterpret_cast<double *>(h + o_zig) + kZigTable);
@@ -502,8 +526,18 @@ int noalloc_ensemble_run(const Network &net, int64_t n_traj, const int64_t *d_x0
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ce = cudaMemsetAsync(dbase, 0, kNoAllocCounterBytes, s);
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(dbase + o_zig, h + o_zig, used - o_zig, cudaMemcpyHostToDevice, s);
-    if (ce != cudaSuccess) return err = std::string("staging copy: ") + cudaGetErrorString(ce), 2;
+    if (ce != cudaSuccess) return err = std::string("counter reset: ") + cudaGetErrorString(ce), 2;
+    // The image goes over as launch parameters, copied when each staging
+    // kernel is launched, so g_na_host is free for the next call on return.
+    for (size_t off = o_zig; off < used; off += kNoAllocStageChunk) {
+        const size_t nb = std::min<size_t>(kNoAllocStageChunk, used - off);
+        g_na_chunk.offset = (uint32_t)off;
+        g_na_chunk.nbytes = (uint32_t)nb;
+        std::memcpy(g_na_chunk.data, h + off, nb);
+        noalloc_stage_kernel<<<8, 128, 0, s>>>(g_na_chunk);
+        ce = cudaGetLastError();
+        if (ce != cudaSuccess) return err = std::string("staging launch: ") + cudaGetErrorString(ce), 2;
+    }
 
     SsaArgs a{};
     a.S = (int32_t)S;

@@ -60,6 +60,21 @@ int main(int argc, char **argv) {
     e.add_reaction(rebop::Rate::lma(0.1, {0, 1, 0, 0}), {0, -1, 0, 0});
     e.add_reaction(rebop::Rate::lma(1.0, {0, 0, 1, 0}), {0, 0, -1, 0});
     EXPECT(e.nb_species() == 4 && e.nb_reactions() == 5);
+    // Ensemble::run checks its arguments before any GPU work
+    threw = false;
+    try {
+        e.run({1, 0, 0}, {1, 2}, 1.0, 10);  // 3 counts for 4 species
+    } catch (const std::invalid_argument &) {
+        threw = true;
+    }
+    EXPECT(threw);
+    threw = false;
+    try {
+        e.run({1, 0, 0, 0}, {1, 2}, 1.0, -5);
+    } catch (const std::invalid_argument &) {
+        threw = true;
+    }
+    EXPECT(threw);
     // define_system! (gillespie_macro.rs:50-58): parameters start NaN
     auto d = rebop::Ensemble::from_dsl(
         "rtx rtl rdi rdm rdp; Dimers { gene, mRNA, protein, dimer } "

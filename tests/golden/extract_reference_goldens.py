@@ -9,12 +9,14 @@ records each golden with the file:line it came from:
 plus the numpy seed the reference's Python wrapper derives for rng=42
 (python/rebop/gillespie.py:139-140), computed with numpy itself.
 
-Usage: python tests/golden/extract_reference_goldens.py [REFERENCE_ROOT]
+Usage: python tests/golden/extract_reference_goldens.py REFERENCE_ROOT
+(or set REBOP_REFERENCE to the rebop source tree).
 """
 
 from __future__ import annotations
 
 import json
+import os
 import re
 import sys
 from pathlib import Path
@@ -143,7 +145,11 @@ def extract_vilar(ref: Path) -> dict:
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    # the reference source tree: first argument, else $REBOP_REFERENCE
+    arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REBOP_REFERENCE")
+    if not arg:
+        sys.exit("usage: extract_reference_goldens.py <rebop source tree>  (or set REBOP_REFERENCE)")
+    ref = Path(arg)
     data = extract(ref)
     (HERE / "reference_goldens.json").write_text(json.dumps(data, indent=1) + "\n")
     print({k: (len(v) if isinstance(v, list) else v) for k, v in data.items()})

@@ -129,3 +129,30 @@ def test_batch_of_networks_beyond_256_reactions(rb):
     for k, net, x0, seeds, tmax, nb, rates, save in specs:
         _check(b, k, net, x0, seeds, tmax, nb, rates, save)
         assert b.mapping(k) == 5
+
+
+def test_bench_batch_against_oracle(rb, O):
+    # The bench's whole heterogeneous batch (4096 Michaelis-Menten parameter
+    # sets and 1024 random networks of 8-64 species and 16-256 reactions, 64
+    # trajectories each) runs once; every 16th parameter set, every 8th random
+    # network and every random network of 240 reactions or more are compared
+    # with the oracle, bit for bit, before and after a replay with new seeds.
+    import bench
+
+    items = bench.batch_items()
+    b, _ = bench.make_batch(rb, items, want_events=True)
+    n_mm = bench.BATCH["n_mm"]
+    pick = [j for j in range(len(items))
+            if (j < n_mm and j % 16 == 0) or (j >= n_mm and ((j - n_mm) % 8 == 0 or len(items[j][1]) >= 240))]
+    assert len(pick) > 400
+    for step in range(2):
+        if step:
+            for j in range(len(items)):
+                b.seeds(j)[:] = bench.batch_seeds(1, j)
+        st = b.run()
+        assert st["events"] > 0
+        for j in pick:
+            net, tmax = bench.batch_oracle_net(O, items[j])
+            ref, ev, _, _ = net.run_ensemble(items[j][2], b.seeds(j), tmax, bench.BATCH["nb_steps"])
+            np.testing.assert_array_equal(b.counts(j), ref, err_msg=f"item {j} (step {step})")
+            np.testing.assert_array_equal(b.events(j), ev, err_msg=f"item {j} (step {step})")

@@ -52,6 +52,34 @@ def test_fixed_seed_golden_through_dropin(rb, goldens):
     assert [int(ds[s][-1]) for s in ("S", "I", "R")] == [fs["final"][s] for s in ("S", "I", "R")]
 
 
+def test_dense_vs_sparse_through_dropin(rb, O, goldens):
+    # tests/test_rebop.py:55-65: sparse=None / False / True at rng=42 give the
+    # same dataset.  The drop-in runs all three on the GPU; the oracle runs the
+    # reference's dense (Rate::lma) and sparse (Rate::lma_sparse) forms with
+    # the seed the reference's wrapper derives from rng=42.
+    sir = rb.Gillespie()
+    sir.add_reaction(1e-4, ["S", "I"], ["I", "I"])
+    sir.add_reaction(0.01, ["I"], ["R"])
+    init, tmax, nb_steps, seed = {"S": 999, "I": 1}, 250, 250, 42
+    ds_auto = sir.run(init, tmax=tmax, nb_steps=nb_steps, rng=seed, sparse=None)
+    ds_dense = sir.run(init, tmax=tmax, nb_steps=nb_steps, rng=seed, sparse=False)
+    ds_sparse = sir.run(init, tmax=tmax, nb_steps=nb_steps, rng=seed, sparse=True)
+    for s in ("S", "I", "R"):
+        np.testing.assert_array_equal(np.asarray(ds_dense[s]), np.asarray(ds_auto[s]))
+        np.testing.assert_array_equal(np.asarray(ds_dense[s]), np.asarray(ds_sparse[s]))
+    np.testing.assert_array_equal(np.asarray(ds_dense.time), np.asarray(ds_sparse.time))
+    s64 = O.numpy_seed(seed)
+    dense, _, _, _ = O.sir_net().run_ensemble([999, 1, 0], [s64], float(tmax), nb_steps)
+    sp = (O.OracleNet(3).add_lma_sparse(1e-4, [(0, 1), (1, 1)], [-1, 1, 0])
+          .add_lma_sparse(0.01, [(1, 1)], [0, -1, 1]))
+    sparse, _, _, _ = sp.run_ensemble([999, 1, 0], [s64], float(tmax), nb_steps)
+    np.testing.assert_array_equal(dense, sparse)
+    for k, s in enumerate(("S", "I", "R")):
+        np.testing.assert_array_equal(np.asarray(ds_dense[s]), dense[:, k, 0])
+    fs = goldens["fixed_seed"]
+    assert [int(ds_sparse[s][-1]) for s in ("S", "I", "R")] == [fs["final"][s] for s in ("S", "I", "R")]
+
+
 def test_sir_ensemble_bit_exact(rb, O):
     seeds = _seeds(1000)
     res = _sir(rb).run_ensemble([999, 1, 0], seeds, 250.0, 250)

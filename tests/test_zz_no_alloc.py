@@ -9,8 +9,13 @@ the C ABI twice in a row, and each result must equal, bit for bit, what the
 allocating entry point rb_ensemble_run_device returns for the same inputs
 (integer counts: the same zero tolerance as every parity test of this engine).
 The second call checks that the array's leftovers from the first call do not
-leak into the next result.
+leak into the next result.  The no-allocation call also runs first on a network
+that has never been run, and afterwards that network still holds no per-network
+device state, and the device's free memory is the same before and after the
+second call.
 """
+
+import ctypes
 
 import numpy as np
 import pytest
@@ -33,7 +38,8 @@ def test_noalloc_entry_point_matches_allocating_one():
     import rebop_gb300 as rb
     from rebop_gb300._lib import RB_ERR_INVALID, RB_OK, last_error, lib
 
-    net = _dimer(rb)
+    net = _dimer(rb)       # runs through the no-allocation entry point only
+    ref_net = _dimer(rb)   # the same network for the allocating entry point
     n, nb, S = 1000, 50, 4
     stream = torch.cuda.current_stream().cuda_stream
     d_x0 = torch.tensor([1, 0, 0, 0], dtype=torch.int64, device="cuda")
@@ -45,18 +51,28 @@ def test_noalloc_entry_point_matches_allocating_one():
         na_out = torch.full((nb + 1, S, n), -7, dtype=torch.int64, device="cuda")
         na_ev = torch.full((n,), -7, dtype=torch.int64, device="cuda")
         status = torch.full((2,), -7, dtype=torch.int64, device="cuda")
-        rc = lib.rb_ensemble_run_device(net._h, n, d_x0.data_ptr(), 0, None, 0, d_seeds.data_ptr(), 1.0, nb, None,
-                                        -1, ref_out.data_ptr(), ref_ev.data_ptr(), None, stream)
-        assert rc == RB_OK, last_error()
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         rc = lib.rb_ensemble_run_device_noalloc(net._h, n, d_x0.data_ptr(), 0, None, 0, d_seeds.data_ptr(), 1.0,
                                                 nb, None, -1, na_out.data_ptr(), na_ev.data_ptr(),
                                                 status.data_ptr(), stream)
+        assert rc == RB_OK, last_error()
+        torch.cuda.synchronize()
+        if call == 1:
+            # the second call on an already set-up device takes no device memory
+            assert torch.cuda.mem_get_info()[0] == free0
+        rc = lib.rb_ensemble_run_device(ref_net._h, n, d_x0.data_ptr(), 0, None, 0, d_seeds.data_ptr(), 1.0, nb,
+                                        None, -1, ref_out.data_ptr(), ref_ev.data_ptr(), None, stream)
         assert rc == RB_OK, last_error()
         torch.cuda.synchronize()
         assert torch.equal(na_out, ref_out)
         assert torch.equal(na_ev, ref_ev)
         assert int(status[0]) == int(ref_ev.sum()) > n * 1000
         assert int(status[1]) == 0
+        # the network that only ran without allocation never built device state
+        ev = np.zeros(1, dtype=np.uint64)
+        assert lib.rb_ensemble_last_events(net._h, ev.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))) == RB_ERR_INVALID
+        assert "no run on this network yet" in last_error()
 
     # A sampling grid beyond the fixed array is refused with a clear error.
     rc = lib.rb_ensemble_run_device_noalloc(net._h, n, d_x0.data_ptr(), 0, None, 0, d_seeds.data_ptr(), 1.0,
