@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <random>
+#include <thread>
 
 #include "engine.hpp"
 #include "batch.hpp"
@@ -368,6 +369,7 @@ int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, i
     size_t o_x0 = c.take<int64_t>(n_x0 * S), o_rates = c.take<double>(n_rates * R), o_seed = c.take<uint64_t>(N);
     size_t o_st = c.take<double>(NT), o_save = c.take<int32_t>(NS), o_out = c.take<int64_t>(NT * NS * N);
     size_t o_ev = c.take<uint64_t>(N), o_fin = c.take<int64_t>(final_species ? N * S : 0);
+    size_t o_rows = c.take<uint32_t>(NT);
     if (!rbg::ensure_io(dn, c.off)) return RB_ERR_NOMEM;
     unsigned char *b = static_cast<unsigned char *>(dn.io);
     uint64_t h2d = 0, d2h = 0;
@@ -406,6 +408,25 @@ int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, i
     r.fin_species = final_species ? reinterpret_cast<int64_t *>(b + o_fin) : nullptr;
     r.times_ok = std::isfinite(tmax) && tmax >= 0;
     r.t_last = tmax;
+    // Sample rows stream back while the kernel runs: the speculative kernels
+    // count, per row, the trajectories whose samples are written (after a
+    // fence), and rows every trajectory has written are copied on a second
+    // stream; the rest follow the kernel.
+    const bool stream_rows = !out_host && N && NS && NT < 65536;
+    unsigned int *row_done = reinterpret_cast<unsigned int *>(b + o_rows);
+    if (stream_rows) {
+        r.row_done = row_done;
+        if (!cuda_check(cudaMemsetAsync(row_done, 0, NT * 4, dn.stream), "cudaMemsetAsync")) return RB_ERR_CUDA;
+        if (dn.pin_rows_n < NT) {
+            if (dn.pin_rows) cudaFreeHost(dn.pin_rows);
+            dn.pin_rows = nullptr;
+            dn.pin_rows_n = 0;
+            if (!cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&dn.pin_rows), NT * 4, cudaHostAllocDefault),
+                            "cudaHostAlloc"))
+                return RB_ERR_NOMEM;
+            dn.pin_rows_n = NT;
+        }
+    }
     int mapping = 0;
     if (!rbg::launch_sampled(net, dn, r, dn.stream, true, &mapping)) return RB_ERR_CUDA;
     if (out_host) d2h += NT * NS * N * 8;
@@ -415,11 +436,49 @@ int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, i
         d2h += bytes;
         return cuda_check(cudaMemcpyAsync(dst, b + off, bytes, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync");
     };
+    // only the speculative kernels (mappings 3, 4) count rows
+    const bool streaming = stream_rows && (mapping == 3 || mapping == 4);
+    size_t rows_copied = 0;
+    if (streaming) {
+        const size_t row_bytes = NS * N * 8;
+        char *hout = reinterpret_cast<char *>(out);
+        while (rows_copied < NT) {
+            // the kernel's end first: once it is over every row is final
+            const cudaError_t q = cudaEventQuery(dn.ev_stop);
+            if (q != cudaSuccess && q != cudaErrorNotReady) {
+                cuda_check(q, "SSA kernel");
+                return RB_ERR_CUDA;
+            }
+            size_t k = rows_copied;
+            if (q == cudaSuccess) {
+                k = NT;
+            } else {
+                if (!cuda_check(cudaMemcpyAsync(dn.pin_rows, row_done, NT * 4, cudaMemcpyDeviceToHost, dn.copy_stream),
+                                "cudaMemcpyAsync") ||
+                    !cuda_check(cudaStreamSynchronize(dn.copy_stream), "cudaStreamSynchronize"))
+                    return RB_ERR_CUDA;
+                while (k < NT && dn.pin_rows[k] >= (unsigned int)N) ++k;
+            }
+            if (k > rows_copied) {
+                cudaStream_t cs = q == cudaSuccess ? dn.stream : dn.copy_stream;
+                if (!cuda_check(cudaMemcpyAsync(hout + rows_copied * row_bytes, b + o_out + rows_copied * row_bytes,
+                                                (k - rows_copied) * row_bytes, cudaMemcpyDeviceToHost, cs),
+                                "cudaMemcpyAsync"))
+                    return RB_ERR_CUDA;
+                d2h += (k - rows_copied) * row_bytes;
+                rows_copied = k;
+            } else {
+                std::this_thread::sleep_for(std::chrono::microseconds(50));
+            }
+        }
+    }
     unsigned long long sc[3] = {0, 0, 0};  // total events, timeout flag, exact re-runs
-    if ((!out_host && !d2h_copy(out, o_out, NT * NS * N * 8)) || (!ev_host && !d2h_copy(events, o_ev, N * 8)) ||
+    if ((!out_host && !streaming && !d2h_copy(out, o_out, NT * NS * N * 8)) ||
+        (!ev_host && !d2h_copy(events, o_ev, N * 8)) ||
         !d2h_copy(final_species, o_fin, final_species ? N * S * 8 : 0) ||
         !cuda_check(cudaMemcpyAsync(sc, dn.scratch + 1, 24, cudaMemcpyDeviceToHost, dn.stream), "cudaMemcpyAsync") ||
-        !cuda_check(cudaStreamSynchronize(dn.stream), "ssa_thread_kernel"))
+        !cuda_check(cudaStreamSynchronize(dn.stream), "ssa_thread_kernel") ||
+        (streaming && !cuda_check(cudaStreamSynchronize(dn.copy_stream), "cudaStreamSynchronize")))
         return RB_ERR_CUDA;
     if (sc[1]) return fail(RB_ERR_TIMEOUT, "ensemble run ran out of its time budget (RB_KERNEL_BUDGET_S)");
     const uint64_t total_events = sc[0];

@@ -105,6 +105,8 @@ DeviceNet::~DeviceNet() {
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_stop) cudaEventDestroy(ev_stop);
     if (stream) cudaStreamDestroy(stream);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    if (pin_rows) cudaFreeHost(pin_rows);
 }
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -148,6 +150,7 @@ bool ensure_device(const Network &net) {
         auto dn = std::make_unique<DeviceNet>();
         dn->device = ctx->device;
         if (!cuda_ok(cudaStreamCreateWithFlags(&dn->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+            !cuda_ok(cudaStreamCreateWithFlags(&dn->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
             !cuda_ok(cudaEventCreate(&dn->ev_start), "cudaEventCreate") ||
             !cuda_ok(cudaEventCreate(&dn->ev_stop), "cudaEventCreate") ||
             !cuda_ok(cudaMalloc(&dn->scratch, 4 * sizeof(unsigned long long)), "cudaMalloc(scratch)"))
@@ -346,10 +349,12 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
         return true;
     }
     if (spec) {
+        a.row_done = r.n_samples < 65536 ? r.row_done : nullptr;
         block = lanes ? 128 : ssa_spec_block();
         a.n_slots = lanes ? 128 : spec_slots;
         a.lanes = lanes;
         if (const char *ph = std::getenv("RB_SPEC_PHASE")) a.phase_steps = std::atoi(ph);
+        if (const char *sc = std::getenv("RB_SPEC_SCHED")) a.sched = std::strcmp(sc, "rot") == 0 ? 1 : 0;
         smem = ssa_spec_smem(a, a.n_slots);
         per_sm = ssa_spec_occupancy(a, block, smem);
     } else if (fast) {

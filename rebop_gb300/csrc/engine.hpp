@@ -48,6 +48,9 @@ struct DeviceNet {
     void *io = nullptr;                 // staging for rb_ensemble_run & friends
     size_t io_bytes = 0;
     cudaStream_t stream = nullptr;      // library stream of host-pointer calls
+    cudaStream_t copy_stream = nullptr; // result rows copied back while the kernel runs
+    unsigned int *pin_rows = nullptr;   // page-locked copy of the row counters
+    size_t pin_rows_n = 0;
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaStream_t last_stream = nullptr; // stream of the last device-pointer run
     int64_t runs = 0;                   // sampled launches of this network
@@ -94,6 +97,7 @@ struct RunDev {
     double *fin_t = nullptr;
     uint64_t *fin_rng = nullptr;
     uint64_t *events = nullptr;
+    unsigned int *row_done = nullptr;  // [n_samples] row counters (speculative kernels)
     bool times_ok = false;  // every sample time finite and >= 0 (lets the fast kernels run)
     double t_last = 0.0;    // largest sample time
 };

@@ -61,6 +61,10 @@ struct SsaArgs {
     // scratch: [0] trajectory ticket, [1] total accepted events,
     // [2] set to 1 when the time budget ran out, [3] exact interval re-runs
     unsigned long long *work;
+    // Speculative kernels, nullable: [n_samples] per sample row, the number of
+    // trajectories whose row of `out` is written and visible device-wide (the
+    // host copies finished rows while the launch runs).  n_samples < 65536.
+    unsigned int *row_done;
 
     // Exp1 ziggurat tables: x[257] then f[257]
     const double *zig;
@@ -83,6 +87,13 @@ struct SsaArgs {
     // Small ensembles spread over more warps and SMs with fewer lanes each,
     // which shortens every trajectory's step latency.
     int32_t lanes;
+    // Speculative kernel: which live slots a warp's lanes take at a phase
+    // boundary when there are more than 32.  0: the 32 whose clocks lag
+    // furthest behind (every trajectory advances through simulated time at
+    // about the same pace, so the ones with the most events get the most steps
+    // and the warp's trajectories end together); 1: rotation over the live
+    // slots (every trajectory gets the same number of steps).
+    int32_t sched;
 
     // Warp-per-trajectory kernel, one network: row j of dep_tab ([R][32])
     // holds the number n of reactions whose propensity reads a species that

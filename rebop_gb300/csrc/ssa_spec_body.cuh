@@ -273,6 +273,7 @@ __host__ __device__ inline size_t spec_smem_bytes(const SsaArgs &a, int slots) {
     b += 80 * (size_t)slots;                            // 10 state words
     b += 32 * (size_t)slots;                            // 7 float state words, flags
     b += 4 * (size_t)slots + 512;                       // slot list, block counters
+    b += 8 * (size_t)slots;                             // rows recorded, not yet counted
     b += 4 * ((size_t)R * P + (size_t)R * Q);           // fac, jsp
     return (b + 15) & ~(size_t)15;
 }
@@ -355,6 +356,65 @@ __device__ __noinline__ int exact_choice_table(const SsaArgs &a, const ExactTabl
 
 // Slot flags.
 constexpr uint32_t kLive = 1, kNat = 2, kExactTraj = 4, kBegin = 8, kHave = 16;
+
+// Rows [lo, hi) of `out` hold this lane's trajectory's samples: count them in
+// a.row_done, after a fence that makes the sample stores visible device-wide
+// first (the host copies a row once its count reaches n_traj).
+__device__ __forceinline__ void count_rows_nofence(const SsaArgs &a, uint32_t lo, uint32_t hi) {
+    for (uint32_t r = lo; r < hi; ++r) atomicAdd(a.row_done + r, 1u);
+}
+static __device__ __noinline__ void count_rows(const SsaArgs &a, uint32_t lo, uint32_t hi) {
+    __threadfence();
+    count_rows_nofence(a, lo, hi);
+}
+
+// Live-slot entries per lane that the lag scheduler keeps in registers (it
+// covers warps of up to 128 live slots; beyond that the lanes rotate).
+constexpr int kSpecSchedPerLane = 4;
+
+// Slot for this lane among a warp's n_live > 32 live slots (wlist[0 ..
+// n_live)): the 32 whose clocks lag furthest behind.  A slot that holds no
+// trajectory yet counts as time 0.  Keys are the clock's float bits (monotone
+// for t >= 0) with the low bits replaced by the list position, so they are
+// unique; a radix search finds tau, the 33rd smallest key, and the keys below
+// it go to the lanes in list order.  stf[0 .. NS) holds each slot's clock.
+static __device__ __noinline__ int lag_select(const float *stf, const uint32_t *stflag, int32_t *wlist, int n_live, int lane) {
+    const int nb = 32 - __clz(n_live - 1);  // bits of a list position
+    const uint32_t low = (1u << nb) - 1u;
+    uint32_t key[kSpecSchedPerLane];
+    int32_t sl[kSpecSchedPerLane];
+#pragma unroll
+    for (int c = 0; c < kSpecSchedPerLane; ++c) {
+        const int e = c * 32 + lane;
+        key[c] = 0xFFFFFFFFu;
+        sl[c] = -1;
+        if (e < n_live) {
+            const int32_t s = wlist[e];
+            const uint32_t t = (stflag[s] & kHave) ? __float_as_uint(stf[s]) : 0u;
+            key[c] = (t & ~low) | (uint32_t)e;
+            sl[c] = s;
+        }
+    }
+    uint32_t tau = 0;
+    for (int b = 31; b >= 0; --b) {
+        const uint32_t cand = tau | (1u << b);
+        unsigned int cnt = 0;
+#pragma unroll
+        for (int c = 0; c < kSpecSchedPerLane; ++c) cnt += key[c] < cand ? 1u : 0u;
+        if (__reduce_add_sync(0xffffffffu, cnt) <= 32u) tau = cand;
+    }
+    __syncwarp();  // every lane has read its list entries
+    int n_sel = 0;
+#pragma unroll
+    for (int c = 0; c < kSpecSchedPerLane; ++c) {
+        const bool sel = key[c] < tau;
+        const unsigned int bal = __ballot_sync(0xffffffffu, sel);
+        if (sel) wlist[n_sel + __popc(bal & ((1u << lane) - 1u))] = sl[c];
+        n_sel += __popc(bal);
+    }
+    __syncwarp();
+    return wlist[lane];
+}
 
 // Network operations of the float-pair step over a data-driven descriptor:
 // the counts stay in the slot's shared-memory column and every reaction walks
@@ -451,7 +511,12 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     uint32_t *stflag = reinterpret_cast<uint32_t *>(stf + 7 * (size_t)NS);
     int32_t *slot_list = reinterpret_cast<int32_t *>(stflag + NS);
     int32_t *ctr = slot_list + NS;  // [1] abort flag
-    int32_t *fac = ctr + 128;
+    // rows a slot's trajectories recorded since the last count (a.row_done):
+    // spend = lo | hi << 16 for rows [lo, hi) of the trajectory it holds (0:
+    // none), sfin = lo + 1 for rows [lo, n_samples) of one that ended (0: none)
+    uint32_t *spend = reinterpret_cast<uint32_t *>(ctr + 128);
+    uint32_t *sfin = spend + NS;
+    int32_t *fac = reinterpret_cast<int32_t *>(sfin + NS);
     int32_t *jsp = fac + (size_t)R * P;
     int32_t *ssave = jsp + (size_t)R * Q;  // saved species indices
     const int n_cache = spec_sample_cache(a);
@@ -481,7 +546,11 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
         }
     // every slot a lane may hold starts live and empty (no trajectory taken yet)
     const int lanes = a.lanes > 0 && a.lanes < 32 ? a.lanes : 32;
-    for (int k = tid; k < NS; k += BD) stflag[k] = lanes == 32 || (k % SPW) < lanes ? kLive : 0u;
+    for (int k = tid; k < NS; k += BD) {
+        stflag[k] = lanes == 32 || (k % SPW) < lanes ? kLive : 0u;
+        spend[k] = 0;
+        sfin[k] = 0;
+    }
     if (tid < 128) ctr[tid] = 0;
     __syncthreads();
     const ExactTables ex{zxk, zf, zd, fac, jsp, jd};
@@ -698,6 +767,10 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                     const uint64_t i = st[9 * NS];
                     int64_t *o = a.out + (size_t)i * a.n_save * a.n_traj + traj;
                     for (int k = 0; k < a.n_save; ++k) o[(size_t)k * a.n_traj] = sp[ssave[k] * NS];
+                    if (a.row_done) {
+                        const uint32_t pw = spend[slot];
+                        spend[slot] = (pw ? (pw & 0xFFFFu) : (uint32_t)i) | ((uint32_t)(i + 1) << 16);
+                    }
                     if ((long long)i + 1 < a.n_samples) {
                         st[9 * NS] = i + 1;
                         st[4 * NS] = st[5 * NS];  // next interval starts at T
@@ -717,8 +790,24 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                         if (a.events) a.events[traj] = ev;
                         lane_events += ev;
                         have = false;
+                        if (a.row_done) {
+                            // a second trajectory ending in one phase counts
+                            // the first one's rows now
+                            if (sfin[slot]) count_rows(a, sfin[slot] - 1u, (uint32_t)a.n_samples);
+                            sfin[slot] = (spend[slot] & 0xFFFFu) + 1u;
+                            spend[slot] = 0;
+                        }
                     }
                 }
+            }
+            // ---- count the rows recorded in this phase (one fence per lane)
+            if (a.row_done && (spend[slot] | sfin[slot])) {
+                const uint32_t pw = spend[slot], fw = sfin[slot];
+                __threadfence();
+                if (fw) count_rows_nofence(a, fw - 1u, (uint32_t)a.n_samples);
+                if (pw) count_rows_nofence(a, pw & 0xFFFFu, pw >> 16);
+                spend[slot] = 0;
+                sfin[slot] = 0;
             }
             // ---- park the slot's hot state
             if (live) {
@@ -743,10 +832,11 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
         __syncwarp();
         // ---------------------------------------------------------- compaction
         // Each warp owns slots [wbase, wbase + SPW) and never waits for
-        // another warp: its live slots, in slot order, go to its list; lanes
-        // take consecutive list entries, so the warp stays full while
-        // trajectories end at different times.  With more live slots than
-        // lanes the starting entry rotates by 32 per phase.
+        // another warp: its live slots, in slot order, go to its list, so the
+        // warp stays full while trajectories end at different times.  With
+        // more live slots than lanes the lanes take the 32 slots whose clocks
+        // lag furthest behind (a.sched == 0), or the starting entry rotates by
+        // 32 per phase (a.sched == 1).
         int n_live = 0;
         for (int c0 = 0; c0 < SPW; c0 += 32) {
             const int j = c0 + lane;
@@ -764,12 +854,14 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
         if (n_live <= 32) {
             slot = lane < n_live ? wlist[lane] : -1;
             rot = 0;
-        } else {
+        } else if (a.sched != 0 || n_live > 32 * kSpecSchedPerLane) {
             rot %= (unsigned int)n_live;
             unsigned int k = rot + (unsigned int)lane;
             if (k >= (unsigned int)n_live) k -= (unsigned int)n_live;
             slot = wlist[k];
             rot += 32u;
+        } else {
+            slot = lag_select(stf, stflag, wlist, n_live, lane);
         }
         live = slot >= 0;
         if (live) {

@@ -77,7 +77,7 @@ def test_large_network_full_size(rb, O):
     res = net.run_ensemble(w["x0"], seeds, w["tmax"], w["nb_steps"])
     assert res.stats["mapping"] == 5
     assert res.events.mean() > 5e4
-    pick = np.unique(np.concatenate([np.arange(0, 10_000, 40), [1, 9998, 9999]]))
+    pick = np.unique(np.concatenate([np.arange(0, 10_000, 38), [1, 9998, 9999]]))
     assert pick.size >= 256
     ref, ev, _, _ = onet.run_ensemble(w["x0"], seeds[pick], w["tmax"], w["nb_steps"])
     np.testing.assert_array_equal(res.counts[:, :, pick], ref)
