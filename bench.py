@@ -251,15 +251,22 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU side
-def cpu_reference(w, n_traj: int, steps: int, warmup: int, threads: int) -> dict:
-    from oracle import oracle as O
-
+def oracle_net_of(O, w):
     net = O.OracleNet(w["S"])
     for k, e, d in w["reactions"]:
         if w.get("sparse"):  # Rate::lma_sparse: the reference's form for large networks
             net.add_lma_sparse(k, [(i, x) for i, x in enumerate(e) if x], d)
         else:
             net.add_lma(k, e, d)
+    return net
+
+
+def cpu_reference(w, n_traj: int, steps: int, warmup: int, threads: int) -> dict:
+    """The oracle port of the reference's CPU path: `steps` timed passes over
+    n_traj trajectories of workload w on `threads` threads."""
+    from oracle import oracle as O
+
+    net = oracle_net_of(O, w)
     tot_ev, tot_s = 0, 0.0
     for step in range(warmup + steps):
         seeds = seeds_for(0, 1000 + step, n_traj)
@@ -272,21 +279,36 @@ def cpu_reference(w, n_traj: int, steps: int, warmup: int, threads: int) -> dict
     return {"value": tot_ev / tot_s, "events": tot_ev, "seconds": tot_s}
 
 
+def oracle_build_flags() -> str:
+    from oracle import oracle as O
+
+    return " ".join(O.compile_flags())
+
+
+def workload_config(w, n: int) -> dict:
+    """The `config` both arms report for workload w at n trajectories."""
+    return {"workload": w["desc"], "n_traj": n, "nb_steps": w["nb_steps"], "tmax": w["tmax"],
+            "rng": "reference stream: xoshiro256++/SplitMix64 seeds, ziggurat Exp1",
+            "l2": "GPU arm: 256 MB written between timed steps (L2 flush)"}
+
+
 def run_reference_arm(args, w):
+    """The reference's CPU path (oracle port, all host cores) on the same
+    workload as the GPU arm: every step simulates all w['n_traj'] trajectories."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    n = args.cpu_sample or w["cpu_sample"]
+    n = args.n_traj or w["n_traj"]
     r = cpu_reference(w, n, args.steps, args.warmup, threads)
-    sample = (f"{n} of the {w['n_traj']} trajectories per step ({w['name']}), oracle port of the "
-              f"reference's CPU path, {threads} threads")
+    sample = (f"all {n} trajectories of the workload per step ({w['name']}), oracle port of the reference's "
+              f"CPU path, {threads} threads, gcc {oracle_build_flags()}")
     line = {
         "impl": "reference", "metric": "SSA reaction events/sec", "value": r["value"], "unit": "events/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * r["seconds"] / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64+int64", "data": "synthetic",
-        "config": {"workload": w["desc"], "n_traj": w["n_traj"], "sample_traj_per_step": n},
+        "config": workload_config(w, n),
         "cpu_baseline": {"value": r["value"], "unit": "events/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": r["value"], "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -322,7 +344,8 @@ MAPPINGS = {
                            "touches re-evaluated, float-pair scan, exact binary64 fold for close choices and "
                            "re-runs of undecided intervals"),
     4: ("rbg_net_kernel", "thread per trajectory, kernel generated for the network and compiled at run time "
-                          "(NVRTC); float-pair speculation with exact binary64 re-runs"),
+                          "(NVRTC); float-pair speculation with exact binary64 re-runs; lanes go to the "
+                          "trajectories whose clocks lag furthest behind"),
     3: ("ssa_spec_kernel", "thread per trajectory, packed-descriptor speculative kernel"),
     2: ("ssa_fast_kernel", "thread per trajectory, lockstep exact integer-binary64 kernel"),
     0: ("ssa_thread_kernel", "thread per trajectory, generic exact kernel"),
@@ -330,7 +353,8 @@ MAPPINGS = {
 
 
 def read_profile(kernel: str, workload: str) -> dict:
-    """Per-launch figures (``key: value`` lines) of the committed ncu summary."""
+    """Per-launch figures (``key: value`` lines) of the committed ncu summary
+    of `kernel` on `workload` (profiles/<kernel>_<workload>.md)."""
     p = ROOT / "profiles" / f"{kernel}_{workload}.md"
     out = {}
     if not p.exists():
@@ -345,6 +369,157 @@ def read_profile(kernel: str, workload: str) -> dict:
     return out
 
 
+def hbm_peak() -> tuple[float, str]:
+    """Measured HBM copy bandwidth (GB/s) of the GB300s, else the fallback."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback 6.8 TB/s (of fallback)"
+
+
+def roofline(kname: str, wname: str, events_per_launch: float, launch_s: float, sample_bytes: float,
+             sm_mhz, sms: int, fe: int, dfma_per_s: float | None) -> dict:
+    """Roofline of the dominant kernel.  The SSA is a chain of dependent steps
+    per trajectory with no reuse to stage: the bound is instruction issue
+    (4 schedulers x 32 lanes per SM per clock) over the thread instructions the
+    kernel executes per event, measured by ncu on the same kernel and workload
+    (the committed profile).  HBM carries only the samples (algorithmic bytes:
+    the sample array written once); the FP64-equivalent figure is the direct
+    method's binary64 work per event against the DFMA rate measured live, a
+    speed-up over an FP64-pipe-bound kernel, not a roofline fraction."""
+    prof = read_profile(kname, wname)
+    out = {"bound": "issue", "achieved": None, "peak": None, "unit": "T thread-instructions/s", "frac": None,
+           "traffic": prof.get("traffic_bytes_per_launch"), "kernel": kname}
+    tipe = prof.get("thread_inst_per_event")
+    if tipe and sm_mhz:
+        peak = sms * 4 * 32 * sm_mhz * 1e6 / 1e12
+        ach = tipe * events_per_launch / launch_s / 1e12
+        out.update(achieved=ach, peak=peak, frac=ach / peak, thread_inst_per_event=tipe,
+                   peak_source=f"{sms} SMs x 4 schedulers x 32 lanes x the SM clock sampled in this run",
+                   inst_source=f"profiles/{kname}_{wname}.md (ncu, same kernel and workload)")
+    hp, hsrc = hbm_peak()
+    out["hbm"] = {"algorithmic_bytes": sample_bytes, "achieved_gbs": sample_bytes / launch_s / 1e9,
+                  "peak_gbs": hp, "frac": sample_bytes / launch_s / 1e9 / hp, "peak_source": hsrc,
+                  "traffic_vs_algorithmic": (prof["traffic_bytes_per_launch"] / sample_bytes
+                                             if prof.get("traffic_bytes_per_launch") and sample_bytes else None)}
+    if dfma_per_s:
+        ach64 = events_per_launch * fe / launch_s / 1e9
+        out["fp64_equivalent"] = {"ops_per_event": fe, "achieved_gops": ach64, "dfma_rate_gops": dfma_per_s / 1e9,
+                                  "speedup_over_fp64_pipe": ach64 / (dfma_per_s / 1e9),
+                                  "note": "binary64 work done exactly on the FP32/integer pipes"}
+    return out
+
+
+def measure_workload(args, w, steps: int, warmup: int, n: int | None = None, dist=None, rank: int = 0,
+                     local: int = 0, cpu: bool = True, fp64_rate: bool = False) -> dict:
+    """Device time (HBM-resident inputs, L2 flushed between steps) and end to
+    end time (C-ABI host call from page-locked buffers, copies inside) of
+    `steps` passes over workload w; the CPU port on a bounded sample beside it."""
+    import torch
+
+    import rebop_gb300 as rb
+    from rebop_gb300._lib import lib as rblib
+
+    world = 1 if dist is None else dist.get_world_size()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    net = rb.Network(w["S"])
+    for k, e, d in w["reactions"]:
+        net.add_reaction(rb.Rate.lma(k, e), d)
+    n = n or w["n_traj"]
+    NT, S = w["nb_steps"] + 1, w["S"]
+    stream = torch.cuda.current_stream()
+    sid = stream.cuda_stream
+    d_x0 = torch.tensor(w["x0"], dtype=torch.int64, device="cuda")
+    d_seeds = [torch.from_numpy(shard_seeds(rank, s, n).view(np.int64)).cuda() for s in range(warmup + steps)]
+    d_out = torch.empty((NT, S, n), dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def launch(seeds):
+        net.run_ensemble_device(n, d_x0.data_ptr(), False, seeds.data_ptr(), w["tmax"], w["nb_steps"],
+                                d_out.data_ptr(), stream=sid)
+
+    for s in range(warmup):
+        launch(d_seeds[s])
+    torch.cuda.synchronize()
+    dfma = rblib.rbg_internal_fp64_fma_rate(sid) if fp64_rate else None  # DFMA instructions / s, live
+
+    vis = [v for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    clocks = ClockSampler(int(vis[local]) if local < len(vis) and vis[local].strip().isdigit() else local)
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    events_per_step = []
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    for s in range(steps):
+        flush.zero_()  # L2 flush between timed steps (256 MB > 129 MB L2)
+        ev0[s].record(stream)
+        launch(d_seeds[warmup + s])
+        ev1[s].record(stream)
+        events_per_step.append(net.last_events())
+    torch.cuda.synchronize()
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    dev_s = sum(step_ms) / 1e3
+    ev_total = sum(events_per_step)
+    dev_s_all, ev_all = reduce_over_ranks(dist, dev_s, float(ev_total), "cuda")
+
+    # end to end: the C-ABI host call with page-locked buffers, copies in the timed region
+    pin_out = torch.empty((NT, S, n), dtype=torch.int64, pin_memory=True).numpy()
+    pin_seeds = [torch.from_numpy(seeds_for(rank, 500 + s, n).view(np.int64)).pin_memory().numpy().view(np.uint64)
+                 for s in range(steps + 1)]
+    x0_host = np.asarray(w["x0"], dtype=np.int64)
+    net.run_ensemble(x0_host, pin_seeds[0], w["tmax"], w["nb_steps"], out=pin_out, want_events=False)
+    barrier()
+    e2e_ev, e2e_s, h2d, d2h, k_ms = 0, 0.0, 0, 0, 0.0
+    for s in range(steps):
+        t0 = time.perf_counter()
+        res = net.run_ensemble(x0_host, pin_seeds[1 + s], w["tmax"], w["nb_steps"], out=pin_out,
+                               want_events=False)
+        e2e_s += time.perf_counter() - t0
+        e2e_ev += res.total_events
+        h2d, d2h = res.stats["h2d_bytes"], res.stats["d2h_bytes"]
+        k_ms += res.stats["kernel_ms"]
+    clk = clocks.stop()
+    e2e_s_all, e2e_ev_all = reduce_over_ranks(dist, e2e_s, float(e2e_ev), "cuda")
+
+    mapping = int(res.stats["mapping"])
+    kname, kdesc = MAPPINGS.get(mapping, ("?", "?"))
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    rl = roofline(kname, w["name"], ev_total / steps, dev_s / steps, NT * S * n * 8.0, clk.get("sm_mhz"), sms,
+                  f_event(w), dfma)
+
+    cpu_b = None
+    if cpu and rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        nb = args.cpu_sample or w["cpu_sample"]
+        r = cpu_reference(w, nb, 1, 0, threads)
+        # one core as well, on a sample of about a second
+        n1 = max(1, min(nb, int(nb * 1.0 / max(r["seconds"] * threads, 1e-9))))
+        r1 = cpu_reference(w, n1, 1, 0, 1)
+        cpu_b = {"value": r["value"], "unit": "events/s", "cores": threads, "kind": "port",
+                 "sample": f"{nb} trajectories of the same workload, oracle port of the reference CPU path, "
+                           f"{threads} threads, gcc {oracle_build_flags()}",
+                 "value_1core": r1["value"], "sample_1core": f"{n1} trajectories on one thread"}
+    return {
+        "value": ev_all / dev_s_all, "unit": "events/s", "steps": steps, "warmup": warmup,
+        "ms_per_step": 1e3 * dev_s_all / steps, "events_per_step": ev_total / steps, "wall_s": t_wall,
+        "e2e": {"value": e2e_ev_all / e2e_s_all, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s / steps,
+                "kernel_ms_per_step": k_ms / steps},
+        "gpu_launches": steps, "roofline": rl, "cpu_baseline": cpu_b, "clocks": clk,
+        "kernel": kname, "mapping": kdesc, "n_traj": n,
+        "_net": net, "_x0": x0_host, "_world": world,
+    }
+
+
 def run_ours(args, w):
     import torch
 
@@ -357,110 +532,8 @@ def run_ours(args, w):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    import rebop_gb300 as rb
-    from rebop_gb300._lib import lib as rblib
-
-    net = rb.Network(w["S"])
-    for k, e, d in w["reactions"]:
-        net.add_reaction(rb.Rate.lma(k, e), d)
-    n = args.n_traj or w["n_traj"]
-    NT, S = w["nb_steps"] + 1, w["S"]
-    stream = torch.cuda.current_stream()
-    sid = stream.cuda_stream
-    d_x0 = torch.tensor(w["x0"], dtype=torch.int64, device="cuda")
-    d_seeds = [torch.from_numpy(shard_seeds(rank, s, n).view(np.int64)).cuda()
-               for s in range(args.warmup + args.steps)]
-    d_out = torch.empty((NT, S, n), dtype=torch.int64, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def launch(seeds):
-        net.run_ensemble_device(n, d_x0.data_ptr(), False, seeds.data_ptr(), w["tmax"], w["nb_steps"],
-                                d_out.data_ptr(), stream=sid)
-
-    for s in range(args.warmup):
-        launch(d_seeds[s])
-    torch.cuda.synchronize()
-    peak_ops = rblib.rbg_internal_fp64_fma_rate(sid)  # DFMA instructions / s, measured live
-
-    vis = [v for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
-    clocks = ClockSampler(int(vis[local]) if local < len(vis) and vis[local].strip().isdigit() else local)
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    events_per_step = []
-    barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    t_wall0 = time.perf_counter()
-    for s in range(args.steps):
-        flush.zero_()  # L2 flush between timed steps (256 MB > 129 MB L2)
-        ev0[s].record(stream)
-        launch(d_seeds[args.warmup + s])
-        ev1[s].record(stream)
-        events_per_step.append(net.last_events())
-    torch.cuda.synchronize()
-    barrier()
-    t_wall = time.perf_counter() - t_wall0
-    clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
-    dev_s = sum(step_ms) / 1e3
-    ev_total = sum(events_per_step)
-    dev_s_all, ev_all = reduce_over_ranks(dist, dev_s, float(ev_total), "cuda")
-    value = ev_all / dev_s_all
-
-    # e2e: the C-ABI host call with page-locked buffers, copies in the timed region.
-    pin_out = torch.empty((NT, S, n), dtype=torch.int64, pin_memory=True).numpy()
-    pin_seeds = [torch.from_numpy(seeds_for(rank, 500 + s, n).view(np.int64)).pin_memory().numpy().view(np.uint64)
-                 for s in range(args.steps + 1)]
-    x0_host = np.asarray(w["x0"], dtype=np.int64)
-    net.run_ensemble(x0_host, pin_seeds[0], w["tmax"], w["nb_steps"], out=pin_out, want_events=False)
-    barrier()
-    e2e_ev, e2e_s, h2d, d2h = 0, 0.0, 0, 0
-    for s in range(args.steps):
-        t0 = time.perf_counter()
-        res = net.run_ensemble(x0_host, pin_seeds[1 + s], w["tmax"], w["nb_steps"], out=pin_out,
-                               want_events=False)
-        e2e_s += time.perf_counter() - t0
-        e2e_ev += res.total_events
-        h2d, d2h = res.stats["h2d_bytes"], res.stats["d2h_bytes"]
-    e2e_s, e2e_ev = reduce_over_ranks(dist, e2e_s, float(e2e_ev), "cuda")
-    e2e_value = e2e_ev / e2e_s
-
-    # roofline of the dominant kernel: the binary64 work of the direct method
-    # against the FP64 pipe, and the instruction issue the kernel really needs
-    mapping = int(res.stats["mapping"])
-    kname, kdesc = MAPPINGS.get(mapping, ("?", "?"))
-    prof = read_profile(kname, w["name"])
-    avg_launch_s = dev_s / args.steps
-    fe = f_event(w)
-    achieved = (ev_total / args.steps) * fe / avg_launch_s / 1e9
-    peak = peak_ops / 1e9
-    traffic = prof.get("traffic_bytes_per_launch")
-    issue = None
-    if "thread_inst_per_event" in prof and clk.get("sm_mhz"):
-        sms = torch.cuda.get_device_properties(local).multi_processor_count
-        i_peak = sms * 4 * 32 * clk["sm_mhz"] * 1e6 / 1e12  # thread instructions / s (4 schedulers per SM)
-        i_ach = prof["thread_inst_per_event"] * (ev_total / args.steps) / avg_launch_s / 1e12
-        issue = {"achieved": i_ach, "peak": i_peak, "unit": "T thread-instructions/s", "frac": i_ach / i_peak,
-                 "thread_inst_per_event": prof["thread_inst_per_event"],
-                 "source": f"profiles/{kname}_{w['name']}.md (ncu) and the SM clock sampled in this run"}
-
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        nb = args.cpu_sample or w["cpu_sample"]
-        r = cpu_reference(w, nb, 1, 0, threads)
-        # one core as well, on a sample of about a second
-        n1 = max(1, min(nb, int(nb * 1.0 / max(r["seconds"] * threads, 1e-9))))
-        r1 = cpu_reference(w, n1, 1, 0, 1)
-        cpu = {"value": r["value"], "unit": "events/s", "cores": threads, "kind": "port",
-               "sample": f"{nb} trajectories of the same workload, oracle port of the reference CPU path, "
-                         f"{threads} threads",
-               "value_1core": r1["value"], "sample_1core": f"{n1} trajectories on one thread"}
+    m = measure_workload(args, w, args.steps, args.warmup, n=args.n_traj or None, dist=dist, rank=rank,
+                         local=local, cpu=not args.no_cpu_baseline, fp64_rate=True)
 
     calib = None
     if rank == 0 and w.get("calib_n"):
@@ -468,6 +541,7 @@ def run_ours(args, w):
         # host API (host buffers, copies inside the timed region)
         nc = int(w["calib_n"])
         cs = seeds_for(rank, 900, nc)
+        net, x0_host = m["_net"], m["_x0"]
         net.run_ensemble(x0_host, cs, w["tmax"], w["nb_steps"], want_events=False)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -483,35 +557,44 @@ def run_ours(args, w):
             r1 = cpu_reference(w, 16, 1, 0, 1)
             calib["cpu_port_1thread_ms_per_traj"] = 1e3 * r1["seconds"] / 16
 
+    # the other configurations, a few steps each, beside the headline (one GPU only)
+    subs = {}
+    if rank == 0 and world == 1 and args.workloads != "none":
+        for name in [x for x in args.workloads.split(",") if x and x != w["name"]]:
+            if name == "batch":
+                subs[name] = measure_batch(args, min(args.steps, 3), min(args.warmup, 2),
+                                           cpu=not args.no_cpu_baseline)
+            else:
+                sw = WORKLOADS[name]
+                st, wu = SUB_STEPS.get(name, (3, 2))
+                r = measure_workload(args, sw, min(args.steps, st), min(args.warmup, wu),
+                                     cpu=not args.no_cpu_baseline)
+                r["config"] = workload_config(sw, r["n_traj"])
+                subs[name] = {k: v for k, v in r.items() if not k.startswith("_")}
+
     if rank == 0:
         line = {
-            "metric": "SSA reaction events/sec", "value": value, "unit": "events/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s_all / args.steps,
+            "metric": "SSA reaction events/sec", "value": m["value"], "unit": "events/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+int64",
             "data": "synthetic",
-            "config": {"workload": w["desc"], "n_traj_per_gpu": n, "events_per_step": ev_total / args.steps,
-                       "rng": "reference stream: xoshiro256++/SplitMix64 seeds, ziggurat Exp1",
-                       "mapping": kdesc, "kernel": kname, "l2": "flushed between steps (256 MB write)",
-                       "wall_s": t_wall},
-            "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": args.steps,
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "Gop/s (binary64)",
-                         "frac": achieved / peak if peak else None, "traffic": traffic,
-                         "ops_per_event": fe,
-                         "peak_source": "DFMA throughput measured live in this run (not in MEASURED_PEAKS.json)",
-                         "note": ("the kernel does the binary64 work exactly on the FP32 and integer pipes, so "
-                                  "frac > 1 is its gain over an FP64-pipe-bound kernel; 'issue' is the bound "
-                                  "it runs against"),
-                         "issue": issue},
-            "cpu_baseline": cpu,
-            "clocks": clk,
+            "config": workload_config(w, m["n_traj"]),
+            "events_per_step": m["events_per_step"], "kernel": m["kernel"], "mapping": m["mapping"],
+            "wall_s": m["wall_s"],
+            "e2e": m["e2e"], "gpu_launches": m["gpu_launches"], "roofline": m["roofline"],
+            "cpu_baseline": m["cpu_baseline"], "clocks": m["clocks"],
         }
         if calib is not None:
-            line["config"]["reference_benchmark_run"] = calib
+            line["reference_benchmark_run"] = calib
+        if subs:
+            line["workloads"] = subs
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+# steps / warm-up of the configurations run beside the headline
+SUB_STEPS = {"sir": (5, 3), "large": (2, 1), "vilar": (2, 1)}
 
 
 def _batch_cpu(items, every: int, traj: int, threads: int):
@@ -532,18 +615,59 @@ def _batch_cpu(items, every: int, traj: int, threads: int):
     return ev_tot / t_tot, ev_tot, t_tot
 
 
-def run_batch(args):
+def measure_batch(args, steps: int, warmup: int, cpu: bool = True) -> dict:
     import torch
 
     import rebop_gb300 as rb
 
     items = batch_items()
-    traj = BATCH["traj"]
+    b, nets = make_batch(rb, items)
+    n_thread, n_warp = b.plan()
+    for s in range(warmup):
+        b.run()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    dev_ms, wall, events, h2d, d2h, launches = 0.0, 0.0, 0, 0, 0, 0
+    for s in range(steps):
+        for j in range(len(items)):
+            b.seeds(j)[:] = batch_seeds(1 + s, j)
+        t0 = time.perf_counter()
+        st = b.run()
+        wall += time.perf_counter() - t0
+        dev_ms += st["kernel_ms"]
+        events += st["events"]
+        launches += st["kernel_launches"]
+        h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    cpu_b = None
+    if cpu:
+        threads = os.cpu_count() or 1
+        v, _, _ = _batch_cpu(items, BATCH["cpu_every"] * 4, BATCH["traj"], threads)
+        cpu_b = {"value": v, "unit": "events/s", "cores": threads, "kind": "port",
+                 "sample": f"every {BATCH['cpu_every'] * 4}th item of each kind, oracle port, {threads} threads"}
+    return {
+        "value": events / (dev_ms / 1e3), "unit": "events/s", "steps": steps, "warmup": warmup,
+        "ms_per_step": dev_ms / steps,
+        "config": {"workload": BATCH["desc"], "items": len(items), "trajectories": len(items) * BATCH["traj"],
+                   "events_per_step": events / steps, "thread_launches": n_thread, "warp_batch_items": n_warp,
+                   "timing": "device time of the replayed graph: input copy, kernels, result copy",
+                   "l2": "inputs and outputs far above L2 are copied in every step"},
+        "e2e": {"value": events / wall, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": launches, "cpu_baseline": cpu_b, "clocks": clk,
+    }
+
+
+def run_batch(args):
+    import torch
+
+    items = batch_items()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return
         threads = os.cpu_count() or 1
-        v, ev, t = _batch_cpu(items, BATCH["cpu_every"], traj, threads)
+        v, ev, t = _batch_cpu(items, BATCH["cpu_every"], BATCH["traj"], threads)
         print(json.dumps({"impl": "reference", "metric": "SSA reaction events/sec", "value": v, "unit": "events/s",
                           "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * t,
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+int64",
@@ -554,41 +678,10 @@ def run_batch(args):
                                   "d2h_bytes_per_step": 0}}), flush=True)
         return
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    b, nets = make_batch(rb, items)
-    n_thread, n_warp = b.plan()
-    for s in range(args.warmup):
-        b.run()
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    clocks.start()
-    dev_ms, wall, events, h2d, d2h = 0.0, 0.0, 0, 0, 0
-    for s in range(args.steps):
-        for j in range(len(items)):
-            b.seeds(j)[:] = batch_seeds(1 + s, j)
-        t0 = time.perf_counter()
-        st = b.run()
-        wall += time.perf_counter() - t0
-        dev_ms += st["kernel_ms"]
-        events += st["events"]
-        h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
-    clk = clocks.stop()
-    cpu = None
-    if not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        v, _, _ = _batch_cpu(items, BATCH["cpu_every"] * 4, traj, threads)
-        cpu = {"value": v, "unit": "events/s", "cores": threads, "kind": "port",
-               "sample": f"every {BATCH['cpu_every'] * 4}th item of each kind, oracle port, {threads} threads"}
-    print(json.dumps({
-        "metric": "SSA reaction events/sec", "value": events / (dev_ms / 1e3), "unit": "events/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64+int64", "data": "synthetic",
-        "config": {"workload": BATCH["desc"], "items": len(items), "trajectories": len(items) * traj,
-                   "events_per_step": events / args.steps, "thread_launches": n_thread, "warp_batch_items": n_warp,
-                   "timing": "device time of the replayed graph: input copy, kernels, result copy",
-                   "l2": "inputs and outputs far above L2 are copied in every step"},
-        "e2e": {"value": events / wall, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": args.steps * (n_thread + (1 if n_warp else 0)),
-        "cpu_baseline": cpu, "clocks": clk}), flush=True)
+    m = measure_batch(args, args.steps, args.warmup, cpu=not args.no_cpu_baseline)
+    line = {"metric": "SSA reaction events/sec", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64+int64", "data": "synthetic", **m}
+    print(json.dumps(line), flush=True)
 
 
 SURROGATE = dict(
@@ -705,6 +798,8 @@ def main():
     ap.add_argument("--n-traj", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workloads", default="sir,large,batch",
+                    help="configurations measured beside the headline (comma list, or 'none')")
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch(args)

@@ -25,17 +25,30 @@ BUILD_DIR = HERE / "_build"
 LIB_PATH = BUILD_DIR / "libssa_oracle.so"
 
 
+def compile_flags() -> list[str]:
+    """gcc flags of the oracle: optimised for the host CPU it runs on (the
+    CPU baseline is timed there), never contracting a*b+c or reassociating,
+    so results stay the reference's binary64 results on any host."""
+    import platform
+
+    tune = "-mcpu=native" if platform.machine().lower() in ("aarch64", "arm64") else "-march=native"
+    return ["-O3", tune, "-ffp-contract=off", "-fno-fast-math"]
+
+
 def build(force: bool = False) -> Path:
-    """Compile ssa_oracle.c into a shared library (gcc, -ffp-contract=off)."""
+    """Compile ssa_oracle.c into a shared library (gcc, compile_flags())."""
     src = HERE / "ssa_oracle.c"
-    if LIB_PATH.exists() and not force and LIB_PATH.stat().st_mtime >= src.stat().st_mtime:
+    stamp = BUILD_DIR / "flags.txt"
+    flags = compile_flags()
+    if (LIB_PATH.exists() and not force and LIB_PATH.stat().st_mtime >= src.stat().st_mtime
+            and stamp.exists() and stamp.read_text() == " ".join(flags)):
         return LIB_PATH
     BUILD_DIR.mkdir(exist_ok=True)
     tmp = LIB_PATH.with_suffix(f".{os.getpid()}.tmp")
-    cmd = ["gcc", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
-           "-o", str(tmp), str(src), "-lm"]
+    cmd = ["gcc", *flags, "-fPIC", "-shared", "-pthread", "-o", str(tmp), str(src), "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB_PATH)
+    stamp.write_text(" ".join(flags))
     return LIB_PATH
 
 
