@@ -443,6 +443,13 @@ def measure_workload(args, w, steps: int, warmup: int, n: int | None = None, dis
         net.run_ensemble_device(n, d_x0.data_ptr(), False, seeds.data_ptr(), w["tmax"], w["nb_steps"],
                                 d_out.data_ptr(), stream=sid)
 
+    # the autotuner picks the kernel and launch shape for this network and
+    # ensemble size (pilot runs, outside the timed region)
+    tuning = None
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        tr = net.tune(w["x0"], n, w["tmax"], w["nb_steps"])
+        tuning = {"best": tr["best"], "trials": tr["trials"], "seconds": time.perf_counter() - t0}
     for s in range(warmup):
         launch(d_seeds[s])
     torch.cuda.synchronize()
@@ -515,7 +522,7 @@ def measure_workload(args, w, steps: int, warmup: int, n: int | None = None, dis
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s / steps,
                 "kernel_ms_per_step": k_ms / steps},
         "gpu_launches": steps, "roofline": rl, "cpu_baseline": cpu_b, "clocks": clk,
-        "kernel": kname, "mapping": kdesc, "n_traj": n,
+        "kernel": kname, "mapping": kdesc, "n_traj": n, "tuning": tuning,
         "_net": net, "_x0": x0_host, "_world": world,
     }
 
@@ -582,7 +589,7 @@ def run_ours(args, w):
             "events_per_step": m["events_per_step"], "kernel": m["kernel"], "mapping": m["mapping"],
             "wall_s": m["wall_s"],
             "e2e": m["e2e"], "gpu_launches": m["gpu_launches"], "roofline": m["roofline"],
-            "cpu_baseline": m["cpu_baseline"], "clocks": m["clocks"],
+            "cpu_baseline": m["cpu_baseline"], "clocks": m["clocks"], "tuning": m["tuning"],
         }
         if calib is not None:
             line["reference_benchmark_run"] = calib
@@ -798,6 +805,7 @@ def main():
     ap.add_argument("--n-traj", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner's pilot runs")
     ap.add_argument("--workloads", default="sir,large,batch",
                     help="configurations measured beside the headline (comma list, or 'none')")
     args = ap.parse_args()

@@ -194,6 +194,41 @@ int rb_ensemble_run_device_noalloc(const rb_network *net, int64_t n_traj, const 
  * of its time budget. */
 int rb_ensemble_last_events(const rb_network *net, uint64_t *events);
 
+/* ------------------------------------------------------------ autotuner ---
+ * No counterpart in the reference, which has one CPU code path.  The kernels
+ * that can run an ensemble map it differently (a kernel generated for the
+ * network, the speculative kernel over the packed descriptor, the lockstep
+ * exact kernel -- a thread per trajectory -- or a warp per trajectory), and
+ * the fastest, with its block size, phase length and slot scheduler, depends
+ * on the network and the ensemble.  rb_ensemble_tune times pilot runs of this
+ * workload (the arguments of rb_ensemble_run, internal seeds) for every
+ * kernel that covers it, then the launch shapes of the fastest, and keeps the
+ * winner for networks of the same shape (species, reactions, reactant
+ * orders, macro arithmetic, log2 of the trajectory count, per-trajectory
+ * rates) on this GPU, in memory and in a cache file ($RB_TUNE_CACHE, default
+ * $HOME/.cache/rebop_gb300/tune_cache.txt).  Later runs of such networks use
+ * it (RB_TUNE=0: never).  Results are the same bit for bit whichever kernel
+ * runs. */
+typedef struct {
+    int32_t mapping;      /* rb_run_stats.mapping code of the kernel */
+    int32_t block;        /* lanes per block of the generated kernel (0: 384) */
+    int32_t phase_steps;  /* steps per phase of the speculative kernels (0: 128) */
+    int32_t sched;        /* their slot scheduler: 0 lagging clocks first, 1 rotation, -1 default */
+    double ms;            /* pilot run time (best of two); < 0: the shape failed */
+} rb_tune_result;
+/* best: the winner; trials[0 .. min(max_trials, *n_trials)): every shape timed. */
+int rb_ensemble_tune(const rb_network *net, int64_t n_traj, const int64_t *x0, int32_t x0_per_traj,
+                     const double *rates, int32_t rates_per_traj, double tmax, int64_t nb_steps,
+                     rb_tune_result *best, rb_tune_result *trials, int32_t max_trials, int32_t *n_trials);
+/* The remembered shape for this network and ensemble size on the current GPU
+ * (RB_ERR_INVALID: none). */
+int rb_tune_lookup(const rb_network *net, int64_t n_traj, int32_t rates_per_traj, rb_tune_result *out);
+/* Path of the cache file (length returned; copied NUL-terminated into buf). */
+size_t rb_tune_cache_path(char *buf, size_t len);
+/* Forget the tuned shapes held in memory (the next lookup reads the cache file
+ * again), and delete the cache file when remove_file. */
+void rb_tune_clear(int32_t remove_file);
+
 /* Every-event run of one trajectory, src/pyo3_gillespie.rs:209-223: records
  * (t, saved species) at t = 0 and after each reaction while t < tmax; the
  * last record is the first event at or after tmax, or t = +inf when the

@@ -33,6 +33,19 @@ class RunStats(C.Structure):
     ]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [
+        ("mapping", C.c_int32),
+        ("block", C.c_int32),
+        ("phase_steps", C.c_int32),
+        ("sched", C.c_int32),
+        ("ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class EngineError(RuntimeError):
     """A CUDA or resource failure inside the engine."""
 
@@ -88,6 +101,16 @@ _SIGS = {
     "rb_batch_run": ([_vp, P(RunStats)], C.c_int),
     "rb_batch_plan": ([_vp, P(_i32), P(_i32)], C.c_int),
     "rb_batch_item_mapping": ([_vp, _i32, P(_i32)], C.c_int),
+    "rb_ensemble_tune": ([_vp, _i64, P(_i64), _i32, P(_f64), _i32, _f64, _i64, P(TuneResult), P(TuneResult),
+                          _i32, P(_i32)], C.c_int),
+    "rb_tune_lookup": ([_vp, _i64, _i32, P(TuneResult)], C.c_int),
+    "rb_tune_cache_path": ([_cp, _sz], _sz),
+    "rb_tune_clear": ([_i32], None),
+    "rbg_internal_tune_key": ([_vp, _i32, _cp, _i64, _i32, _cp, _sz], C.c_int),
+    "rbg_internal_tune_candidates": ([_vp, _i32, _sz, _i64, _i64, _f64, _i32, _i32, P(TuneResult), P(TuneResult),
+                                      _i32, P(_i32)], C.c_int),
+    "rbg_internal_tune_store": ([_cp, P(TuneResult)], C.c_int),
+    "rbg_internal_tune_get": ([_cp, P(TuneResult)], C.c_int),
     "rb_gillespie_new": ([P(_i64), _i32, _i32, P(_vp)], C.c_int),
     "rb_gillespie_new_with_seed": ([P(_i64), _i32, _i32, _u64, P(_vp)], C.c_int),
     "rb_gillespie_free": ([_vp], None),

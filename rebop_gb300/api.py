@@ -15,7 +15,7 @@ from typing import Iterable, Sequence
 
 import numpy as np
 
-from ._lib import RunStats, check, lib, ptr
+from ._lib import RunStats, TuneResult, check, lib, ptr
 
 _u32, _i64, _u64, _f64, _i32 = C.c_uint32, C.c_int64, C.c_uint64, C.c_double, C.c_int32
 
@@ -274,6 +274,36 @@ class Network:
                                          float(tmax), int(nb_steps), ptr(save_arr, _i32), n_save,
                                          out_ptr or None, events_ptr or None, final_ptr or None,
                                          stream or None))
+
+    def tune(self, x0, n_traj: int, tmax: float, nb_steps: int, *, rates=None) -> dict:
+        """Autotune the kernel and launch shape for ensembles of this network
+        (``rb_ensemble_tune``): pilot runs of ``n_traj`` trajectories from
+        ``x0`` (one count vector or one per trajectory) with ``rates`` (None,
+        one vector, or one per trajectory).  The winner is remembered for
+        networks of this shape on this GPU and used by later runs.  Returns
+        ``{"best": {...}, "trials": [...]}`` (times in ms)."""
+        S = self.nb_species
+        x0 = _i64a(np.asarray(x0, dtype=np.int64))
+        x0_per = 1 if x0.ndim == 2 else 0
+        if x0.size != (n_traj * S if x0_per else S):
+            raise ValueError("x0 must have one count per species, or one row per trajectory")
+        r_arr, r_per = None, 0
+        if rates is not None:
+            r_arr = np.ascontiguousarray(np.asarray(rates, dtype=np.float64))
+            r_per = 1 if r_arr.ndim == 2 else 0
+        best = TuneResult()
+        trials = (TuneResult * 64)()
+        n = C.c_int32()
+        check(lib.rb_ensemble_tune(self._h, int(n_traj), ptr(x0, _i64), x0_per, ptr(r_arr, _f64), r_per,
+                                   float(tmax), int(nb_steps), C.byref(best), trials, 64, C.byref(n)))
+        return {"best": best.as_dict(), "trials": [trials[k].as_dict() for k in range(min(n.value, 64))]}
+
+    def tuned(self, n_traj: int, *, rates_per_traj: bool = False) -> dict | None:
+        """The remembered shape for this network at ``n_traj`` trajectories, or None."""
+        out = TuneResult()
+        if lib.rb_tune_lookup(self._h, int(n_traj), int(bool(rates_per_traj)), C.byref(out)) != 0:
+            return None
+        return out.as_dict()
 
     def last_events(self) -> int:
         v = C.c_uint64()

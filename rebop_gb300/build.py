@@ -23,7 +23,7 @@ LIB = BUILD / "librebop_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["ssa_thread.cu", "ssa_fast.cu", "ssa_spec.cu", "ssa_warp.cu", "fp64_peak.cu", "mdn.cu"]
-CXX_SOURCES = ["network.cpp", "engine.cpp", "capi.cpp", "ssa_jit.cpp", "batch.cpp"]
+CXX_SOURCES = ["network.cpp", "engine.cpp", "capi.cpp", "ssa_jit.cpp", "batch.cpp", "tune.cpp"]
 # Device headers embedded in the library for run-time network compilation.
 JIT_HEADERS = ["rtc_types.hpp", "ssa_args.hpp", "b64.cuh", "rng.cuh", "ssa_exact.cuh", "ssa_spec_body.cuh"]
 JIT_SOURCES_CPP = "jit_headers.cpp"

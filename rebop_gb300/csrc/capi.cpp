@@ -12,6 +12,7 @@
 #include "batch.hpp"
 #include "ssa_jit.hpp"
 #include "network.hpp"
+#include "tune.hpp"
 
 using rbg::set_error;
 
@@ -412,7 +413,8 @@ int rb_ensemble_run(const rb_network *netp, int64_t n_traj, const int64_t *x0, i
     // count, per row, the trajectories whose samples are written (after a
     // fence), and rows every trajectory has written are copied on a second
     // stream; the rest follow the kernel.
-    const bool stream_rows = !out_host && N && NS && NT < 65536;
+    const char *srows = std::getenv("RB_STREAM_ROWS");  // 0: copy every row after the kernel
+    const bool stream_rows = !out_host && N && NS && NT < 65536 && !(srows && std::strcmp(srows, "0") == 0);
     unsigned int *row_done = reinterpret_cast<unsigned int *>(b + o_rows);
     if (stream_rows) {
         r.row_done = row_done;
@@ -810,6 +812,127 @@ int rb_batch_item_mapping(const rb_batch *b, int32_t item, int32_t *mapping) {
     if (!b || !mapping || item < 0 || item >= (int32_t)b->b.items.size())
         return fail(RB_ERR_INVALID, "item index out of range");
     *mapping = b->b.items[item].mapping;
+    return RB_OK;
+}
+
+// ---------------------------------------------------------------- autotuner
+static void shape_out(const rbg::LaunchShape &s, double ms, rb_tune_result *o) {
+    o->mapping = s.kernel;
+    o->block = s.block;
+    o->phase_steps = s.phase;
+    o->sched = s.sched;
+    o->ms = ms;
+}
+
+int rb_ensemble_tune(const rb_network *netp, int64_t n_traj, const int64_t *x0, int32_t x0_per_traj,
+                     const double *rates, int32_t rates_per_traj, double tmax, int64_t nb_steps,
+                     rb_tune_result *best, rb_tune_result *trials, int32_t max_trials, int32_t *n_trials) {
+    if (!netp) return fail(RB_ERR_INVALID, "null network");
+    const rbg::Network &net = netp->net;
+    if (n_traj < 1) return fail(RB_ERR_INVALID, "tuning needs at least one trajectory");
+    if (nb_steps < 1) return fail(RB_ERR_INVALID, "nb_steps must be >= 1");
+    if (net.n_species && !x0) return fail(RB_ERR_INVALID, "null x0");
+    if (max_trials > 0 && !trials) return fail(RB_ERR_INVALID, "null trials");
+    std::lock_guard<std::mutex> lk(net.mu);
+    rbg::LaunchShape b;
+    double ms = 0;
+    std::vector<rbg::TuneTrial> tr;
+    if (!rbg::tune_ensemble(net, n_traj, x0, x0_per_traj != 0, rates, rates_per_traj != 0, tmax, nb_steps, b, ms, tr))
+        return RB_ERR_CUDA;
+    if (best) shape_out(b, ms, best);
+    for (int32_t k = 0; k < max_trials && k < (int32_t)tr.size(); k++) shape_out(tr[k].shape, tr[k].ms, trials + k);
+    if (n_trials) *n_trials = (int32_t)tr.size();
+    return RB_OK;
+}
+
+int rb_tune_lookup(const rb_network *netp, int64_t n_traj, int32_t rates_per_traj, rb_tune_result *out) {
+    if (!netp || !out) return fail(RB_ERR_INVALID, "null argument");
+    rbg::DeviceCtx *ctx = rbg::device_ctx();
+    if (!ctx) return RB_ERR_CUDA;
+    rbg::Packed p;
+    {
+        std::lock_guard<std::mutex> lk(netp->net.mu);
+        p = netp->net.pack();
+    }
+    rbg::LaunchShape s;
+    double ms = 0;
+    if (!rbg::tune_get(rbg::tune_key(p, ctx->sm_count, ctx->name, n_traj, rates_per_traj != 0), s, &ms))
+        return fail(RB_ERR_INVALID, "no tuned shape for this network and ensemble size");
+    shape_out(s, ms, out);
+    return RB_OK;
+}
+
+size_t rb_tune_cache_path(char *buf, size_t len) {
+    const std::string path = rbg::tune_cache_path();
+    if (buf && len) {
+        const size_t n = std::min(len - 1, path.size());
+        std::memcpy(buf, path.data(), n);
+        buf[n] = 0;
+    }
+    return path.size();
+}
+
+void rb_tune_clear(int32_t remove_file) { rbg::tune_clear(remove_file != 0); }
+
+// The tuner's cache key and the candidate shapes of one stage, for a device
+// with `sm_count` SMs and `smem_optin` bytes of shared memory per block named
+// `gpu` (no GPU needed).  best: the best shape so far (stages 1, 2).
+int rbg_internal_tune_key(const rb_network *netp, int32_t sm_count, const char *gpu, int64_t n_traj,
+                          int32_t rates_per_traj, char *buf, size_t len) {
+    if (!netp || !gpu) return fail(RB_ERR_INVALID, "null argument");
+    rbg::Packed p;
+    {
+        std::lock_guard<std::mutex> lk(netp->net.mu);
+        p = netp->net.pack();
+    }
+    return copy_name(rbg::tune_key(p, sm_count, gpu, n_traj, rates_per_traj != 0), buf, len);
+}
+
+int rbg_internal_tune_candidates(const rb_network *netp, int32_t sm_count, size_t smem_optin, int64_t n_traj,
+                                 int64_t nb_steps, double tmax, int32_t rates_per_traj, int32_t stage,
+                                 const rb_tune_result *best, rb_tune_result *out, int32_t cap, int32_t *n_out) {
+    if (!netp || !n_out) return fail(RB_ERR_INVALID, "null argument");
+    rbg::Packed p;
+    {
+        std::lock_guard<std::mutex> lk(netp->net.mu);
+        p = netp->net.pack();
+    }
+    rbg::DeviceCtx ctx;
+    ctx.sm_count = sm_count;
+    ctx.smem_optin = smem_optin;
+    const rbg::Feasible f = rbg::feasible_kernels(p, ctx, n_traj, nb_steps + 1, std::isfinite(tmax) && tmax >= 0,
+                                                   tmax, rates_per_traj != 0);
+    rbg::LaunchShape b;
+    if (best) {
+        b.kernel = best->mapping;
+        b.block = best->block;
+        b.phase = best->phase_steps;
+        b.sched = best->sched;
+    }
+    const auto c = rbg::tune_candidates(f, stage, b);
+    for (int32_t k = 0; k < cap && k < (int32_t)c.size(); k++) shape_out(c[k], 0, out + k);
+    *n_out = (int32_t)c.size();
+    return RB_OK;
+}
+
+// Record a tuned shape under a key (tests of the cache file).
+int rbg_internal_tune_store(const char *key, const rb_tune_result *s) {
+    if (!key || !s) return fail(RB_ERR_INVALID, "null argument");
+    rbg::LaunchShape l;
+    l.kernel = s->mapping;
+    l.block = s->block;
+    l.phase = s->phase_steps;
+    l.sched = s->sched;
+    rbg::tune_store(key, l, s->ms);
+    return RB_OK;
+}
+
+int rbg_internal_tune_get(const char *key, rb_tune_result *out) {
+    if (!key || !out) return fail(RB_ERR_INVALID, "null argument");
+    rbg::LaunchShape l;
+    double ms = 0;
+    if (!rbg::tune_get(key, l, &ms)) return fail(RB_ERR_INVALID, "no entry");
+    shape_out(l, ms, out);
     return RB_OK;
 }
 

@@ -1,6 +1,7 @@
 // Host engine implementation.
 #include "engine.hpp"
 #include "ssa_jit.hpp"
+#include "tune.hpp"
 
 #include <cmath>
 #include <cstdlib>
@@ -75,6 +76,7 @@ DeviceCtx *device_ctx() {
     }
     c->sm_count = prop.multiProcessorCount;
     c->smem_optin = prop.sharedMemPerBlockOptin;
+    c->name = prop.name;
     std::vector<double> tab(kZigWords);
     zig_tables_host(tab.data(), tab.data() + kZigOffF);
     zig_fast_tables_host(tab.data(), tab.data() + kZigOffF, reinterpret_cast<uint64_t *>(tab.data() + kZigOffK),
@@ -230,17 +232,50 @@ std::vector<double> sample_times(double tmax, int64_t nb_steps) {
     return t;
 }
 
-bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStream_t stream, bool timed,
-                    int *mapping) {
-    DeviceCtx *ctx = device_ctx();
-    if (!ctx) return false;
-    const Packed &p = dn.packed;
+static SsaArgs base_args(const Packed &p) {
     SsaArgs a{};
     a.S = p.S;
     a.R = p.R;
     a.P = p.P;
     a.Q = p.Q;
     a.macro_mode = p.macro_mode;
+    int mm = 0;
+    for (int32_t rr = 0; rr < p.R; rr++) {
+        int s = 0;
+        for (int32_t k = 0; k < p.P; k++) s += p.fac_ord[(size_t)rr * p.P + k];
+        mm = std::max(mm, s);
+    }
+    a.max_mults = mm;
+    return a;
+}
+
+Feasible feasible_kernels(const Packed &p, const DeviceCtx &ctx, int64_t n_traj, int64_t n_samples, bool times_ok,
+                          double t_last, bool rates_per_traj) {
+    SsaArgs a = base_args(p);
+    a.n_traj = n_traj;
+    a.n_samples = n_samples;
+    a.n_save = p.S;
+    a.rate_stride = rates_per_traj ? p.R : 0;
+    Feasible f;
+    const int spec_grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>(ctx.sm_count, (n_traj + ssa_spec_block() - 1) / ssa_spec_block()));
+    f.spec = !p.has_expr && times_ok && t_last < 0x1p60 && ssa_spec_supported(a, p.max_order) &&
+             ssa_spec_slots(a, spec_grid, ctx.smem_optin, ssa_spec_block()) > 0;
+    f.jit = f.spec && jit_supported(p);
+    f.warp = !p.has_expr && ssa_warp_supported(a, p.max_order) && ssa_warp_warps(a, ctx.smem_optin) > 0;
+    f.fast = !p.has_expr && times_ok && ssa_fast_supported(a, p.max_order) && ssa_fast_smem(a, 128) <= ctx.smem_optin;
+    f.generic = p.R <= 32 && ssa_thread_max_block(a, ctx.smem_optin) > 0;
+    f.spread = n_traj < (int64_t)ctx.sm_count * 4 * 32;
+    f.reactions = p.R;
+    return f;
+}
+
+bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStream_t stream, bool timed,
+                    int *mapping, const LaunchShape *force) {
+    DeviceCtx *ctx = device_ctx();
+    if (!ctx) return false;
+    const Packed &p = dn.packed;
+    SsaArgs a = base_args(p);
     a.rate = r.rates ? r.rates : dn.rate;
     a.rate_stride = r.rates ? r.rate_stride : 0;
     a.fac_sp = dn.fac_sp;
@@ -272,37 +307,41 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     if (!cuda_ok(cudaMemsetAsync(dn.scratch, 0, 4 * sizeof(unsigned long long), stream), "cudaMemsetAsync"))
         return false;
     if (r.n_traj == 0) return true;
-    // Kernel choice (RB_SSA_KERNEL=spec|fast|generic overrides): the
-    // speculative float-pair kernel, else the lockstep exact kernel, else
-    // the generic shared-memory kernel.
-    {
-        int mm = 0;
-        for (int32_t rr = 0; rr < p.R; rr++) {
-            int s = 0;
-            for (int32_t k = 0; k < p.P; k++) s += p.fac_ord[(size_t)rr * p.P + k];
-            mm = std::max(mm, s);
-        }
-        a.max_mults = mm;
-    }
+    // Kernel choice: a forced shape, else the autotuner's choice for this
+    // network shape, else the speculative float-pair kernel, the lockstep
+    // exact kernel, the generic shared-memory kernel (RB_SSA_KERNEL=
+    // spec|fast|generic|warp overrides).
     const char *pref = std::getenv("RB_SSA_KERNEL");
-    const bool want_generic = pref && std::strcmp(pref, "generic") == 0;
-    const bool want_fast = pref && std::strcmp(pref, "fast") == 0;
+    LaunchShape shape;
+    if (force) shape = *force;
+    else if (!pref && !r.in_species && tune_lookup(p, *ctx, r.n_traj, r.rate_stride != 0, shape) &&
+             !tune_shape_feasible(feasible_kernels(p, *ctx, r.n_traj, r.n_samples, r.times_ok, r.t_last,
+                                                   r.rate_stride != 0),
+                                  shape))
+        shape = LaunchShape{};
+    const int k = pref ? -1 : shape.kernel;
+    const bool want_generic = (pref && std::strcmp(pref, "generic") == 0) || k == 0;
+    const bool want_fast = (pref && std::strcmp(pref, "fast") == 0) || k == 2;
+    const bool want_desc = (pref && std::strcmp(pref, "spec") == 0) || k == 3;  // descriptor, not generated
+    const bool want_jit = k == 4;
+    const bool want_warp = (pref && std::strcmp(pref, "warp") == 0) || k == 5;
     const int spec_grid = (int)std::max<int64_t>(
         1, std::min<int64_t>(ctx->sm_count, (r.n_traj + ssa_spec_block() - 1) / ssa_spec_block()));
     const int spec_slots = ssa_spec_slots(a, spec_grid, ctx->smem_optin, ssa_spec_block());
     // Rate::Expr networks run on the generic kernel (native binary64 programs).
-    const bool spec = !p.has_expr && !want_generic && !want_fast && r.times_ok && r.t_last < 0x1p60 &&
+    const bool spec = !p.has_expr && !want_generic && !want_fast && !want_warp && r.times_ok && r.t_last < 0x1p60 &&
                       ssa_spec_supported(a, p.max_order) && spec_slots > 0;
     // Networks beyond the thread kernels' reach (more than 32 reactions, or
     // too large for their shared memory) take a warp per trajectory.
-    const bool want_warp = pref && std::strcmp(pref, "warp") == 0;
     const int warp_w = ssa_warp_supported(a, p.max_order) ? ssa_warp_warps(a, ctx->smem_optin) : 0;
-    const bool warp = warp_w > 0 && !want_generic && !p.has_expr &&
+    const bool warp = warp_w > 0 && !want_generic && !want_fast && !p.has_expr &&
                       (want_warp || (!spec && !(p.R <= 32 && ssa_thread_max_block(a, ctx->smem_optin) > 0)));
     const bool fast = !warp && !spec && !p.has_expr && !want_generic && r.times_ok && ssa_fast_supported(a, p.max_order) &&
                       ssa_fast_smem(a, 128) <= ctx->smem_optin;
-    if (pref && ((want_fast && !fast) || (want_warp && !warp) || (std::strcmp(pref, "spec") == 0 && !spec))) {
-        set_error(std::string("RB_SSA_KERNEL=") + pref + " does not cover this network or sample grid");
+    const bool strict = pref || force;  // a kernel asked for must run
+    if (strict && ((want_fast && !fast) || (want_warp && !warp) || ((want_desc || want_jit) && !spec))) {
+        set_error(std::string("kernel ") + (pref ? pref : std::to_string(k).c_str()) +
+                  " does not cover this network or sample grid");
         return false;
     }
     // Ensembles too small to fill every SM scheduler with a full warp spread
@@ -353,6 +392,8 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
         block = lanes ? 128 : ssa_spec_block();
         a.n_slots = lanes ? 128 : spec_slots;
         a.lanes = lanes;
+        a.phase_steps = shape.phase;
+        a.sched = shape.sched > 0 ? 1 : 0;
         if (const char *ph = std::getenv("RB_SPEC_PHASE")) a.phase_steps = std::atoi(ph);
         if (const char *sc = std::getenv("RB_SPEC_SCHED")) a.sched = std::strcmp(sc, "rot") == 0 ? 1 : 0;
         smem = ssa_spec_smem(a, a.n_slots);
@@ -384,12 +425,13 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
     const int64_t run_no = ++dn.runs;
     if (spec && jit_supported(p)) {
         const char *jit = std::getenv("RB_JIT");
-        // RB_SSA_KERNEL=spec asks for the packed-descriptor kernel itself
-        const bool off = (jit && std::strcmp(jit, "0") == 0) || (pref && std::strcmp(pref, "spec") == 0);
-        const bool compile = jit ? !off : (r.n_traj >= 4096 || run_no >= 2);
+        // RB_SSA_KERNEL=spec (or a shape of kernel 3) asks for the
+        // packed-descriptor kernel itself
+        const bool off = (jit && std::strcmp(jit, "0") == 0) || want_desc;
+        const bool compile = jit ? !off : (want_jit || r.n_traj >= 4096 || run_no >= 2);
         if (!off) {
             // generated kernels may run larger blocks (fewer registers per lane)
-            int kb = jit_block();
+            int kb = shape.block > 0 && !std::getenv("RB_JIT_BLOCK") ? shape.block : jit_block();
             // spread launches run 128 lanes of a kernel built for 128 (all
             // registers to the few lanes that hold trajectories)
             const bool spread = lanes != 0;
@@ -409,7 +451,7 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
                         dn.jit_version = dn.version;
                     }
                 }
-                if (!jk && jit && std::strcmp(jit, "1") == 0) return false;
+                if (!jk && ((jit && std::strcmp(jit, "1") == 0) || (want_jit && force))) return false;
                 if (jk) {
                     block = jb;
                     grid = jgrid;

@@ -23,6 +23,7 @@ struct DeviceCtx {
     int device = -1;
     int sm_count = 0;
     size_t smem_optin = 0;
+    std::string name;       // device name (the autotuner's cache key)
     double *zig = nullptr;  // device [2][257]
 };
 // Context of the current device (created on first use); nullptr + error on failure.
@@ -102,10 +103,40 @@ struct RunDev {
     double t_last = 0.0;    // largest sample time
 };
 
+// Kernel and launch shape of a sampled run.  kernel is a mapping code
+// (rb_run_stats.mapping: 0 generic, 2 lockstep exact, 3 speculative over the
+// descriptor, 4 generated for the network, 5 warp per trajectory) or -1 for
+// the built-in choice; block (generated kernel: lanes per block), phase
+// (speculative kernels: steps per phase) and sched (their slot scheduler)
+// are 0 / 0 / -1 for the defaults.
+struct LaunchShape {
+    int kernel = -1;
+    int block = 0;
+    int phase = 0;
+    int sched = -1;
+};
+
 // Enqueue the sampled-run kernel on `stream` (scratch reset included).
-// Records ev_start/ev_stop around the kernel when `timed`.
+// Records ev_start/ev_stop around the kernel when `timed`.  `force` fixes the
+// kernel and launch shape (an error if it does not cover the run); without
+// it the autotuner's choice for networks of this shape is used when it has
+// one (tune.cpp), else the built-in choice.  RB_SSA_KERNEL, RB_JIT_BLOCK,
+// RB_SPEC_PHASE and RB_SPEC_SCHED override both.
 bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStream_t stream, bool timed,
-                    int *mapping);
+                    int *mapping, const LaunchShape *force = nullptr);
+
+// Which kernels can run a sampled run of this network (no GPU work).
+struct Feasible {
+    bool spec = false;     // speculative float-pair kernels (descriptor; generated when jit)
+    bool jit = false;      // a kernel generated for the network
+    bool fast = false;     // lockstep exact kernel
+    bool warp = false;     // warp per trajectory
+    bool generic = false;  // generic exact thread kernel
+    bool spread = false;   // the ensemble is spread over fewer lanes per warp
+    int reactions = 0;
+};
+Feasible feasible_kernels(const Packed &p, const DeviceCtx &ctx, int64_t n_traj, int64_t n_samples, bool times_ok,
+                          double t_last, bool rates_per_traj);
 
 // Ensemble run whose engine-side device data lives in a fixed array compiled
 // into the library (ssa_thread.cu); returns 0, or 1 (invalid), 2 (CUDA),

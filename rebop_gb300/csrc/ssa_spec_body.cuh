@@ -567,7 +567,7 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     const float c_sel = (float)(a.max_mults + R + 6) * 0x1p-24f * 1.001f;
     const int64_t t_start = global_ns();
     const int phase_steps = a.phase_steps > 0 ? a.phase_steps : kSpecPhase;
-    unsigned int tick = 0, rot = 0;
+    unsigned int rot = 0;
     unsigned long long lane_events = 0;
 
     // ---- this lane's slot; the hot state sits in registers during a phase,
@@ -592,75 +592,73 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
             uint64_t *const rl = rate + (rate_cols ? slot : 0);
             float2 *const rf = rdf + (rate_cols ? slot : 0);
             for (int step = 0; step < phase_steps && live; ++step) {
-                if (!have) {
-                    // take the next trajectory into this slot
-                    const long long traj = (long long)atomicAdd(a.work, 1ull);
-                    if (traj >= a.n_traj) {
-                        live = false;
-                        break;
-                    }
-                    uint64_t t0;
-                    if (a.in_species) {
-                        for (int s = 0; s < S; ++s) sp[s * NS] = a.in_species[traj * S + s];
-                        t0 = (uint64_t)__double_as_longlong(a.in_t[traj]);
-                        g.s0 = a.in_rng[traj * 4 + 0];
-                        g.s1 = a.in_rng[traj * 4 + 1];
-                        g.s2 = a.in_rng[traj * 4 + 2];
-                        g.s3 = a.in_rng[traj * 4 + 3];
-                    } else {
-                        for (int s = 0; s < S; ++s) sp[s * NS] = a.x0[traj * a.x0_stride + s];
-                        t0 = 0;
-                        xo_seed(g, a.seeds[traj]);
-                    }
-                    nat = !emul_domain(t0);
-                    exact_traj = (t0 >> 52) > 1023 + 60;
-                    for (int r = 0; r < R; ++r) {
-                        const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[traj * a.rate_stride + r]);
-                        nat |= !emul_domain(rb);
-                        exact_traj |= !spec_rate_ok(rb);
-                        if (rate_cols) {
-                            rl[r * RS] = rb;
-                            const DF d = df_from_double(__longlong_as_double((long long)rb));
-                            rf[r * RS] = make_float2(d.h, d.l);
+                if (!have || begin) {  // rare: one branch for both
+                    if (!have) {
+                        // take the next trajectory into this slot
+                        const long long traj = (long long)atomicAdd(a.work, 1ull);
+                        if (traj >= a.n_traj) {
+                            live = false;
+                            break;
                         }
+                        uint64_t t0;
+                        if (a.in_species) {
+                            for (int s = 0; s < S; ++s) sp[s * NS] = a.in_species[traj * S + s];
+                            t0 = (uint64_t)__double_as_longlong(a.in_t[traj]);
+                            g.s0 = a.in_rng[traj * 4 + 0];
+                            g.s1 = a.in_rng[traj * 4 + 1];
+                            g.s2 = a.in_rng[traj * 4 + 2];
+                            g.s3 = a.in_rng[traj * 4 + 3];
+                        } else {
+                            for (int s = 0; s < S; ++s) sp[s * NS] = a.x0[traj * a.x0_stride + s];
+                            t0 = 0;
+                            xo_seed(g, a.seeds[traj]);
+                        }
+                        nat = !emul_domain(t0);
+                        exact_traj = (t0 >> 52) > 1023 + 60;
+                        for (int r = 0; r < R; ++r) {
+                            const uint64_t rb = (uint64_t)__double_as_longlong(a.rate[traj * a.rate_stride + r]);
+                            nat |= !emul_domain(rb);
+                            exact_traj |= !spec_rate_ok(rb);
+                            if (rate_cols) {
+                                rl[r * RS] = rb;
+                                const DF d = df_from_double(__longlong_as_double((long long)rb));
+                                rf[r * RS] = make_float2(d.h, d.l);
+                            }
+                        }
+                        exact_traj |= nat;
+                        exact_traj |= !Ops::load(c, a, sp, NS);
+                        tc = tf_from_double(__longlong_as_double((long long)t0));
+                        st[4 * NS] = t0;
+                        st[6 * NS] = (uint64_t)traj;
+                        st[9 * NS] = 0;
+                        ev = 0;
+                        have = true;
+                        begin = true;
                     }
-                    exact_traj |= nat;
-                    exact_traj |= !Ops::load(c, a, sp, NS);
-                    tc = tf_from_double(__longlong_as_double((long long)t0));
-                    st[4 * NS] = t0;
-                    st[6 * NS] = (uint64_t)traj;
-                    st[9 * NS] = 0;
-                    ev = 0;
-                    have = true;
-                    begin = true;
-                }
-                if (begin) {
-                    // a sample interval starts at t0 (the clock tc holds t0
-                    // exactly): save what a re-run needs
-                    const int si = (int)st[9 * NS];
-                    if (si < n_cache) {
-                        st[5 * NS] = sTb[si];
-                        Tc = TF{sTf[3 * si], sTf[3 * si + 1], sTf[3 * si + 2]};
-                    } else {
-                        const double T = a.sample_t[si];
-                        st[5 * NS] = (uint64_t)__double_as_longlong(T);
-                        Tc = tf_from_double(T);
+                    if (begin) {
+                        // a sample interval starts at t0 (the clock tc holds t0
+                        // exactly): save what a re-run needs
+                        const int si = (int)st[9 * NS];
+                        if (si < n_cache) {
+                            st[5 * NS] = sTb[si];
+                            Tc = TF{sTf[3 * si], sTf[3 * si + 1], sTf[3 * si + 2]};
+                        } else {
+                            const double T = a.sample_t[si];
+                            st[5 * NS] = (uint64_t)__double_as_longlong(T);
+                            Tc = tf_from_double(T);
+                        }
+                        err_t = 0.f;
+                        if (exact_traj)
+                            for (int s = 0; s < S; ++s) sps[s * NS] = sp[s * NS];
+                        else
+                            Ops::save(c, a, sp, sps, NS);
+                        gsv[0] = g.s0;
+                        gsv[NS] = g.s1;
+                        gsv[2 * NS] = g.s2;
+                        gsv[3 * NS] = g.s3;
+                        st[8 * NS] = ev;
+                        begin = false;
                     }
-                    err_t = 0.f;
-                    if (exact_traj)
-                        for (int s = 0; s < S; ++s) sps[s * NS] = sp[s * NS];
-                    else
-                        Ops::save(c, a, sp, sps, NS);
-                    gsv[0] = g.s0;
-                    gsv[NS] = g.s1;
-                    gsv[2 * NS] = g.s2;
-                    gsv[3 * NS] = g.s3;
-                    st[8 * NS] = ev;
-                    begin = false;
-                }
-                if ((++tick & 1023u) == 0 && global_ns() - t_start > a.budget_ns) {
-                    abort_run = true;
-                    break;
                 }
 
                 bool fire = false, replay = exact_traj;
@@ -725,6 +723,15 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                                 idx += dr < 0.0f ? 1 : 0;
                                 close |= fabsf(dr) <= msel;
                             }
+                        }
+                        if (!amb && fire && !close) {
+                            // the common step, decided in float32: commit the
+                            // clock and fire the reaction
+                            tc = tn;
+                            err_t = err_tn;
+                            ++ev;
+                            Ops::jump(c, a, ex, sp, NS, idx);
+                            continue;
                         }
                         if (!amb) {
                             if (fire) {
@@ -800,6 +807,9 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
                     }
                 }
             }
+            // ---- the wall-clock budget, once per phase (a phase is at most
+            // phase_steps steps, and an interval re-run checks it itself)
+            if (global_ns() - t_start > a.budget_ns) abort_run = true;
             // ---- count the rows recorded in this phase (one fence per lane)
             if (a.row_done && (spend[slot] | sfin[slot])) {
                 const uint32_t pw = spend[slot], fw = sfin[slot];
