@@ -375,8 +375,11 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
 }
 
 // Draws: row r of out takes query r / per_query's mixture; component by its
-// weight, then two Gaussians (Box-Muller).
-__global__ void mdn_sample_kernel(const float *O, int B, int K, uint64_t seed, float *out, int per_query) {
+// weight, then two Gaussians (Box-Muller).  With `base` ([queries][2]) the
+// draw z is a residual in log space and the row receives the count
+// floor(exp(z + base)), at least 0.
+__global__ void mdn_sample_kernel(const float *O, int B, int K, uint64_t seed, float *out, int per_query,
+                                  const float *base) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= B) return;
     const float *o = O + (size_t)(row / per_query) * 5 * K;
@@ -399,8 +402,58 @@ __global__ void mdn_sample_kernel(const float *O, int B, int K, uint64_t seed, f
     }
     const float rad = sqrtf(-2.0f * logf(u1)), ang = 6.2831853f * u2;
     const float s1 = softplusf_(o[3 * K + c]) + 1e-3f, s2 = softplusf_(o[4 * K + c]) + 1e-3f;
-    out[2 * row] = o[K + c] + s1 * rad * cosf(ang);
-    out[2 * row + 1] = o[2 * K + c] + s2 * rad * sinf(ang);
+    const float z1 = o[K + c] + s1 * rad * cosf(ang), z2 = o[2 * K + c] + s2 * rad * sinf(ang);
+    if (base) {
+        const float *bq = base + (size_t)(row / per_query) * 2;
+        out[2 * row] = fmaxf(floorf(expf(z1 + bq[0])), 0.0f);
+        out[2 * row + 1] = fmaxf(floorf(expf(z2 + bq[1])), 0.0f);
+    } else {
+        out[2 * row] = z1;
+        out[2 * row + 1] = z2;
+    }
+}
+
+// Reaction rate equations of a mass-action network -- the deterministic
+// limit of the SSA, dx/dt = sum_r nu_r k_r prod_s ff(x_s, e_rs) with ff the
+// falling factorial x (x - 1) ... (x - e + 1), clamped at 0 where it would turn
+// negative -- integrated in float32 from x0 to each query's t by classic
+// fourth-order Runge-Kutta with n_steps equal steps.  E[R][S] holds the
+// reactant orders, N[R][S] the net changes; rates is [Q][R].  out[q][j] is
+// the solution's species out_idx[j] at t_q.  The surrogate predicts the SSA's
+// count distribution relative to this solution.
+constexpr int kRreMaxS = 16, kRreMaxR = 32;
+
+__device__ void rre_rhs(const int *E, const float *N, const float *k, int S, int R, const float *x, float *dx) {
+    for (int s = 0; s < S; ++s) dx[s] = 0.0f;
+    for (int r = 0; r < R; ++r) {
+        float a = k[r];
+        for (int s = 0; s < S; ++s) {
+            const int e = E[r * S + s];
+            for (int j = 0; j < e; ++j) a *= fmaxf(x[s] - (float)j, 0.0f);
+        }
+        for (int s = 0; s < S; ++s) dx[s] += N[r * S + s] * a;
+    }
+}
+
+__global__ void rre_kernel(const float *rates, const float *tq, int Q, int S, int R, const int *E, const float *N,
+                           const float *x0, int n_steps, const int *out_idx, int n_out, float *out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Q) return;
+    float k[kRreMaxR], x[kRreMaxS], xt[kRreMaxS], k1[kRreMaxS], k2[kRreMaxS], k3[kRreMaxS], k4[kRreMaxS];
+    for (int r = 0; r < R; ++r) k[r] = rates[(size_t)q * R + r];
+    for (int s = 0; s < S; ++s) x[s] = x0[s];
+    const float h = tq[q] / (float)n_steps;
+    for (int n = 0; n < n_steps; ++n) {
+        rre_rhs(E, N, k, S, R, x, k1);
+        for (int s = 0; s < S; ++s) xt[s] = x[s] + 0.5f * h * k1[s];
+        rre_rhs(E, N, k, S, R, xt, k2);
+        for (int s = 0; s < S; ++s) xt[s] = x[s] + 0.5f * h * k2[s];
+        rre_rhs(E, N, k, S, R, xt, k3);
+        for (int s = 0; s < S; ++s) xt[s] = x[s] + h * k3[s];
+        rre_rhs(E, N, k, S, R, xt, k4);
+        for (int s = 0; s < S; ++s) x[s] = fmaxf(x[s] + h / 6.0f * (k1[s] + 2.0f * k2[s] + 2.0f * k3[s] + k4[s]), 0.0f);
+    }
+    for (int j = 0; j < n_out; ++j) out[(size_t)q * n_out + j] = x[out_idx[j]];
 }
 
 }  // namespace
@@ -408,6 +461,16 @@ __global__ void mdn_sample_kernel(const float *O, int B, int K, uint64_t seed, f
 }  // namespace rbg
 
 extern "C" {
+
+// Rate-equation solution at each query (see rre_kernel); device pointers.
+int rbg_mdn_rre(const float *rates, const float *tq, int Q, int S, int R, const int *E, const float *N,
+                const float *x0, int n_steps, const int *out_idx, int n_out, float *out, void *stream) {
+    if (S < 1 || S > rbg::kRreMaxS || R < 1 || R > rbg::kRreMaxR || n_steps < 1) return (int)cudaErrorInvalidValue;
+    if (Q == 0) return 0;
+    rbg::rre_kernel<<<(Q + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(rates, tq, Q, S, R, E, N, x0,
+                                                                                   n_steps, out_idx, n_out, out);
+    return (int)cudaGetLastError();
+}
 
 // Surrogate kernels (device pointers, the caller's stream).  Internal to the
 // Python surrogate module; no counterpart in the reference.
@@ -474,10 +537,11 @@ int rbg_mdn_adam(float *w, void *wb, const float *g, float *m, float *v, int n, 
     return (int)cudaGetLastError();
 }
 
-int rbg_mdn_sample(const float *O, int B, int K, uint64_t seed, float *out, int per_query, void *stream) {
+int rbg_mdn_sample(const float *O, int B, int K, uint64_t seed, float *out, int per_query, const float *base,
+                   void *stream) {
     if (per_query < 1) return (int)cudaErrorInvalidValue;
     rbg::mdn_sample_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, B, K, seed, out,
-                                                                                          per_query);
+                                                                                          per_query, base);
     return (int)cudaGetLastError();
 }
 

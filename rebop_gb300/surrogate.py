@@ -2,15 +2,22 @@
 5 rate constants log-uniform over one decade either side of their values, t
 in [0, 1]).
 
-A multilayer perceptron (6 inputs -> 4 x 256 SiLU -> 40) maps
-(log10 rate factors, t) to an 8-component diagonal Gaussian mixture over
-(log1p protein, log1p dimer) counts.  Weights are BF16 with FP32 master
-copies; every forward and backward GEMM runs on the 5th-generation tensor
-cores (tcgen05.mma into tensor memory, FP32 accumulation), and the loss, its gradient, the optimiser and
-the sampler are the engine's own kernels (rebop_gb300/csrc/mdn.cu).  PyTorch
-only holds the device memory.  Training data, the validation that decides
-where the surrogate is trusted, and the fallback for the rest all come from
-the SSA engine itself.
+A query (u, t) -- the log10 factors u of the five rate constants and the time
+-- gets a count distribution of (protein, dimer).  Its deterministic part
+comes from the network's reaction rate equations (the SSA's mean-field
+limit), integrated per query on the GPU (rbg_mdn_rre): b = log(x_RRE + 1).  A
+multilayer perceptron (8 inputs: u, t, b -> 4 x 256 SiLU -> 40) maps the query
+to an 8-component diagonal Gaussian mixture over the residual
+log(n + v) - b of the counts n, v ~ U[0, 1) (dequantised integers); a draw z
+becomes the count floor(exp(z + b)).  So the network learns only the
+stochastic correction around the rate equations, a small and smooth function
+that BF16 resolves finely.  Weights are BF16 with FP32 master copies; every
+forward and backward GEMM runs on the 5th-generation tensor cores (tcgen05.mma
+into tensor memory, FP32 accumulation), and the rate-equation solver, the
+loss, its gradient, the optimiser and the sampler are the engine's own kernels
+(rebop_gb300/csrc/mdn.cu).  PyTorch only holds the device memory.  Training
+data, the validation that decides where the surrogate is trusted, and the
+fallback for the rest all come from the SSA engine itself.
 """
 
 from __future__ import annotations
@@ -21,42 +28,80 @@ from ._lib import check, lib
 
 RATES0 = (25.0, 1000.0, 0.001, 0.1, 1.0)  # G->G+M, M->M+P, 2P->D, M->0, P->0
 X0 = (1, 0, 0, 0)
-N_IN, HIDDEN, LAYERS, K = 6, 256, 4, 8
+EXPS = ([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 2, 0], [0, 1, 0, 0], [0, 0, 1, 0])
+DIFFS = ([0, 1, 0, 0], [0, 0, 1, 0], [0, 0, -2, 1], [0, -1, 0, 0], [0, 0, -1, 0])
+N_QUERY, N_IN, HIDDEN, LAYERS, K = 6, 8, 256, 4, 8
 N_OUT = 5 * K
+RRE_STEPS = 128
 
 
 def dimer_network(rates=RATES0):
     from .api import Network, Rate
 
     net = Network(4)
-    for k, e, d in zip(rates, ([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 2, 0], [0, 1, 0, 0], [0, 0, 1, 0]),
-                       ([0, 1, 0, 0], [0, 0, 1, 0], [0, 0, -2, 1], [0, -1, 0, 0], [0, 0, -1, 0])):
+    for k, e, d in zip(rates, EXPS, DIFFS):
         net.add_reaction(Rate.lma(k, e), d)
     return net
 
 
-def generate(n_traj: int, seed: int, nb_steps: int = 100, net=None, per_traj: int = 1, chunk: int = 1 << 17):
-    """SSA training data: per-trajectory rate factors 10^u, u ~ U[-1, 1]^5, and
-    `per_traj` sample times per trajectory drawn from the grid t = i / nb_steps
-    (one by default, so every tuple is an independent draw of its
-    distribution).  Returns inputs [n*per_traj][6] (u, t) and targets
-    [n*per_traj][2] (log1p protein, log1p dimer)."""
+def rre_log_means(x):
+    """b = log(x_RRE + 1) of (protein, dimer) at each query row of x [Q][6]
+    (u, t) on the GPU: the reaction rate equations integrated from the initial
+    counts to t (rbg_mdn_rre, RK4 in float32, RRE_STEPS steps)."""
+    import torch
+
+    x = x.to("cuda", torch.float32).contiguous()
+    Q = x.shape[0]
+    rates = (torch.tensor(RATES0, device="cuda") * torch.pow(10.0, x[:, :5])).contiguous()
+    t = x[:, 5].contiguous()
+    E = torch.tensor(EXPS, dtype=torch.int32, device="cuda")
+    N = torch.tensor(DIFFS, dtype=torch.float32, device="cuda")
+    x0 = torch.tensor(X0, dtype=torch.float32, device="cuda")
+    idx = torch.tensor([2, 3], dtype=torch.int32, device="cuda")
+    out = torch.empty(Q, 2, dtype=torch.float32, device="cuda")
+    check(lib.rbg_mdn_rre(rates.data_ptr(), t.data_ptr(), Q, 4, 5, E.data_ptr(), N.data_ptr(), x0.data_ptr(),
+                          RRE_STEPS, idx.data_ptr(), 2, out.data_ptr(), torch.cuda.current_stream().cuda_stream))
+    return torch.log1p(out)
+
+
+def features(x):
+    """Network inputs of queries x [Q][6]: (u, t, b)."""
+    import torch
+
+    x = x.to("cuda", torch.float32).contiguous()
+    return torch.cat([x, rre_log_means(x)], dim=1).contiguous()
+
+
+def generate(n_traj: int, seed: int, nb_steps: int = 100, net=None, per_traj: int = 1, chunk: int = 1 << 17,
+             draws: int = 1):
+    """SSA training data: rate factors 10^u, u ~ U[-1, 1]^5, and a sample time
+    from the grid t = i / nb_steps per tuple; each tuple gets `draws`
+    trajectories (1: every tuple an independent draw of its distribution) and
+    each trajectory `per_traj` sample times.  Returns queries [n][6] (u, t),
+    targets [n][2] (the residuals log(n + v) - b, v ~ U[0, 1)) and b [n][2]."""
+    import torch
+
     rng = np.random.default_rng(seed)
     net = net or dimer_network()
     xs, ys = [], []
     for c0 in range(0, n_traj, chunk):
         n = min(chunk, n_traj - c0)
-        u = rng.uniform(-1.0, 1.0, size=(n, 5))
+        n_u = -(-n // draws)
+        u = np.repeat(rng.uniform(-1.0, 1.0, size=(n_u, 5)), draws, axis=0)[:n]
         rates = np.asarray(RATES0) * 10.0 ** u
         seeds = rng.integers(np.iinfo(np.uint64).max, size=n, dtype=np.uint64)
         res = net.run_ensemble(list(X0), seeds, 1.0, nb_steps, save=[2, 3], rates=rates, want_events=False)
         c = res.counts  # [nb+1][2][n]
-        ti = rng.integers(0, nb_steps + 1, size=(n, per_traj))
+        ti = np.repeat(rng.integers(0, nb_steps + 1, size=(n_u, per_traj)), draws, axis=0)[:n]
         j = np.repeat(np.arange(n), per_traj)
         t = ti.reshape(-1)
         xs.append(np.concatenate([u[j], (t / nb_steps)[:, None]], axis=1))
-        ys.append(np.log1p(np.stack([c[t, 0, j], c[t, 1, j]], axis=1).astype(np.float64)))
-    return np.concatenate(xs).astype(np.float32), np.concatenate(ys).astype(np.float32), None
+        cnt = np.stack([c[t, 0, j], c[t, 1, j]], axis=1).astype(np.float64)
+        ys.append(np.log(cnt + rng.uniform(0.0, 1.0, size=cnt.shape)))
+    x = np.concatenate(xs).astype(np.float32)
+    b = rre_log_means(torch.from_numpy(x)).cpu().numpy().astype(np.float64)
+    y = (np.concatenate(ys) - b).astype(np.float32)
+    return x, y, b.astype(np.float32)
 
 
 class MDN:
@@ -109,8 +154,8 @@ class MDN:
             raise RuntimeError("tcgen05 GEMM: a completion wait ran out")
 
     def forward(self, x):
-        """x [B][6] float (unnormalised u, t) -> head outputs [B][40]; keeps the
-        activations for backward."""
+        """x [B][8] float features (unnormalised u, t, b) -> head outputs [B][40];
+        keeps the activations for backward."""
         torch = self.torch
         B = x.shape[0]
         h = ((x - self.x_mean) / self.x_std).to(torch.bfloat16).contiguous()
@@ -175,9 +220,9 @@ class MDN:
         return loss
 
     def fit(self, x, y, epochs: int = 20, batch: int = 4096, lr: float = 2e-3, seed: int = 0, log=None):
-        """Train on host arrays x [N][6], y [N][2] (log1p counts)."""
+        """Train on host arrays x [N][6] (queries u, t), y [N][2] (residuals)."""
         torch = self.torch
-        X = torch.from_numpy(np.ascontiguousarray(x)).to(self.dev)
+        X = features(torch.from_numpy(np.ascontiguousarray(x)))
         Y = torch.from_numpy(np.ascontiguousarray(y)).to(self.dev)
         self.x_mean = X.mean(0)
         self.x_std = X.std(0) + 1e-6
@@ -201,18 +246,20 @@ class MDN:
 
     def sample_counts(self, x, n_draws: int, seed: int = 1):
         """n_draws samples of (protein, dimer) counts at each query row of x [Q][6]:
-        one forward pass per query, then n_draws draws from its mixture."""
-        X = self._queries(x)
+        the rate equations and one forward pass per query, then n_draws draws
+        from its mixture, each turned into a count by the sampler kernel."""
+        F = features(self._queries(x))
         torch = self.torch
-        o = self.forward(X)
-        z = torch.empty(X.shape[0] * n_draws, 2, dtype=torch.float32, device=self.dev)
-        check(lib.rbg_mdn_sample(o.data_ptr(), z.shape[0], K, int(seed), z.data_ptr(), int(n_draws), self._s()))
-        c = torch.clamp(torch.round(torch.expm1(z)), min=0)
-        return c.view(X.shape[0], n_draws, 2)
+        o = self.forward(F)
+        base = F[:, N_QUERY:].contiguous()
+        c = torch.empty(F.shape[0] * n_draws, 2, dtype=torch.float32, device=self.dev)
+        check(lib.rbg_mdn_sample(o.data_ptr(), c.shape[0], K, int(seed), c.data_ptr(), int(n_draws),
+                                 base.data_ptr(), self._s()))
+        return c.view(F.shape[0], n_draws, 2)
 
     def predict_params(self, x):
-        """Mixture parameters at each query row (one forward pass): [Q][40]."""
-        return self.forward(self._queries(x))
+        """Mixture parameters (over the residuals) at each query row: [Q][40]."""
+        return self.forward(features(self._queries(x)))
 
     def _queries(self, x):
         torch = self.torch
@@ -256,7 +303,7 @@ class Surrogate:
         x = np.concatenate([u, t[:, None]], axis=1).astype(np.float32)
         draws = self.model.sample_counts(x, n_ssa, seed=seed + 1).cpu().numpy()
         out = {"w1": np.zeros((n_points, 2)), "ks": np.zeros((n_points, 2)), "w1_floor": np.zeros((n_points, 2)),
-               "mean": np.zeros((n_points, 2))}
+               "mean": np.zeros((n_points, 2)), "t": t}
         for p in range(n_points):
             sl = slice(p * n_ssa, (p + 1) * n_ssa)
             for s in range(2):

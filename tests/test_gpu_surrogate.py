@@ -38,9 +38,11 @@ def test_mdn_gradients_match_oracle(torch):
 
     rng = np.random.default_rng(1)
     model = sg.MDN(seed=3)
-    x = rng.uniform(-1, 1, size=(512, 6)).astype(np.float32)
+    # network inputs: u (5), t, and the rate-equation log means (2)
+    x = rng.uniform(-1, 1, size=(512, sg.N_IN)).astype(np.float32)
     x[:, 5] = rng.uniform(0, 1, 512)
-    y = np.stack([rng.uniform(0, 8, 512), rng.uniform(0, 6, 512)], axis=1).astype(np.float32)
+    x[:, 6:] = rng.uniform(0, 8, (512, 2))
+    y = rng.normal(0.0, 0.3, size=(512, 2)).astype(np.float32)
     model.x_mean = torch.tensor(x.mean(0)).cuda()
     model.x_std = torch.tensor(x.std(0) + 1e-6).cuda()
     loss, dW, db = model.loss_and_grad(torch.tensor(x).cuda(), torch.tensor(y).cuda())
@@ -61,12 +63,12 @@ def test_mdn_training_lowers_the_loss(torch):
 
     x, y, _ = sg.generate(20000, seed=5, nb_steps=50)
     model = sg.MDN(seed=1)
-    X, Y = torch.tensor(x).cuda(), torch.tensor(y).cuda()
+    X, Y = sg.features(torch.tensor(x)), torch.tensor(y).cuda()
     model.x_mean, model.x_std = X.mean(0), X.std(0) + 1e-6
     before = float(model.loss_and_grad(X[:4096], Y[:4096])[0])
     model.fit(x, y, epochs=8, batch=1024, lr=3e-3)
     after = float(model.loss_and_grad(X[:4096], Y[:4096])[0])
-    assert after < before - 1.0, (before, after)
+    assert after < before - 0.5, (before, after)
     c = model.sample_counts(x[:16], 200).cpu().numpy()
     assert c.shape == (16, 200, 2) and (c >= 0).all()
 
@@ -93,3 +95,29 @@ def test_gemm_tcgen05_matches_float64(torch):
                 ref = (A.T if ta else A) @ (B.T if tb else B)
                 err = np.abs(c.cpu().numpy() - ref).max() / (np.abs(ref).max() + 1e-30)
                 assert err < 1e-5, (M, N, K, ta, tb, err)
+
+
+def test_rate_equation_kernel_matches_scipy(torch):
+    # rbg_mdn_rre (float32 RK4, the surrogate's deterministic part) against an
+    # adaptive float64 solution of the same rate equations
+    from scipy.integrate import solve_ivp
+
+    from rebop_gb300 import surrogate as sg
+
+    rng = np.random.default_rng(4)
+    x = np.concatenate([rng.uniform(-1, 1, (64, 5)), rng.uniform(0.01, 1, (64, 1))], axis=1).astype(np.float32)
+    got = np.expm1(sg.rre_log_means(torch.tensor(x)).cpu().numpy().astype(np.float64))
+    E, N = np.array(sg.EXPS, float), np.array(sg.DIFFS, float)
+    for q in range(64):
+        k = np.asarray(sg.RATES0) * 10.0 ** x[q, :5].astype(np.float64)
+
+        def rhs(_, v):
+            a = k.copy()
+            for r in range(5):
+                for s in range(4):
+                    for j in range(int(E[r, s])):
+                        a[r] *= max(v[s] - j, 0.0)
+            return N.T @ a
+
+        sol = solve_ivp(rhs, (0.0, float(x[q, 5])), np.array(sg.X0, float), method="LSODA", rtol=1e-9, atol=1e-9)
+        np.testing.assert_allclose(got[q], sol.y[2:4, -1], rtol=2e-3, atol=1e-3)
