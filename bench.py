@@ -119,7 +119,7 @@ WORKLOADS = {"dimer": DIMER, "sir": SIR, "large": LARGE, "vilar": VILAR}
 
 BATCH = dict(
     name="batch",
-    desc=("heterogeneous batch in one CUDA graph: 4096 Michaelis-Menten sets (E+S<->ES->E+P, rates log-uniform "
+    desc=("heterogeneous batch in one CUDA graph around one persistent launch: 4096 Michaelis-Menten sets (E+S<->ES->E+P, rates log-uniform "
           "in [1e-3, 1e1], E0 ~ U[10, 100], S0 ~ U[100, 1000], tmax 1) and 1024 random mass-action networks "
           "(8-64 species, 16-256 reactions, order <= 2, stoichiometry in {-2..2}, counts ~ U[0, 500], tmax 1e-3); "
           "64 trajectories each, nb_steps 100 (seed 20260105)"),
@@ -629,7 +629,7 @@ def measure_batch(args, steps: int, warmup: int, cpu: bool = True) -> dict:
 
     items = batch_items()
     b, nets = make_batch(rb, items)
-    n_thread, n_warp = b.plan()
+    n_own, n_persistent = b.plan()
     for s in range(warmup):
         b.run()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
@@ -657,7 +657,8 @@ def measure_batch(args, steps: int, warmup: int, cpu: bool = True) -> dict:
         "value": events / (dev_ms / 1e3), "unit": "events/s", "steps": steps, "warmup": warmup,
         "ms_per_step": dev_ms / steps,
         "config": {"workload": BATCH["desc"], "items": len(items), "trajectories": len(items) * BATCH["traj"],
-                   "events_per_step": events / steps, "thread_launches": n_thread, "warp_batch_items": n_warp,
+                   "events_per_step": events / steps, "own_launches": n_own, "persistent_items": n_persistent,
+                   "mode": os.environ.get("RB_BATCH_MODE", "persistent"),
                    "timing": "device time of the replayed graph: input copy, kernels, result copy",
                    "l2": "inputs and outputs far above L2 are copied in every step"},
         "e2e": {"value": events / wall, "unit": "events/s", "h2d_bytes_per_step": int(h2d),

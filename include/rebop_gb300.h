@@ -59,7 +59,8 @@ typedef struct {
     int32_t mapping;       /* kernel that ran: 0 generic thread-per-trajectory,
                             * 2 lockstep exact, 3 speculative float-pair,
                             * 4 speculative generated for the network (NVRTC),
-                            * 5 warp per trajectory, 6 batch graph */
+                            * 5 warp per trajectory, 6 batch graph,
+                            * 7 thread unit of a batch's persistent launch */
     uint64_t exact_reruns; /* sample intervals the speculative kernel re-ran
                             * exactly because a decision fell inside its
                             * error margin */
@@ -252,11 +253,16 @@ void rb_rng_state_from_seed(uint64_t seed, uint64_t *state);
  * No counterpart in the reference, which runs one network and one parameter
  * set per call.  A batch holds many ensembles -- different networks, rate
  * constants, initial counts, horizons, trajectory counts -- and runs them all
- * with one CUDA graph: ensembles of one network structure and sample grid
- * merge into a single thread-per-trajectory launch with per-trajectory rates
- * and counts; the rest share one warp-per-trajectory launch that takes the
- * items with the most estimated work first.  Every result equals what
- * rb_ensemble_run gives for the same item, bit for bit. */
+ * with one CUDA graph around one persistent launch: its warps take work from
+ * one queue, a trajectory of a large network (a warp per trajectory, items
+ * with the most estimated work first) or a thread unit -- 32 trajectories of
+ * a network of at most 16 species and 16 reactions, one per lane, with the
+ * exact per-lane step.  Items with rate expressions, define_system! items
+ * whose arithmetic differs from the launch's and per-trajectory rates on
+ * networks too large for a thread unit run as launches of their own in the
+ * same graph.  (RB_BATCH_MODE=merged: ensembles of one network structure and
+ * sample grid merge into one thread-per-trajectory launch instead.)  Every
+ * result equals what rb_ensemble_run gives for the same item, bit for bit. */
 typedef struct rb_batch rb_batch;
 int rb_batch_create(rb_batch **out);
 void rb_batch_destroy(rb_batch *b);
@@ -272,10 +278,12 @@ int rb_batch_add(rb_batch *b, const rb_network *net, int64_t n_traj, const int64
  * the graph; later runs replay it.  stats->kernel_ms is the graph's device
  * time (copies included), stats->kernel_launches its kernel count. */
 int rb_batch_run(rb_batch *b, rb_run_stats *stats);
-/* The launch classes the planner forms (no GPU needed), and the kernel an
- * item runs on (rb_run_stats.mapping codes; 4 until the first run confirms
- * whether the generated kernel compiled). */
-int rb_batch_plan(rb_batch *b, int32_t *n_thread_launches, int32_t *n_warp_items);
+/* The plan (no GPU needed): launches of their own, and items of the
+ * persistent launch; and the kernel an item runs on (rb_run_stats.mapping
+ * codes: 5 warp per trajectory and 7 thread unit in the persistent launch;
+ * 4 for a merged class until the first run confirms whether the generated
+ * kernel compiled). */
+int rb_batch_plan(rb_batch *b, int32_t *n_own_launches, int32_t *n_persistent_items);
 int rb_batch_item_mapping(const rb_batch *b, int32_t item, int32_t *mapping);
 
 /* ------------------------------------------ stateful single trajectory ---

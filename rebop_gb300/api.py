@@ -471,6 +471,7 @@ class Batch:
         return self._out[k][1]
 
     def plan(self) -> tuple[int, int]:
+        """(launches of their own, items of the persistent launch)."""
         a, b = C.c_int32(), C.c_int32()
         check(lib.rb_batch_plan(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value

@@ -95,11 +95,36 @@ std::string Batch::add(const Network *net, const ItemIn &in) {
     return "";
 }
 
-// Group into classes and choose each class's mapping.
+// Choose each item's mapping.  By default one persistent launch runs every
+// mass-action item of the launch's arithmetic: items of at most 16 species
+// and 16 reactions as thread units (32 trajectories of one item, one per
+// lane), the others a warp per trajectory, all from one queue -- warp items
+// with the most estimated work first, thread units after them, filling the
+// tail.  Rate expressions, define_system! items whose arithmetic differs
+// from the launch's, and per-trajectory rates on networks too large for a
+// thread unit run as launches of their own.  RB_BATCH_MODE=merged keeps the
+// earlier plan: items of one structure and sample grid merged into one
+// thread-per-trajectory launch, the rest in the warp launch.
 bool Batch::plan() {
     classes.clear();
     warp_items.clear();
+    thread_items.clear();
+    const char *mode = std::getenv("RB_BATCH_MODE");
+    const bool merged_mode = mode && std::strcmp(mode, "merged") == 0;
+    // the persistent launch's arithmetic: the items' majority
+    int64_t n_macro = 0, n_plain = 0;
+    for (const Item &it : items)
+        if (!it.packed.has_expr) (it.packed.macro_mode ? n_macro : n_plain) += 1;
+    macro_mode = n_macro > n_plain ? 1 : 0;
     std::map<std::string, int> by_key;
+    auto single = [&](int i) {
+        items[i].mapping = 0;  // a launch of its own (launch_sampled picks the kernel)
+        Class c;
+        c.kind = Class::Single;
+        c.items.push_back(i);
+        c.n_traj = items[i].in.n_traj;
+        classes.push_back(c);
+    };
     for (size_t i = 0; i < items.size(); i++) {
         Item &it = items[i];
         const Packed &p = it.packed;
@@ -108,23 +133,26 @@ bool Batch::plan() {
         probe.R = p.R;
         probe.P = p.P;
         probe.Q = p.Q;
-        int mm = 0;
-        for (int32_t r = 0; r < p.R; r++) {
-            int s = 0;
-            for (int32_t k = 0; k < p.P; k++) s += p.fac_ord[(size_t)r * p.P + k];
-            mm = std::max(mm, s);
+        const bool times_ok = std::isfinite(it.in.tmax) && it.in.tmax >= 0 && it.in.tmax < 0x1p60;
+        if (!merged_mode) {
+            if (p.has_expr || p.macro_mode != macro_mode) {
+                single((int)i);
+            } else if (p.S <= 16 && p.R <= 16 && times_ok) {
+                it.mapping = 7;
+                thread_items.push_back((int)i);
+            } else if (it.in.rates_per_traj) {
+                single((int)i);
+            } else {
+                it.mapping = 5;
+                warp_items.push_back((int)i);
+            }
+            continue;
         }
         // thread-per-trajectory classes: networks the generated kernels cover
-        const bool thread_ok = !p.has_expr && jit_supported(p) && ssa_spec_supported(probe, p.max_order) &&
-                               std::isfinite(it.in.tmax) && it.in.tmax >= 0 && it.in.tmax < 0x1p60;
+        const bool thread_ok = !p.has_expr && jit_supported(p) && ssa_spec_supported(probe, p.max_order) && times_ok;
         if (!thread_ok) {
-            if (p.has_expr || it.in.rates_per_traj) {
-                it.mapping = 0;  // generic kernel, a launch of its own
-                Class c;
-                c.kind = Class::Single;
-                c.items.push_back((int)i);
-                c.n_traj = it.in.n_traj;
-                classes.push_back(c);
+            if (p.has_expr || it.in.rates_per_traj || p.macro_mode != macro_mode) {
+                single((int)i);
             } else {
                 it.mapping = 5;
                 warp_items.push_back((int)i);
@@ -148,26 +176,28 @@ bool Batch::plan() {
         c.n_traj += it.in.n_traj;
         it.mapping = 4;
     }
-    // a thread launch for a handful of trajectories wastes the GPU: small
-    // classes join the warp batch (RB_BATCH_MIN_THREAD trajectories, default
-    // 2048, make a class worth its own launch)
-    int64_t min_thread = 2048;
-    if (const char *e = std::getenv("RB_BATCH_MIN_THREAD")) min_thread = std::max<int64_t>(1, std::atoll(e));
-    std::vector<Class> kept;
-    for (Class &c : classes) {
-        bool movable = c.kind == Class::Merged && c.n_traj < min_thread;
-        for (int i : c.items) movable = movable && !items[i].in.rates_per_traj;
-        if (!movable) {
-            kept.push_back(c);
-            continue;
+    if (merged_mode) {
+        // a thread launch for a handful of trajectories wastes the GPU: small
+        // classes join the warp batch (RB_BATCH_MIN_THREAD trajectories,
+        // default 2048, make a class worth its own launch)
+        int64_t min_thread = 2048;
+        if (const char *e = std::getenv("RB_BATCH_MIN_THREAD")) min_thread = std::max<int64_t>(1, std::atoll(e));
+        std::vector<Class> kept;
+        for (Class &c : classes) {
+            bool movable = c.kind == Class::Merged && c.n_traj < min_thread;
+            for (int i : c.items) movable = movable && !items[i].in.rates_per_traj;
+            if (!movable) {
+                kept.push_back(c);
+                continue;
+            }
+            for (int i : c.items) {
+                items[i].mapping = 5;
+                warp_items.push_back(i);
+            }
         }
-        for (int i : c.items) {
-            items[i].mapping = 5;
-            warp_items.push_back(i);
-        }
+        classes.swap(kept);
     }
-    classes.swap(kept);
-    // the warp batch: most work first
+    // warp items: most work first; thread units follow in item order
     std::vector<std::pair<double, int>> order;
     for (int i : warp_items) {
         const Item &it = items[i];
@@ -212,7 +242,7 @@ bool Batch::build(cudaStream_t st) {
         c.o_save = take(4 * (size_t)std::max(c.n_save, 1));
     }
     // warp batch items
-    int32_t maxS = 1, maxR = 1, maxP = 1, maxQ = 1, macro = 0;
+    int32_t maxS = 1, maxR = 1, maxP = 1, maxQ = 1;
     for (int i : warp_items) {
         Item &it = items[i];
         const Packed &p = it.packed;
@@ -220,7 +250,6 @@ bool Batch::build(cudaStream_t st) {
         maxR = std::max(maxR, p.R);
         maxP = std::max(maxP, p.P);
         maxQ = std::max(maxQ, p.Q);
-        macro |= p.macro_mode;
         const size_t RP = 32 * (size_t)((p.R + 31) / 32);
         it.o_x0 = take(8 * (size_t)(it.in.x0_per_traj ? it.in.n_traj : 1) * p.S);
         it.o_seeds = take(8 * (size_t)it.in.n_traj);
@@ -235,8 +264,25 @@ bool Batch::build(cudaStream_t st) {
         it.o_lfac = take(4 * RP * p.P);
         it.o_shape = take(4 * RP);
     }
+    // thread-unit items
+    int32_t maxTS = 1;
+    for (int i : thread_items) {
+        Item &it = items[i];
+        const Packed &p = it.packed;
+        maxTS = std::max(maxTS, p.S);
+        it.o_x0 = take(8 * (size_t)(it.in.x0_per_traj ? it.in.n_traj : 1) * p.S);
+        it.o_seeds = take(8 * (size_t)it.in.n_traj);
+        it.o_times = take(8 * (size_t)(it.in.nb_steps + 1));
+        it.o_save = take(4 * (size_t)std::max<size_t>(it.save.size(), 1));
+        it.o_rates = take(8 * (size_t)(it.in.rates && it.in.rates_per_traj ? it.in.n_traj : 1) * std::max(p.R, 1));
+        it.o_fpk = take(4 * (size_t)std::max(p.R * p.P, 1));
+        it.o_jsp = take(4 * (size_t)std::max(p.R * p.Q, 1));
+        it.o_jd = take(8 * (size_t)std::max(p.R * p.Q, 1));
+    }
     o_items = take(sizeof(SsaArgs) * std::max<size_t>(warp_items.size(), 1));
     o_start = take(8 * (warp_items.size() + 1));
+    o_titems = take(sizeof(SsaArgs) * std::max<size_t>(thread_items.size(), 1));
+    o_tunit = take(8 * (thread_items.size() + 1));
     in_bytes = off;
     // outputs
     for (Class &c : classes) {
@@ -244,6 +290,11 @@ bool Batch::build(cudaStream_t st) {
         c.o_events = take(8 * (size_t)std::max<int64_t>(c.n_traj, 1));
     }
     for (int i : warp_items) {
+        Item &it = items[i];
+        it.o_out = take(8 * (size_t)(it.in.nb_steps + 1) * it.save.size() * it.in.n_traj);
+        it.o_events = take(8 * (size_t)std::max<int64_t>(it.in.n_traj, 1));
+    }
+    for (int i : thread_items) {
         Item &it = items[i];
         it.o_out = take(8 * (size_t)(it.in.nb_steps + 1) * it.save.size() * it.in.n_traj);
         it.o_events = take(8 * (size_t)std::max<int64_t>(it.in.n_traj, 1));
@@ -265,13 +316,14 @@ bool Batch::build(cudaStream_t st) {
         std::memcpy(h + c.o_save, it0.save.data(), 4 * it0.save.size());
     }
     warp_warps = 0;
-    if (!warp_items.empty()) {
+    if (!warp_items.empty() || !thread_items.empty()) {
         SsaArgs la{};
         la.S = maxS;
         la.R = maxR;
         la.P = maxP;
         la.Q = maxQ;
         la.batch = reinterpret_cast<const SsaArgs *>(d + o_items);
+        la.tbatch_S = maxTS;
         warp_warps = ssa_warp_warps(la, ctx->smem_optin);
         if (warp_warps < 1) {
             set_error("the largest network of the batch does not fit the warp kernel");
@@ -338,23 +390,75 @@ bool Batch::build(cudaStream_t st) {
             }
         }
         start[warp_items.size()] = acc;
+        // thread units: 32 trajectories of one item each
+        int64_t *unit = reinterpret_cast<int64_t *>(h + o_tunit);
+        SsaArgs *targs = reinterpret_cast<SsaArgs *>(h + o_titems);
+        int64_t units = 0;
+        for (size_t k = 0; k < thread_items.size(); k++) {
+            Item &it = items[thread_items[k]];
+            const Packed &p = it.packed;
+            unit[k] = units;
+            units += (it.in.n_traj + 31) / 32;
+            const std::vector<double> ts = sample_times(it.in.tmax, it.in.nb_steps);
+            std::memcpy(h + it.o_times, ts.data(), 8 * ts.size());
+            std::memcpy(h + it.o_save, it.save.data(), 4 * it.save.size());
+            int32_t *fpk = reinterpret_cast<int32_t *>(h + it.o_fpk);
+            for (size_t f = 0; f < p.fac_sp.size(); f++) fpk[f] = p.fac_sp[f] | (p.fac_ord[f] << 16);
+            std::memcpy(h + it.o_jsp, p.jmp_sp.data(), 4 * p.jmp_sp.size());
+            std::memcpy(h + it.o_jd, p.jmp_d.data(), 8 * p.jmp_d.size());
+            SsaArgs &x = targs[k];
+            x = SsaArgs{};
+            x.S = p.S;
+            x.R = p.R;
+            x.P = p.P;
+            x.Q = p.Q;
+            x.macro_mode = p.macro_mode;
+            x.rate = reinterpret_cast<const double *>(d + it.o_rates);
+            x.rate_stride = it.in.rates && it.in.rates_per_traj ? p.R : 0;
+            x.fac_packed = reinterpret_cast<const int32_t *>(d + it.o_fpk);
+            x.jmp_sp = reinterpret_cast<const int32_t *>(d + it.o_jsp);
+            x.jmp_d = reinterpret_cast<const int64_t *>(d + it.o_jd);
+            x.n_traj = it.in.n_traj;
+            x.x0 = reinterpret_cast<const int64_t *>(d + it.o_x0);
+            x.x0_stride = it.in.x0_per_traj ? p.S : 0;
+            x.seeds = reinterpret_cast<const uint64_t *>(d + it.o_seeds);
+            x.sample_t = reinterpret_cast<const double *>(d + it.o_times);
+            x.n_samples = it.in.nb_steps + 1;
+            x.save_idx = reinterpret_cast<const int32_t *>(d + it.o_save);
+            x.n_save = (int32_t)it.save.size();
+            x.out = reinterpret_cast<int64_t *>(d + it.o_out);
+            x.events = reinterpret_cast<uint64_t *>(d + it.o_events);
+            x.zig = ctx->zig;
+        }
+        unit[thread_items.size()] = units;
         warp_traj = acc;
         warp_args = SsaArgs{};
         warp_args.S = maxS;
         warp_args.R = maxR;
         warp_args.P = maxP;
         warp_args.Q = maxQ;
-        warp_args.macro_mode = macro;
-        warp_args.n_traj = acc;
+        warp_args.macro_mode = macro_mode;
+        warp_args.n_traj = acc + units;
+        warp_args.n_warp_tickets = acc;
         warp_args.batch = reinterpret_cast<const SsaArgs *>(d + o_items);
         warp_args.batch_start = reinterpret_cast<const int64_t *>(d + o_start);
         warp_args.batch_n = (int32_t)warp_items.size();
+        warp_args.tbatch = reinterpret_cast<const SsaArgs *>(d + o_titems);
+        warp_args.tbatch_unit = reinterpret_cast<const int64_t *>(d + o_tunit);
+        warp_args.tbatch_n = (int32_t)thread_items.size();
+        warp_args.tbatch_S = maxTS;
         warp_args.work = reinterpret_cast<unsigned long long *>(d + o_work);
         warp_args.zig = ctx->zig;
         warp_args.budget_ns = kernel_budget_ns();
         const int per_sm = std::max(1, ssa_warp_occupancy(warp_args, warp_warps, ssa_warp_smem(warp_args, warp_warps)));
         warp_grid = (int)std::max<int64_t>(
-            1, std::min<int64_t>((acc + warp_warps - 1) / warp_warps, (int64_t)ctx->sm_count * per_sm));
+            1, std::min<int64_t>((acc + units + warp_warps - 1) / warp_warps, (int64_t)ctx->sm_count * per_sm));
+        if (warp_cnt0) cudaFree(warp_cnt0);
+        warp_cnt0 = nullptr;
+        if (!cuda_ok(cudaMalloc(&warp_cnt0, 8 * (size_t)warp_grid * warp_warps * std::max(maxS, 1)),
+                     "cudaMalloc(interval-start counts)"))
+            return false;
+        warp_args.warp_cnt0 = warp_cnt0;
     }
 
     // ---------------- every class's network on the device, kernels compiled
@@ -377,7 +481,7 @@ bool Batch::build(cudaStream_t st) {
     ok = ok && cuda_ok(cudaMemsetAsync(d + o_work, 0, 32, st), "cudaMemsetAsync");
     ok = ok && cuda_ok(cudaEventRecord(fork, st), "cudaEventRecord") &&
          cuda_ok(cudaStreamWaitEvent(side, fork, 0), "cudaStreamWaitEvent");
-    if (ok && !warp_items.empty()) {
+    if (ok && (!warp_items.empty() || !thread_items.empty())) {
         const int err = launch_ssa_warp(warp_args, warp_warps, warp_grid, ssa_warp_smem(warp_args, warp_warps), side);
         ok = err == 0 || cuda_ok((cudaError_t)err, "warp batch launch");
     }
@@ -458,6 +562,7 @@ void Batch::stage_inputs() {
         const Item &it = items[i];
         const Packed &p = it.packed;
         const int64_t n = it.in.n_traj;
+        if (n == 0) continue;
         std::memcpy(h + it.o_x0, it.in.x0, 8 * (size_t)(it.in.x0_per_traj ? n : 1) * p.S);
         std::memcpy(h + it.o_seeds, it.in.seeds, 8 * (size_t)n);
         const double *rt = it.in.rates ? it.in.rates : p.rate.data();
@@ -473,6 +578,18 @@ void Batch::stage_inputs() {
             rdf[2 * q] = std::isfinite(v) ? hi : 0.0f;
             rdf[2 * q + 1] = std::isfinite(v) ? (float)(v - (double)hi) : 0.0f;
         }
+    }
+    for (int i : thread_items) {
+        const Item &it = items[i];
+        const Packed &p = it.packed;
+        const int64_t n = it.in.n_traj;
+        if (n == 0) continue;
+        std::memcpy(h + it.o_x0, it.in.x0, 8 * (size_t)(it.in.x0_per_traj ? n : 1) * p.S);
+        std::memcpy(h + it.o_seeds, it.in.seeds, 8 * (size_t)n);
+        if (it.in.rates)
+            std::memcpy(h + it.o_rates, it.in.rates, 8 * (size_t)(it.in.rates_per_traj ? n : 1) * p.R);
+        else
+            std::memcpy(h + it.o_rates, p.rate.data(), 8 * (size_t)p.R);
     }
 }
 
@@ -496,7 +613,8 @@ void Batch::unstage_outputs(uint64_t &events) {
             base += n;
         }
     }
-    for (int i : warp_items) {
+    for (const std::vector<int> *list : {&warp_items, &thread_items})
+    for (int i : *list) {
         const Item &it = items[i];
         const int64_t n = it.in.n_traj;
         const size_t ob = 8 * (size_t)(it.in.nb_steps + 1) * it.save.size() * n;
@@ -534,7 +652,7 @@ bool Batch::run(rb_stats_out &st_out) {
     unsigned long long flag = 0;
     const unsigned long long *wk =
         reinterpret_cast<const unsigned long long *>(static_cast<unsigned char *>(host) + o_work);
-    flag |= warp_items.empty() ? 0 : wk[2];
+    flag |= warp_items.empty() && thread_items.empty() ? 0 : wk[2];
     for (Class &c : classes) {
         unsigned long long sc[4] = {0, 0, 0, 0};
         if (c.scratch && cudaMemcpy(sc, c.scratch, sizeof sc, cudaMemcpyDeviceToHost) == cudaSuccess) flag |= sc[2];
@@ -549,7 +667,7 @@ bool Batch::run(rb_stats_out &st_out) {
     st_out.graph_ms = ms;
     st_out.h2d = in_bytes;
     st_out.d2h = total_bytes - in_bytes;
-    st_out.launches = (int)classes.size() + (warp_items.empty() ? 0 : 1);
+    st_out.launches = (int)classes.size() + (warp_items.empty() && thread_items.empty() ? 0 : 1);
     st_out.replayed = !first;
     return !flag;
 }
@@ -559,6 +677,8 @@ void Batch::free_device() {
     exec = nullptr;
     if (dev) cudaFree(dev);
     dev = nullptr;
+    if (warp_cnt0) cudaFree(warp_cnt0);
+    warp_cnt0 = nullptr;
     if (host) cudaFreeHost(host);
     host = nullptr;
     if (side) cudaStreamDestroy(side);

@@ -44,7 +44,7 @@ struct Batch {
         std::vector<int32_t> save;
         int mapping = -1;
         size_t o_x0 = 0, o_seeds = 0, o_times = 0, o_save = 0, o_rates = 0, o_fsp = 0, o_ford = 0, o_jsp = 0,
-               o_jd = 0, o_rdf = 0, o_lfac = 0, o_shape = 0, o_out = 0, o_events = 0;
+               o_jd = 0, o_rdf = 0, o_lfac = 0, o_shape = 0, o_fpk = 0, o_out = 0, o_events = 0;
     };
     // A launch of the thread-per-trajectory kernels: items of one structure
     // and sample grid merged (Merged), or one item alone (Single).
@@ -60,12 +60,15 @@ struct Batch {
 
     std::vector<Item> items;
     std::vector<Class> classes;
-    std::vector<int> warp_items;  // items of the warp kernel's batch, most work first
+    std::vector<int> warp_items;    // warp-per-trajectory items of the persistent launch, most work first
+    std::vector<int> thread_items;  // its thread-unit items (32 trajectories a unit, one per lane)
+    int macro_mode = 0;             // arithmetic of the persistent launch's items
     bool planned = false;
 
     // device state of the captured graph
     void *host = nullptr, *dev = nullptr;
-    size_t in_bytes = 0, total_bytes = 0, o_items = 0, o_start = 0, o_work = 0;
+    int64_t *warp_cnt0 = nullptr;  // the warp kernel's interval-start counts
+    size_t in_bytes = 0, total_bytes = 0, o_items = 0, o_start = 0, o_work = 0, o_titems = 0, o_tunit = 0;
     SsaArgs warp_args{};
     int warp_warps = 0, warp_grid = 0;
     int64_t warp_traj = 0;

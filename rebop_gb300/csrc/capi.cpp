@@ -800,11 +800,11 @@ int rb_batch_run(rb_batch *b, rb_run_stats *stats) {
     return st.timeout ? RB_ERR_TIMEOUT : RB_ERR_CUDA;
 }
 
-int rb_batch_plan(rb_batch *b, int32_t *n_thread_launches, int32_t *n_warp_items) {
+int rb_batch_plan(rb_batch *b, int32_t *n_own_launches, int32_t *n_persistent_items) {
     if (!b) return fail(RB_ERR_INVALID, "null batch");
     if (!b->b.planned) b->b.plan();
-    if (n_thread_launches) *n_thread_launches = (int32_t)b->b.classes.size();
-    if (n_warp_items) *n_warp_items = (int32_t)b->b.warp_items.size();
+    if (n_own_launches) *n_own_launches = (int32_t)b->b.classes.size();
+    if (n_persistent_items) *n_persistent_items = (int32_t)(b->b.warp_items.size() + b->b.thread_items.size());
     return RB_OK;
 }
 

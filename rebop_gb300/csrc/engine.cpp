@@ -103,6 +103,7 @@ DeviceNet::~DeviceNet() {
     if (desc) cudaFree(desc);
     if (scratch) cudaFree(scratch);
     if (dep) cudaFree(dep);
+    if (warp_cnt0) cudaFree(warp_cnt0);
     if (io) cudaFree(io);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_stop) cudaEventDestroy(ev_stop);
@@ -377,6 +378,18 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
                 return false;
             dn.dep_version = dn.version;
         }
+        const size_t n_cnt0 = (size_t)blocks * warp_w * std::max(p.S, 1);
+        if (dn.warp_cnt0_n < n_cnt0) {
+            if (dn.warp_cnt0) {
+                cudaStreamSynchronize(stream);
+                cudaFree(dn.warp_cnt0);
+            }
+            dn.warp_cnt0 = nullptr;
+            dn.warp_cnt0_n = 0;
+            if (!cuda_ok(cudaMalloc(&dn.warp_cnt0, 8 * n_cnt0), "cudaMalloc(interval-start counts)")) return false;
+            dn.warp_cnt0_n = n_cnt0;
+        }
+        a.warp_cnt0 = dn.warp_cnt0;
         const char *wd = std::getenv("RB_WARP_DEPS");
         if (dn.dep_ok && !(wd && std::strcmp(wd, "0") == 0)) a.dep_tab = dn.dep;
         if (const char *xc = std::getenv("RB_WARP_EXACT_CHOICE")) a.exact_choice = std::strcmp(xc, "0") != 0;

@@ -56,6 +56,8 @@ struct DeviceNet {
     cudaStream_t last_stream = nullptr; // stream of the last device-pointer run
     int64_t runs = 0;                   // sampled launches of this network
     double out_gbs = 0;                 // sample bytes / kernel time of the last host-pointer run
+    int64_t *warp_cnt0 = nullptr;       // warp kernel interval-start counts
+    size_t warp_cnt0_n = 0;             //   (entries)
     uint16_t *dep = nullptr;            // warp kernel dependency table [R][32]
     uint64_t dep_version = 0;           //   for this descriptor version (0: none built)
     bool dep_ok = false;                //   false: the network is beyond the lists' reach

@@ -102,6 +102,10 @@ struct SsaArgs {
     // fires only those are re-evaluated (one coalesced load per step).  Null:
     // every propensity is re-evaluated at every step.
     const uint16_t *dep_tab;
+    // Warp-per-trajectory kernel: [blocks x warps per block][S] counts at the
+    // start of each warp's current sample interval (read only by an exact
+    // re-run of the interval, so they stay out of shared memory).
+    int64_t *warp_cnt0;
     // Warp-per-trajectory kernel: decide every choice with the exact fold, as
     // for a close float-pair comparison (RB_WARP_EXACT_CHOICE=1; tests).
     int32_t exact_choice;
@@ -119,6 +123,19 @@ struct SsaArgs {
     const float2 *lm_rdf;
     const uint32_t *lm_shape;
     const int32_t *lm_fac;
+    // The same launch also runs thread units (batch != null): tickets below
+    // n_warp_tickets are the warp items' trajectories, ticket
+    // n_warp_tickets + u is thread unit u -- up to 32 trajectories of one
+    // small-network item, one per lane, each run by the exact per-lane step.
+    // Thread item k is tbatch[k]; its units are tbatch_unit[k] ..
+    // tbatch_unit[k + 1] - 1, 32 trajectories each (the last one partial);
+    // tbatch_S is the largest species count of the thread items.
+    const SsaArgs *tbatch;
+    const int64_t *tbatch_unit;
+    int32_t tbatch_n, tbatch_S;
+    int64_t n_warp_tickets;
+    // A thread item's reactant factors [R][P], species | order << 16.
+    const int32_t *fac_packed;
 };
 
 // Launch the thread-per-trajectory kernel; returns a cudaError_t value.

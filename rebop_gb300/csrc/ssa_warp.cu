@@ -53,9 +53,9 @@ __host__ __device__ inline int warp_group(int C) { return C > 256 ? (C + 31) / 3
 __host__ __device__ inline int warp_ngroups(int C) { return (C + warp_group(C) - 1) / warp_group(C); }
 
 // Shared memory: block tables (Exp1 tables, float-pair rates when shared,
-// reactant factors in both layouts, jumps), then per warp: counts, counts at
-// the interval start, float-pair propensities (and float-pair rates when per
-// trajectory).
+// reactant factors in both layouts, jumps), then per warp: counts,
+// float-pair propensities (and float-pair rates when per trajectory).  The
+// counts at the interval start go to global memory (SsaArgs::warp_cnt0).
 __host__ __device__ inline WarpLayout warp_layout(const SsaArgs &a) {
     WarpLayout l;
     const size_t RP = 32 * (size_t)warp_chunk(a.R);     // lane-major positions
@@ -68,14 +68,23 @@ __host__ __device__ inline WarpLayout warp_layout(const SsaArgs &a) {
         b += 16;                                            // alignment of the jump deltas
     }
     l.block_bytes = (b + 15) & ~(size_t)15;
-    size_t w = 16 * (size_t)a.S;                        // counts, interval-start counts
+    size_t w = 8 * (size_t)a.S;                         // counts
     w += 4 * ((size_t)a.S + 1);                         // counts as floats, plus the constant 1
     w += 8 * RP + 8;                                    // propensities (lane-major), alignment
     if (a.rate_stride) w += 8 * RP;                     // per-trajectory float-pair rates
     if (!a.batch) w += 8 * 32 * (size_t)warp_ngroups(warp_chunk(a.R)) + 4 * 32;  // group sums, dirty masks
+    const size_t wt = 8 * 32 * (size_t)a.tbatch_S;          // a thread unit's counts [S][32]
+    if (a.batch && wt > w) w = wt;
     l.warp_bytes = (w + 15) & ~(size_t)15;
     return l;
 }
+
+// Physical slot of the float-pair propensity at lane-major position pos
+// (reaction l*C + i at i*32 + l): the lane bits are XORed with the row, so a
+// row read by the 32 lanes (the chunk sums) and a column read by the 32 lanes
+// (the walk through one lane's chunk to the chosen reaction) both touch 32
+// distinct banks.  Without it every lane of the walk hit the same bank.
+__device__ __forceinline__ int pz(int pos) { return pos ^ ((pos >> 5) & 31); }
 
 __device__ __forceinline__ DF shfl_df(DF v, int src) {
     return DF{__shfl_sync(0xffffffffu, v.h, src), __shfl_sync(0xffffffffu, v.l, src)};
@@ -220,9 +229,57 @@ __host__ __device__ inline uint32_t shape_word(const int32_t *fac_sp, const int3
     return sl[0] | of[0] << 15 | sl[1] << 16 | of[1] << 31;
 }
 
+// One thread unit of a persistent batch: lane l runs trajectory
+// first + l of the small-network item `it` (if it has one) from start to end
+// with the exact per-lane step of the thread kernels (ssa_exact.cuh: binary64
+// in exact integer emulation, native binary64 outside its domain), so its
+// counts, events and draws are rebop's.  sp is this warp's [S][32] count
+// block.  Returns the lane's event count; sets `late` if the wall-clock budget
+// ran out (the trajectory is then incomplete).
+template <bool MACRO>
+__device__ __noinline__ unsigned long long thread_unit(const SsaArgs &it, const ExactTables &zt, int64_t *sp,
+                                                       long long first, int64_t t_start, int64_t budget_ns,
+                                                       bool &late) {
+    const int lane = threadIdx.x & 31;
+    const long long traj = first + lane;
+    unsigned long long ev = 0;
+    if (traj >= it.n_traj) return 0;
+    const ExactTables m{zt.zxk, zt.zf, zt.zd, it.fac_packed, it.jmp_sp, it.jmp_d};
+    int64_t *c = sp + lane;  // column of this lane: c[s * 32]
+    for (int s = 0; s < it.S; ++s) c[s * 32] = it.x0[traj * it.x0_stride + s];
+    Xoshiro g;
+    xo_seed(g, it.seeds[traj]);
+    const uint64_t *rl = reinterpret_cast<const uint64_t *>(it.rate + traj * it.rate_stride);
+    bool nat = false;
+    for (int r = 0; r < it.R; ++r) nat |= !emul_domain(rl[r]);
+    uint64_t t = 0;
+    for (long long i = 0; i < it.n_samples; ++i) {
+        const uint64_t T = (uint64_t)__double_as_longlong(it.sample_t[i]);
+        const bool natT = nat || !emul_domain(T);
+        for (unsigned int n = 1;; ++n) {
+            if ((n & 255u) == 0 && global_ns() - t_start > budget_ns) {
+                late = true;
+                return ev;
+            }
+            int ix;
+            uint64_t tx;
+            if (!exact_step<16, MACRO, false>(it, m, c, rl, 1, 32, g, t, T, natT, ix, tx)) break;
+            t = tx;
+            ++ev;
+            if (ix < it.R)
+                for (int k = 0; k < it.Q; ++k) c[it.jmp_sp[ix * it.Q + k] * 32] += it.jmp_d[ix * it.Q + k];
+        }
+        t = T;  // the sample records at T (gillespie.rs:328-330)
+        int64_t *o = it.out + (size_t)i * it.n_save * it.n_traj + traj;
+        for (int k = 0; k < it.n_save; ++k) o[(size_t)k * it.n_traj] = c[it.save_idx[k] * 32];
+    }
+    if (it.events) it.events[traj] = ev;
+    return ev;
+}
+
 // BATCH: the launch runs a.batch's networks (each item's tables in global
-// memory, lane-major); otherwise the one network of `a`, whose tables the
-// block copies to shared memory.
+// memory, lane-major) and a.tbatch's thread units; otherwise the one network
+// of `a`, whose tables the block copies to shared memory.
 template <bool MACRO, bool BATCH>
 __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const __grid_constant__ SsaArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -281,8 +338,8 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
     // ---- this warp's region (sized for the largest network)
     unsigned char *wbase = g_spec_smem + L.block_bytes + (size_t)warp * L.warp_bytes;
     int64_t *cnt = reinterpret_cast<int64_t *>(wbase);
-    int64_t *cnt0 = cnt + a.S;
-    float *cntf = reinterpret_cast<float *>(cnt0 + a.S);  // [S + 1]
+    int64_t *cnt0 = a.warp_cnt0 + ((size_t)blockIdx.x * nw + warp) * (size_t)a.S;  // global
+    float *cntf = reinterpret_cast<float *>(cnt + a.S);  // [S + 1]
     float2 *prop = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(cntf + a.S + 1) + 7) & ~(uintptr_t)7);
     float2 *rdf_w = prop + RP0;  // per-trajectory float-pair rates (single-network mode)
     float2 *gsum = rdf_w + (a.rate_stride ? RP0 : 0);  // group sums [NG][32] (one network only)
@@ -298,6 +355,28 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
         if (lane == 0) ticket = (long long)atomicAdd(a.work, 1ull);
         ticket = __shfl_sync(0xffffffffu, ticket, 0);
         if (ticket >= a.n_traj) break;
+
+        // ---- a thread unit: 32 trajectories of a small network, one per lane
+        if (BATCH && ticket >= a.n_warp_tickets) {
+            const long long u = ticket - a.n_warp_tickets;
+            int lo = 0, hi = a.tbatch_n - 1;  // last item with tbatch_unit <= u
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (a.tbatch_unit[mid] <= u) lo = mid;
+                else hi = mid - 1;
+            }
+            bool late = false;
+            unsigned long long ev = thread_unit<MACRO>(a.tbatch[lo], ex, reinterpret_cast<int64_t *>(wbase),
+                                                       (u - a.tbatch_unit[lo]) * 32, t_start, a.budget_ns, late);
+            for (int off = 16; off > 0; off >>= 1) ev += __shfl_xor_sync(0xffffffffu, ev, off);
+            warp_events += ev;
+            if (__any_sync(0xffffffffu, late)) {
+                if (lane == 0) atomicExch(a.work + 2, 1ull);
+                break;
+            }
+            __syncwarp();
+            continue;
+        }
 
         // ---- the trajectory's network and run
         long long traj = ticket;
@@ -372,7 +451,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                 DF v[8];
 #pragma unroll
                 for (int t = 0; t < 8; ++t) {
-                    const float2 q = b + t < e ? prop[(b + t) * 32 + lane] : make_float2(0.f, 0.f);
+                    const float2 q = b + t < e ? prop[pz((b + t) * 32 + lane)] : make_float2(0.f, 0.f);
                     v[t] = DF{q.x, q.y};
                 }
                 return df_add(df_add(df_add(v[0], v[1]), df_add(v[2], v[3])),
@@ -380,7 +459,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
             }
             DF s{0.f, 0.f};
             for (int i2 = b; i2 < e; ++i2) {
-                const float2 q = prop[i2 * 32 + lane];
+                const float2 q = prop[pz(i2 * 32 + lane)];
                 s = df_add(s, DF{q.x, q.y});
             }
             return s;
@@ -463,7 +542,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                     ls = DF{0.f, 0.f};
                     for (int i2 = 0; i2 < n_own; ++i2) {
                         const DF acc = eval_prop(i2 * 32 + lane, amb);
-                        prop[i2 * 32 + lane] = make_float2(acc.h, acc.l);
+                        prop[pz(i2 * 32 + lane)] = make_float2(acc.h, acc.l);
                         ls = df_add(ls, acc);
                     }
                 } else if (need_full) {
@@ -471,7 +550,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                         const int e = min(n_own, (g + 1) * GS);
                         for (int i2 = g * GS; i2 < e; ++i2) {
                             const DF acc = eval_prop(i2 * 32 + lane, amb);
-                            prop[i2 * 32 + lane] = make_float2(acc.h, acc.l);
+                            prop[pz(i2 * 32 + lane)] = make_float2(acc.h, acc.l);
                         }
                         const DF gs = group_sum(g);
                         gsum[g * 32 + lane] = make_float2(gs.h, gs.l);
@@ -552,7 +631,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                         const bool valid = j < C && k * C + j < R;
                         DF v{0.f, 0.f};
                         if (valid) {
-                            const float2 pa = prop[j * 32 + k];
+                            const float2 pa = prop[pz(j * 32 + k)];
                             v = DF{pa.x, pa.y};
                         }
 #pragma unroll
@@ -596,7 +675,7 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                     } else {
                         if (lane >= 1 && lane <= nd) {
                             const DF acc = eval_prop(v, amb_next);
-                            prop[v] = make_float2(acc.h, acc.l);
+                            prop[pz(v)] = make_float2(acc.h, acc.l);
                             atomicOr(&dmask[v & 31], 1u << ((v >> 5) / GS));
                         }
                         __syncwarp();

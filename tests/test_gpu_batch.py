@@ -2,9 +2,9 @@
 
 Every item of a batch must give exactly what Network.run_ensemble gives for
 the same network, inputs and seeds -- which the parity tests pin to the
-oracle -- whether it ran merged with other parameter sets, in the warp
-kernel's batch mode, or alone; and again when the captured graph is replayed
-with new seeds.
+oracle -- whether it ran as thread units or a warp per trajectory in the
+persistent launch, merged with other parameter sets, or alone; and again when
+the captured graph is replayed with new seeds.
 """
 
 import numpy as np
@@ -66,17 +66,17 @@ def test_batch_matches_individual_runs(rb):
     seeds = rng.integers(np.iinfo(np.uint64).max, size=32, dtype=np.uint64)
     specs.append((b.add(mm, [30, 300, 0, 0], seeds, 5.0, 10, rates=per), mm, [30, 300, 0, 0], seeds, 5.0, 10,
                   per, None))
-    n_thread, n_warp = b.plan()
-    # the Michaelis-Menten sets merge with the per-trajectory-rate item (which
-    # only a thread launch runs) into one class; the rate expression runs
-    # alone; the small 8-species class and the other networks join the warp batch
-    assert n_warp == 4 and n_thread == 2
+    n_own, n_persistent = b.plan()
+    # one persistent launch: the Michaelis-Menten sets, the per-trajectory-rate
+    # item and the 8-species 16-reaction network as thread units, the larger
+    # networks a warp per trajectory; the rate expression runs alone
+    assert n_own == 1 and n_persistent == 45
     st = b.run()
-    assert st["mapping"] == 6 and st["events"] > 0
+    assert st["mapping"] == 6 and st["events"] > 0 and st["kernel_launches"] == 2
     for k, net, x0, seeds, tmax, nb, rates, save in specs:
         _check(b, k, net, x0, seeds, tmax, nb, rates, save)
-    assert {b.mapping(k) for k in list(range(40)) + [45]} <= {2, 3, 4}
-    assert {b.mapping(k) for k in range(40, 44)} == {5}
+    assert {b.mapping(k) for k in list(range(41)) + [45]} == {7}
+    assert {b.mapping(k) for k in range(41, 44)} == {5}
     assert b.mapping(44) == 0
     # replay the captured graph with new seeds
     for k, net, x0, seeds, tmax, nb, rates, save in specs:
@@ -87,8 +87,10 @@ def test_batch_matches_individual_runs(rb):
 
 
 def test_batch_merges_parameter_sets(rb, monkeypatch):
-    # With every class worth a launch, parameter sets of one network run as one
-    # thread-per-trajectory ensemble with per-trajectory rates and counts.
+    # The merged plan: with every class worth a launch, parameter sets of one
+    # network run as one thread-per-trajectory ensemble with per-trajectory
+    # rates and counts.
+    monkeypatch.setenv("RB_BATCH_MODE", "merged")
     monkeypatch.setenv("RB_BATCH_MIN_THREAD", "1")
     rng = np.random.default_rng(6)
     b = rb.Batch()
@@ -122,8 +124,8 @@ def test_batch_of_networks_beyond_256_reactions(rb):
         x0 = rng.integers(0, 501, size=S).tolist()
         seeds = rng.integers(np.iinfo(np.uint64).max, size=24, dtype=np.uint64)
         specs.append((b.add(net, x0, seeds, 1e-3, 5), net, x0, seeds, 1e-3, 5, None, None))
-    n_thread, n_warp = b.plan()
-    assert n_warp == 2 and n_thread == 0
+    n_own, n_persistent = b.plan()
+    assert n_persistent == 2 and n_own == 0
     st = b.run()
     assert st["events"] > 0
     for k, net, x0, seeds, tmax, nb, rates, save in specs:

@@ -246,10 +246,15 @@ def test_generated_network_compiles(rb, tmp_path, monkeypatch):
     assert len(list(tmp_path.glob("net_*.cubin"))) == 1
 
 
-def test_batch_plan_groups_by_structure(rb):
-    # Parameter sets of one network merge into one thread-per-trajectory
-    # launch; large networks and rate expressions go elsewhere.
+def test_batch_plan_groups_by_structure(rb, monkeypatch):
+    # The persistent plan: small networks (at most 16 species and reactions)
+    # become thread units, larger ones a warp per trajectory, rate expressions
+    # and define_system! networks of the other arithmetic launches of their
+    # own.  The merged plan: parameter sets of one network merge into one
+    # thread-per-trajectory launch.
     import bench
+
+    from rebop_gb300 import expr as E
 
     b = rb.Batch()
     mm = rb.Network(4)  # E + S <-> ES -> E + P
@@ -259,30 +264,40 @@ def test_batch_plan_groups_by_structure(rb):
     seeds = np.arange(8, dtype=np.uint64)
     for k in range(3):
         assert b.add(mm, [50, 500, 0, 0], seeds, 10.0, 5, rates=[0.01 * (k + 1), 0.1, 0.05]) == k
-    b.add(mm, [50, 500, 0, 0], seeds, 20.0, 5)  # another horizon: another launch
+    b.add(mm, [50, 500, 0, 0], seeds, 20.0, 5)
     reactions, x0 = bench.random_network(3, 20, 60)
     big = rb.Network(20)
     for k, e, d in reactions:
         big.add_reaction(rb.Rate.lma(k, e), d)
     b.add(big, x0, seeds, 0.01, 4)
     b.add(big, x0, seeds, 0.02, 4)
+    ex = rb.Network(2)
+    ex.add_reaction(rb.Rate.expression(E.parse("3 + A / 4").to_expr({"A": 0}, {})), [1, 0])
+    b.add(ex, [0, 0], seeds, 1.0, 4)
+    d = rb.Network.from_dsl("k; Bd { A } r: A => @ k")
+    d.set_param("k", 1.0)
+    b.add(d, [5], seeds, 1.0, 4)
+    assert b.plan() == (2, 6)
+    assert [b.mapping(k) for k in range(8)] == [7, 7, 7, 7, 5, 5, 0, 0]
+    monkeypatch.setenv("RB_BATCH_MODE", "merged")
     # parameter sets merge by structure and horizon; classes below
     # RB_BATCH_MIN_THREAD trajectories join the warp batch
-    assert b.plan() == (0, 6)
-    assert [b.mapping(k) for k in range(6)] == [5] * 6
-    import os
-
-    os.environ["RB_BATCH_MIN_THREAD"] = "1"
-    try:
-        b2 = rb.Batch()
-        for k in range(3):
-            b2.add(mm, [50, 500, 0, 0], seeds, 10.0, 5, rates=[0.01 * (k + 1), 0.1, 0.05])
-        b2.add(mm, [50, 500, 0, 0], seeds, 20.0, 5)
-        b2.add(big, x0, seeds, 0.01, 4)
-        assert b2.plan() == (2, 1)
-        assert [b2.mapping(k) for k in range(5)] == [4, 4, 4, 4, 5]
-    finally:
-        del os.environ["RB_BATCH_MIN_THREAD"]
+    b1 = rb.Batch()
+    for k in range(3):
+        b1.add(mm, [50, 500, 0, 0], seeds, 10.0, 5, rates=[0.01 * (k + 1), 0.1, 0.05])
+    b1.add(mm, [50, 500, 0, 0], seeds, 20.0, 5)
+    b1.add(big, x0, seeds, 0.01, 4)
+    b1.add(big, x0, seeds, 0.02, 4)
+    assert b1.plan() == (0, 6)
+    assert [b1.mapping(k) for k in range(6)] == [5] * 6
+    monkeypatch.setenv("RB_BATCH_MIN_THREAD", "1")
+    b2 = rb.Batch()
+    for k in range(3):
+        b2.add(mm, [50, 500, 0, 0], seeds, 10.0, 5, rates=[0.01 * (k + 1), 0.1, 0.05])
+    b2.add(mm, [50, 500, 0, 0], seeds, 20.0, 5)
+    b2.add(big, x0, seeds, 0.01, 4)
+    assert b2.plan() == (2, 1)
+    assert [b2.mapping(k) for k in range(5)] == [4, 4, 4, 4, 5]
     with pytest.raises(ValueError):
         b.add(mm, [1, 2, 3], seeds, 1.0, 2)
 
