@@ -8,11 +8,14 @@
 //     (dZ W) and the weight gradient (dZ^T H).
 //   * bias_silu: Z += b; H = bf16(silu(Z)) (or identity for the head).
 //   * silu_backward: dZ = dH * silu'(Z), plus the bias gradient.
-//   * mdn_loss: negative log-likelihood of a K-component diagonal Gaussian
-//     mixture in two dimensions and its gradient with respect to the head's
-//     raw outputs (logits, means, softplus scales).
+//   * count_loss: negative log-likelihood of the count-aware head (per
+//     species a categorical over the counts 0 .. 30 and a tail class, the
+//     tail a Gaussian mixture over the log-count residual) and its gradient
+//     with respect to the head's raw outputs.
+//   * mdn_loss: the same for a K-component diagonal Gaussian mixture in two
+//     dimensions.
 //   * adam: FP32 master weights, BF16 copies refreshed in place.
-//   * mdn_sample: one draw from each row's mixture.
+//   * mdn_sample / count_sample: draws from each row's distribution.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -354,6 +357,65 @@ __global__ void mdn_loss_kernel(const float *O, const float *Y, int B, int K, fl
     }
 }
 
+// Count-aware head, per species s a block of kHS outputs at s * kHS:
+// logits[kNC] (class c < kNC - 1: the count c; class kNC - 1: a count of at
+// least kNC - 1), then the tail's kKT weight logits, means and raw scales
+// (sigma = softplus(raw) + 1e-3) over the residual y = log(n + v) - b_s of a
+// tail count n (v ~ U[0, 1), b_s the rate-equation log mean).  Y rows are
+// (n_protein, n_dimer, y_protein, y_dimer).  loss[row] = sum_s -log P_s with
+// P_s = pi_c for a small count c, pi_tail * sum_k w_k N(y; mu_k, sigma_k) for
+// a tail count; G = d(mean loss)/d(raw head outputs).
+constexpr int kNC = 32, kKT = 4, kHS = kNC + 3 * kKT;
+
+__global__ void count_loss_kernel(const float *O, const float *Y, int B, float *loss, float *G) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= B) return;
+    const float inv_b = 1.0f / (float)B;
+    float total = 0.0f;
+    for (int sp = 0; sp < 2; ++sp) {
+        const float *o = O + (size_t)row * 2 * kHS + sp * kHS;
+        float *gr = G + (size_t)row * 2 * kHS + sp * kHS;
+        const float n = Y[4 * row + sp], y = Y[4 * row + 2 + sp];
+        const int c = n < (float)(kNC - 1) ? (int)n : kNC - 1;
+        float lmax = -1e30f;
+        for (int k = 0; k < kNC; ++k) lmax = fmaxf(lmax, o[k]);
+        float zs = 0.0f;
+        for (int k = 0; k < kNC; ++k) zs += __expf(o[k] - lmax);
+        const float logz = lmax + logf(zs);
+        total += logz - o[c];
+        for (int k = 0; k < kNC; ++k) gr[k] = (__expf(o[k] - logz) - (k == c ? 1.0f : 0.0f)) * inv_b;
+        const float *tw = o + kNC, *tm = tw + kKT, *ts = tm + kKT;
+        float *gw = gr + kNC, *gm = gw + kKT, *gs = gm + kKT;
+        if (c < kNC - 1) {
+            for (int k = 0; k < kKT; ++k) gw[k] = gm[k] = gs[k] = 0.0f;
+            continue;
+        }
+        float wmax = -1e30f;
+        for (int k = 0; k < kKT; ++k) wmax = fmaxf(wmax, tw[k]);
+        float ws = 0.0f;
+        for (int k = 0; k < kKT; ++k) ws += __expf(tw[k] - wmax);
+        const float logw = wmax + logf(ws);
+        float lp[kKT], mx = -1e30f;
+        for (int k = 0; k < kKT; ++k) {
+            const float sg = softplusf_(ts[k]) + 1e-3f, e = (y - tm[k]) / sg;
+            lp[k] = (tw[k] - logw) - 0.5f * e * e - logf(sg) - 0.9189385332f;
+            mx = fmaxf(mx, lp[k]);
+        }
+        float tot = 0.0f;
+        for (int k = 0; k < kKT; ++k) tot += __expf(lp[k] - mx);
+        const float ll = mx + logf(tot);
+        total -= ll;
+        for (int k = 0; k < kKT; ++k) {
+            const float r = __expf(lp[k] - ll), w = __expf(tw[k] - logw);
+            const float sg = softplusf_(ts[k]) + 1e-3f, e = (y - tm[k]) / sg;
+            gw[k] = (w - r) * inv_b;
+            gm[k] = -r * e / sg * inv_b;
+            gs[k] = r * (1.0f - e * e) / sg * sigmoidf_(ts[k]) * inv_b;
+        }
+    }
+    loss[row] = total;
+}
+
 __global__ void adam_kernel(float *w, __nv_bfloat16 *wb, const float *g, float *m, float *v, int n, float lr,
                             float b1, float b2, float eps, float c1, float c2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -456,11 +518,80 @@ __global__ void rre_kernel(const float *rates, const float *tq, int Q, int S, in
     for (int j = 0; j < n_out; ++j) out[(size_t)q * n_out + j] = x[out_idx[j]];
 }
 
+// Draws of the count-aware head: row r of out takes query r / per_query's
+// distributions and receives, per species, the class drawn from the logits
+// -- the count itself -- or for the tail class floor(exp(z + base)), at
+// least kNC - 1, z drawn from the tail mixture.  The two species are drawn
+// independently.
+__global__ void count_sample_kernel(const float *O, int B, uint64_t seed, float *out, int per_query,
+                                    const float *base) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= B) return;
+    const int q = row / per_query;
+    for (int sp = 0; sp < 2; ++sp) {
+        const float *o = O + (size_t)q * 2 * kHS + sp * kHS;
+        uint64_t h = mix64(seed ^ mix64(((uint64_t)row << 1 | (uint64_t)sp) + 0x9E3779B97F4A7C15ull));
+        const float u0 = (float)(h >> 40) * 0x1p-24f;
+        h = mix64(h);
+        const float u1 = (float)(h >> 40) * 0x1p-24f, u2 = ((float)((h >> 16) & 0xFFFFFF) + 0.5f) * 0x1p-24f;
+        h = mix64(h);
+        const float u3 = (float)(h >> 40) * 0x1p-24f;
+        float lmax = -1e30f;
+        for (int k = 0; k < kNC; ++k) lmax = fmaxf(lmax, o[k]);
+        float zs = 0.0f;
+        for (int k = 0; k < kNC; ++k) zs += __expf(o[k] - lmax);
+        int c = kNC - 1;
+        float acc = 0.0f;
+        for (int k = 0; k < kNC; ++k) {
+            acc += __expf(o[k] - lmax) / zs;
+            if (u0 < acc) {
+                c = k;
+                break;
+            }
+        }
+        if (c < kNC - 1) {
+            out[2 * row + sp] = (float)c;
+            continue;
+        }
+        const float *tw = o + kNC, *tm = tw + kKT, *ts = tm + kKT;
+        float wmax = -1e30f;
+        for (int k = 0; k < kKT; ++k) wmax = fmaxf(wmax, tw[k]);
+        float ws = 0.0f;
+        for (int k = 0; k < kKT; ++k) ws += __expf(tw[k] - wmax);
+        int t = kKT - 1;
+        acc = 0.0f;
+        for (int k = 0; k < kKT; ++k) {
+            acc += __expf(tw[k] - wmax) / ws;
+            if (u1 < acc) {
+                t = k;
+                break;
+            }
+        }
+        const float z = tm[t] + (softplusf_(ts[t]) + 1e-3f) * sqrtf(-2.0f * logf(u2)) * cosf(6.2831853f * u3);
+        out[2 * row + sp] = fmaxf(floorf(expf(z + base[2 * q + sp])), (float)(kNC - 1));
+    }
+}
+
 }  // namespace
 
 }  // namespace rbg
 
 extern "C" {
+
+// Count-aware head: loss and gradient, and draws (see count_loss_kernel,
+// count_sample_kernel); device pointers.
+int rbg_mdn_count_loss(const float *O, const float *Y, int B, float *loss, float *G, void *stream) {
+    rbg::count_loss_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, Y, B, loss, G);
+    return (int)cudaGetLastError();
+}
+
+int rbg_mdn_count_sample(const float *O, int B, uint64_t seed, float *out, int per_query, const float *base,
+                         void *stream) {
+    if (per_query < 1 || !base) return (int)cudaErrorInvalidValue;
+    rbg::count_sample_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, B, seed, out,
+                                                                                            per_query, base);
+    return (int)cudaGetLastError();
+}
 
 // Rate-equation solution at each query (see rre_kernel); device pointers.
 int rbg_mdn_rre(const float *rates, const float *tq, int Q, int S, int R, const int *E, const float *N,

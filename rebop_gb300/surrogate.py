@@ -3,15 +3,20 @@
 in [0, 1]).
 
 A query (u, t) -- the log10 factors u of the five rate constants and the time
--- gets a count distribution of (protein, dimer).  Its deterministic part
-comes from the network's reaction rate equations (the SSA's mean-field
+-- gets the count distributions of protein and dimer.  Their deterministic
+part comes from the network's reaction rate equations (the SSA's mean-field
 limit), integrated per query on the GPU (rbg_mdn_rre): b = log(x_RRE + 1).  A
-multilayer perceptron (8 inputs: u, t, b -> 4 x 256 SiLU -> 40) maps the query
-to an 8-component diagonal Gaussian mixture over the residual
-log(n + v) - b of the counts n, v ~ U[0, 1) (dequantised integers); a draw z
-becomes the count floor(exp(z + b)).  So the network learns only the
-stochastic correction around the rate equations, a small and smooth function
-that BF16 resolves finely.  Weights are BF16 with FP32 master copies; every
+multilayer perceptron (8 inputs: u, t, b -> 4 x 256 SiLU -> 88) maps the query
+to a count-aware head per species: a categorical over the counts 0 .. 30 and a
+tail class, and for the tail a 4-component Gaussian mixture over the residual
+log(n + v) - b (v ~ U[0, 1) dequantises the integer n); a tail draw z becomes
+the count floor(exp(z + b)).  Small counts are thus exact classes -- early in a
+trajectory the dimer count is 0, 1 or 2 -- and for large ones the network
+learns only the stochastic correction around the rate equations, a small and
+smooth function that BF16 resolves finely.  The two species' draws are
+independent: the head models each marginal distribution, not their
+correlation.  (head="mixture" selects an 8-component diagonal Gaussian
+mixture over both residuals jointly instead.)  Weights are BF16 with FP32 master copies; every
 forward and backward GEMM runs on the 5th-generation tensor cores (tcgen05.mma
 into tensor memory, FP32 accumulation), and the rate-equation solver, the
 loss, its gradient, the optimiser and the sampler are the engine's own kernels
@@ -31,7 +36,10 @@ X0 = (1, 0, 0, 0)
 EXPS = ([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 2, 0], [0, 1, 0, 0], [0, 0, 1, 0])
 DIFFS = ([0, 1, 0, 0], [0, 0, 1, 0], [0, 0, -2, 1], [0, -1, 0, 0], [0, 0, -1, 0])
 N_QUERY, N_IN, HIDDEN, LAYERS, K = 6, 8, 256, 4, 8
-N_OUT = 5 * K
+NC, KT = 32, 4                # count classes (0 .. 30 and the tail), tail components
+N_OUT_COUNT = 2 * (NC + 3 * KT)
+N_OUT_MIX = 5 * K
+N_OUT = N_OUT_COUNT
 RRE_STEPS = 128
 
 
@@ -78,7 +86,8 @@ def generate(n_traj: int, seed: int, nb_steps: int = 100, net=None, per_traj: in
     from the grid t = i / nb_steps per tuple; each tuple gets `draws`
     trajectories (1: every tuple an independent draw of its distribution) and
     each trajectory `per_traj` sample times.  Returns queries [n][6] (u, t),
-    targets [n][2] (the residuals log(n + v) - b, v ~ U[0, 1)) and b [n][2]."""
+    targets [n][4] (the counts n of protein and dimer, then the residuals
+    log(n + v) - b, v ~ U[0, 1)) and b [n][2]."""
     import torch
 
     rng = np.random.default_rng(seed)
@@ -97,23 +106,28 @@ def generate(n_traj: int, seed: int, nb_steps: int = 100, net=None, per_traj: in
         t = ti.reshape(-1)
         xs.append(np.concatenate([u[j], (t / nb_steps)[:, None]], axis=1))
         cnt = np.stack([c[t, 0, j], c[t, 1, j]], axis=1).astype(np.float64)
-        ys.append(np.log(cnt + rng.uniform(0.0, 1.0, size=cnt.shape)))
+        ys.append((cnt, np.log(cnt + rng.uniform(0.0, 1.0, size=cnt.shape))))
     x = np.concatenate(xs).astype(np.float32)
     b = rre_log_means(torch.from_numpy(x)).cpu().numpy().astype(np.float64)
-    y = (np.concatenate(ys) - b).astype(np.float32)
+    cnt = np.concatenate([a for a, _ in ys])
+    y = np.concatenate([cnt, np.concatenate([r for _, r in ys]) - b], axis=1).astype(np.float32)
     return x, y, b.astype(np.float32)
 
 
 class MDN:
     """The surrogate network; see the module docstring."""
 
-    def __init__(self, seed: int = 0, device: str = "cuda"):
+    def __init__(self, seed: int = 0, device: str = "cuda", head: str = "count"):
         import torch
 
+        if head not in ("count", "mixture"):
+            raise ValueError("head must be 'count' or 'mixture'")
         self.torch = torch
         self.dev = device
+        self.head = head
+        self.n_out = N_OUT_COUNT if head == "count" else N_OUT_MIX
         g = torch.Generator().manual_seed(seed)
-        dims = [N_IN] + [HIDDEN] * LAYERS + [N_OUT]
+        dims = [N_IN] + [HIDDEN] * LAYERS + [self.n_out]
         self.W, self.b = [], []
         for i in range(len(dims) - 1):
             fan_in, fan_out = dims[i], dims[i + 1]
@@ -154,7 +168,7 @@ class MDN:
             raise RuntimeError("tcgen05 GEMM: a completion wait ran out")
 
     def forward(self, x):
-        """x [B][8] float features (unnormalised u, t, b) -> head outputs [B][40];
+        """x [B][8] float features (unnormalised u, t, b) -> head outputs [B][n_out];
         keeps the activations for backward."""
         torch = self.torch
         B = x.shape[0]
@@ -181,14 +195,19 @@ class MDN:
         o = self.forward(x)
         loss = torch.empty(B, dtype=torch.float32, device=self.dev)
         G = torch.empty_like(o)
-        check(lib.rbg_mdn_loss(o.data_ptr(), y.data_ptr(), B, K, loss.data_ptr(), G.data_ptr(), self._s()))
+        if self.head == "count":
+            check(lib.rbg_mdn_count_loss(o.data_ptr(), y.data_ptr(), B, loss.data_ptr(), G.data_ptr(), self._s()))
+        else:
+            yr = y[:, 2:].contiguous()
+            check(lib.rbg_mdn_loss(o.data_ptr(), yr.data_ptr(), B, K, loss.data_ptr(), G.data_ptr(), self._s()))
         dW = [None] * len(self.W)
         db = [None] * len(self.W)
         n = len(self.W)
         # head: bias gradient and a BF16 copy of dO
-        d = torch.empty(B, N_OUT, dtype=torch.bfloat16, device=self.dev)
-        db[n - 1] = torch.empty(N_OUT, dtype=torch.float32, device=self.dev)
-        check(lib.rbg_mdn_head_backward(G.data_ptr(), d.data_ptr(), db[n - 1].data_ptr(), B, N_OUT, self._s()))
+        d = torch.empty(B, self.n_out, dtype=torch.bfloat16, device=self.dev)
+        db[n - 1] = torch.empty(self.n_out, dtype=torch.float32, device=self.dev)
+        check(lib.rbg_mdn_head_backward(G.data_ptr(), d.data_ptr(), db[n - 1].data_ptr(), B, self.n_out,
+                                        self._s()))
         for i in range(n - 1, -1, -1):
             out, inp = self.W[i].shape
             h = self._H[i]
@@ -220,7 +239,7 @@ class MDN:
         return loss
 
     def fit(self, x, y, epochs: int = 20, batch: int = 4096, lr: float = 2e-3, seed: int = 0, log=None):
-        """Train on host arrays x [N][6] (queries u, t), y [N][2] (residuals)."""
+        """Train on host arrays x [N][6] (queries u, t), y [N][4] (counts, residuals)."""
         torch = self.torch
         X = features(torch.from_numpy(np.ascontiguousarray(x)))
         Y = torch.from_numpy(np.ascontiguousarray(y)).to(self.dev)
@@ -247,18 +266,22 @@ class MDN:
     def sample_counts(self, x, n_draws: int, seed: int = 1):
         """n_draws samples of (protein, dimer) counts at each query row of x [Q][6]:
         the rate equations and one forward pass per query, then n_draws draws
-        from its mixture, each turned into a count by the sampler kernel."""
+        from its head, each turned into a count by the sampler kernel."""
         F = features(self._queries(x))
         torch = self.torch
         o = self.forward(F)
         base = F[:, N_QUERY:].contiguous()
         c = torch.empty(F.shape[0] * n_draws, 2, dtype=torch.float32, device=self.dev)
-        check(lib.rbg_mdn_sample(o.data_ptr(), c.shape[0], K, int(seed), c.data_ptr(), int(n_draws),
-                                 base.data_ptr(), self._s()))
+        if self.head == "count":
+            check(lib.rbg_mdn_count_sample(o.data_ptr(), c.shape[0], int(seed), c.data_ptr(), int(n_draws),
+                                           base.data_ptr(), self._s()))
+        else:
+            check(lib.rbg_mdn_sample(o.data_ptr(), c.shape[0], K, int(seed), c.data_ptr(), int(n_draws),
+                                     base.data_ptr(), self._s()))
         return c.view(F.shape[0], n_draws, 2)
 
     def predict_params(self, x):
-        """Mixture parameters (over the residuals) at each query row: [Q][40]."""
+        """Head outputs at each query row (one forward pass): [Q][n_out]."""
         return self.forward(features(self._queries(x)))
 
     def _queries(self, x):

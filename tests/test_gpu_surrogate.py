@@ -32,24 +32,28 @@ def test_gemm_bf16_all_transposes(torch):
                 assert err < 1e-5, (M, N, K, ta, tb, err)
 
 
-def test_mdn_gradients_match_oracle(torch):
+@pytest.mark.parametrize("head", ["count", "mixture"])
+def test_mdn_gradients_match_oracle(torch, head):
     from oracle import mdn_oracle
     from rebop_gb300 import surrogate as sg
 
     rng = np.random.default_rng(1)
-    model = sg.MDN(seed=3)
+    model = sg.MDN(seed=3, head=head)
     # network inputs: u (5), t, and the rate-equation log means (2)
     x = rng.uniform(-1, 1, size=(512, sg.N_IN)).astype(np.float32)
     x[:, 5] = rng.uniform(0, 1, 512)
     x[:, 6:] = rng.uniform(0, 8, (512, 2))
-    y = rng.normal(0.0, 0.3, size=(512, 2)).astype(np.float32)
+    # targets: counts (small ones and tail ones) and residuals
+    n = np.where(rng.random((512, 2)) < 0.5, rng.integers(0, 31, (512, 2)), rng.integers(31, 5000, (512, 2)))
+    y = np.concatenate([n, rng.normal(0.0, 0.3, size=(512, 2))], axis=1).astype(np.float32)
     model.x_mean = torch.tensor(x.mean(0)).cuda()
     model.x_std = torch.tensor(x.std(0) + 1e-6).cuda()
     loss, dW, db = model.loss_and_grad(torch.tensor(x).cuda(), torch.tensor(y).cuda())
     W = [w.double().cpu().numpy() for w in model.Wb]
     b = [v.double().cpu().numpy() for v in model.b]
-    rl, rW, rb = mdn_oracle.forward_backward(W, b, x.astype(np.float64), y.astype(np.float64),
-                                             model.x_mean.double().cpu().numpy(), model.x_std.double().cpu().numpy())
+    yo = y.astype(np.float64) if head == "count" else y[:, 2:].astype(np.float64)
+    rl, rW, rb = mdn_oracle.forward_backward(W, b, x.astype(np.float64), yo, model.x_mean.double().cpu().numpy(),
+                                             model.x_std.double().cpu().numpy(), head=head)
     assert abs(float(loss) - rl) <= 1e-3 * abs(rl) + 1e-4
     for i in range(len(W)):
         g, r = dW[i].double().cpu().numpy(), rW[i]
