@@ -27,6 +27,15 @@ namespace {
 
 size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
+// Float pair (hi truncated toward zero, lo rounded) of a rate, as the
+// device's df_from_double makes it; 0 for a rate the float pairs do not cover.
+void float_pair(double v, float *out) {
+    float hi = (float)v;
+    if ((double)hi > v && v > 0) hi = std::nextafter(hi, 0.0f);
+    out[0] = std::isfinite(v) ? hi : 0.0f;
+    out[1] = std::isfinite(v) ? (float)(v - (double)hi) : 0.0f;
+}
+
 // Structure of a network: everything but the rate constants.
 std::string structure_key(const Packed &p) {
     std::string k;
@@ -275,6 +284,7 @@ bool Batch::build(cudaStream_t st) {
         it.o_times = take(8 * (size_t)(it.in.nb_steps + 1));
         it.o_save = take(4 * (size_t)std::max<size_t>(it.save.size(), 1));
         it.o_rates = take(8 * (size_t)(it.in.rates && it.in.rates_per_traj ? it.in.n_traj : 1) * std::max(p.R, 1));
+        it.o_rdf = take(8 * (size_t)(it.in.rates && it.in.rates_per_traj ? it.in.n_traj : 1) * std::max(p.R, 1));
         it.o_fpk = take(4 * (size_t)std::max(p.R * p.P, 1));
         it.o_jsp = take(4 * (size_t)std::max(p.R * p.Q, 1));
         it.o_jd = take(8 * (size_t)std::max(p.R * p.Q, 1));
@@ -429,6 +439,13 @@ bool Batch::build(cudaStream_t st) {
             x.out = reinterpret_cast<int64_t *>(d + it.o_out);
             x.events = reinterpret_cast<uint64_t *>(d + it.o_events);
             x.zig = ctx->zig;
+            x.lm_rdf = reinterpret_cast<const float2 *>(d + it.o_rdf);
+            x.budget_ns = kernel_budget_ns();
+            for (int32_t r = 0; r < p.R; r++) {
+                int m = 0;
+                for (int32_t f = 0; f < p.P; f++) m += p.fac_ord[(size_t)r * p.P + f];
+                x.max_mults = std::max(x.max_mults, m);
+            }
         }
         unit[thread_items.size()] = units;
         warp_traj = acc;
@@ -571,12 +588,7 @@ void Batch::stage_inputs() {
         float *rdf = reinterpret_cast<float *>(h + it.o_rdf);
         for (int q = 0; q < RP; q++) {
             const int r = (q & 31) * C + (q >> 5);
-            const double v = r < p.R ? rt[r] : 0.0;
-            // float pair (hi truncated, lo rounded) of the rate, as the device makes it
-            float hi = (float)v;
-            if ((double)hi > v && v > 0) hi = std::nextafter(hi, 0.0f);
-            rdf[2 * q] = std::isfinite(v) ? hi : 0.0f;
-            rdf[2 * q + 1] = std::isfinite(v) ? (float)(v - (double)hi) : 0.0f;
+            float_pair(r < p.R ? rt[r] : 0.0, rdf + 2 * q);
         }
     }
     for (int i : thread_items) {
@@ -586,10 +598,11 @@ void Batch::stage_inputs() {
         if (n == 0) continue;
         std::memcpy(h + it.o_x0, it.in.x0, 8 * (size_t)(it.in.x0_per_traj ? n : 1) * p.S);
         std::memcpy(h + it.o_seeds, it.in.seeds, 8 * (size_t)n);
-        if (it.in.rates)
-            std::memcpy(h + it.o_rates, it.in.rates, 8 * (size_t)(it.in.rates_per_traj ? n : 1) * p.R);
-        else
-            std::memcpy(h + it.o_rates, p.rate.data(), 8 * (size_t)p.R);
+        const size_t nr = (size_t)(it.in.rates && it.in.rates_per_traj ? n : 1) * p.R;
+        const double *rt = it.in.rates ? it.in.rates : p.rate.data();
+        std::memcpy(h + it.o_rates, rt, 8 * nr);
+        float *rdf = reinterpret_cast<float *>(h + it.o_rdf);
+        for (size_t q = 0; q < nr; q++) float_pair(rt[q], rdf + 2 * q);
     }
 }
 

@@ -462,6 +462,10 @@ bool launch_sampled(const Network &net, DeviceNet &dn, const RunDev &r, cudaStre
                         dn.jit_k = jk;
                         dn.jit_block = kb;
                         dn.jit_version = dn.version;
+                    } else if (!compile) {
+                        // this run takes the descriptor kernel; the generated
+                        // one compiles meanwhile, for the next run to find
+                        jit_compile_async(p, kb);
                     }
                 }
                 if (!jk && ((jit && std::strcmp(jit, "1") == 0) || (want_jit && force))) return false;

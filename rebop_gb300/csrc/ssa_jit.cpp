@@ -25,6 +25,8 @@
 #include <fstream>
 #include <map>
 #include <mutex>
+#include <set>
+#include <thread>
 #include <sstream>
 #include <string>
 #include <sys/stat.h>
@@ -102,9 +104,10 @@ uint64_t fnv1a(const std::string &s, uint64_t h = 0xcbf29ce484222325ull) {
 }
 
 const std::vector<std::string> &compile_options() {
-    static const std::vector<std::string> opts = {"-arch=sm_103a", "-std=c++17", "-fmad=false", "-lineinfo",
-                                                  "-default-device", "-DRBG_JIT=1"};
-    return opts;
+    // never destroyed: a background compile may still read it at exit
+    static const std::vector<std::string> *opts = new std::vector<std::string>{
+        "-arch=sm_103a", "-std=c++17", "-fmad=false", "-lineinfo", "-default-device", "-DRBG_JIT=1"};
+    return *opts;
 }
 
 std::string cache_dir() {
@@ -336,6 +339,30 @@ bool jit_compile(const Packed &p, int block, size_t *image_bytes) {
     if (!compile_image(src, image_key(src, nv), nv, image)) return false;
     if (image_bytes) *image_bytes = image.size();
     return true;
+}
+
+namespace {
+// Background compiles, joined when the library unloads (this object is
+// destroyed before the statics the compiles use, which are defined above).
+struct Background {
+    std::mutex mu;
+    std::set<uint64_t> started;
+    std::vector<std::thread> threads;
+    ~Background() {
+        for (std::thread &t : threads)
+            if (t.joinable()) t.join();
+    }
+} g_background;
+}  // namespace
+
+void jit_compile_async(const Packed &p, int block) {
+    const uint64_t key = fnv1a(jit_net_source(p, block));
+    std::lock_guard<std::mutex> lk(g_background.mu);
+    if (!g_background.started.insert(key).second) return;
+    g_background.threads.emplace_back([p, block]() {
+        size_t n = 0;
+        jit_compile(p, block, &n);  // failures leave the descriptor kernel in use
+    });
 }
 
 const void *jit_kernel(const Packed &p, int block, bool compile) {

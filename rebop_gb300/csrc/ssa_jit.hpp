@@ -24,6 +24,9 @@ bool jit_compile(const Packed &p, int block, size_t *image_bytes);
 // loaded or in the disk cache is returned (null, no error, otherwise).  A
 // kernel built for `block` lanes also runs blocks of fewer lanes.
 const void *jit_kernel(const Packed &p, int block, bool compile = true);
+// Compile the network's kernel into the disk cache on a background thread
+// (once per generated source), so that a later run finds it there.
+void jit_compile_async(const Packed &p, int block);
 int launch_ssa_jit(const void *kern, const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t st);
 // Lanes per block of a generated kernel for a full-size ensemble: 384 (12
 // warps per SM at up to 168 registers a lane; fastest measured on the dimer and

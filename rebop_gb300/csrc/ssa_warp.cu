@@ -73,7 +73,7 @@ __host__ __device__ inline WarpLayout warp_layout(const SsaArgs &a) {
     w += 8 * RP + 8;                                    // propensities (lane-major), alignment
     if (a.rate_stride) w += 8 * RP;                     // per-trajectory float-pair rates
     if (!a.batch) w += 8 * 32 * (size_t)warp_ngroups(warp_chunk(a.R)) + 4 * 32;  // group sums, dirty masks
-    const size_t wt = 8 * 32 * (size_t)a.tbatch_S;          // a thread unit's counts [S][32]
+    const size_t wt = 8 * 32 * (2 * (size_t)a.tbatch_S + 4);  // a thread unit's counts, their copy, generator
     if (a.batch && wt > w) w = wt;
     l.warp_bytes = (w + 15) & ~(size_t)15;
     return l;
@@ -229,49 +229,145 @@ __host__ __device__ inline uint32_t shape_word(const int32_t *fac_sp, const int3
     return sl[0] | of[0] << 15 | sl[1] << 16 | of[1] << 31;
 }
 
-// One thread unit of a persistent batch: lane l runs trajectory
-// first + l of the small-network item `it` (if it has one) from start to end
-// with the exact per-lane step of the thread kernels (ssa_exact.cuh: binary64
-// in exact integer emulation, native binary64 outside its domain), so its
-// counts, events and draws are rebop's.  sp is this warp's [S][32] count
-// block.  Returns the lane's event count; sets `late` if the wall-clock budget
-// ran out (the trajectory is then incomplete).
+// One thread unit of a persistent batch: lane l runs trajectory first + l of
+// the small-network item `it` (if it has one) from start to end with the
+// speculative float-pair step of the thread kernels (ssa_spec_body.cuh):
+// propensities as float pairs summed into a float32 running sum, the clock as
+// a float triple with a rigorous error bound, the choice in float32 with an
+// exact binary64 decision when it is close, and an exact re-run of any sample
+// interval whose clock decision the bound leaves open -- so its counts,
+// events and draws are rebop's.  wreg is this warp's region: counts [S][32],
+// counts at the interval start [S][32] and the generator there [4][32].
+// Returns the lane's event count; sets `late` if the wall-clock budget ran
+// out (the trajectory is then incomplete).
 template <bool MACRO>
-__device__ __noinline__ unsigned long long thread_unit(const SsaArgs &it, const ExactTables &zt, int64_t *sp,
-                                                       long long first, int64_t t_start, int64_t budget_ns,
+__device__ __noinline__ unsigned long long thread_unit(const SsaArgs &it, const ExactTables &zt, const float2 *xdf,
+                                                       unsigned char *wreg, long long first, int64_t t_start,
                                                        bool &late) {
+    using Ops = TableOps<16, MACRO>;
+    constexpr int NS = 32;  // column stride of the per-lane arrays
     const int lane = threadIdx.x & 31;
     const long long traj = first + lane;
-    unsigned long long ev = 0;
     if (traj >= it.n_traj) return 0;
-    const ExactTables m{zt.zxk, zt.zf, zt.zd, it.fac_packed, it.jmp_sp, it.jmp_d};
-    int64_t *c = sp + lane;  // column of this lane: c[s * 32]
-    for (int s = 0; s < it.S; ++s) c[s * 32] = it.x0[traj * it.x0_stride + s];
+    const int S = it.S, R = it.R;
+    int64_t *sp = reinterpret_cast<int64_t *>(wreg) + lane;
+    int64_t *sps = sp + NS * S;
+    uint64_t *gsv = reinterpret_cast<uint64_t *>(sps + NS * S);
+    const ExactTables ex{zt.zxk, zt.zf, zt.zd, it.fac_packed, it.jmp_sp, it.jmp_d};
+    for (int s = 0; s < S; ++s) sp[s * NS] = it.x0[traj * it.x0_stride + s];
     Xoshiro g;
     xo_seed(g, it.seeds[traj]);
     const uint64_t *rl = reinterpret_cast<const uint64_t *>(it.rate + traj * it.rate_stride);
-    bool nat = false;
-    for (int r = 0; r < it.R; ++r) nat |= !emul_domain(rl[r]);
-    uint64_t t = 0;
+    const float2 *rf = it.lm_rdf + traj * it.rate_stride;
+    bool nat = false, exact_traj = false;
+    for (int r = 0; r < R; ++r) {
+        nat |= !emul_domain(rl[r]);
+        exact_traj |= !spec_rate_ok(rl[r]);
+    }
+    exact_traj |= nat;
+    // error model of the float-pair step (ssa_spec_body.cuh)
+    const float G = ((float)(it.max_mults + R + 2) + (float)(R * (R + 1) / 2 + R * (it.max_mults + 2)) * 0.0625f) *
+                    kGamma;
+    const float c_q = G + 6.0f * kGamma;
+    const float c_sel = (float)(it.max_mults + R + 6) * 0x1p-24f * 1.001f;
+    typename Ops::Counts c{};
+    unsigned long long ev = 0;
+    uint64_t t0 = 0;  // clock at the interval start (bits)
+    unsigned int tick = 0;
     for (long long i = 0; i < it.n_samples; ++i) {
-        const uint64_t T = (uint64_t)__double_as_longlong(it.sample_t[i]);
-        const bool natT = nat || !emul_domain(T);
-        for (unsigned int n = 1;; ++n) {
-            if ((n & 255u) == 0 && global_ns() - t_start > budget_ns) {
+        const double Td = it.sample_t[i];
+        const uint64_t T = (uint64_t)__double_as_longlong(Td);
+        const TF Tc = tf_from_double(Td);
+        TF tc = tf_from_double(__longlong_as_double((long long)t0));
+        float err_t = 0.0f;
+        for (int s = 0; s < S; ++s) sps[s * NS] = sp[s * NS];
+        gsv[0] = g.s0;
+        gsv[NS] = g.s1;
+        gsv[2 * NS] = g.s2;
+        gsv[3 * NS] = g.s3;
+        const unsigned long long ev0 = ev;
+        bool replay = exact_traj;
+        while (!replay) {
+            if ((++tick & 1023u) == 0 && global_ns() - t_start > it.budget_ns) {
                 late = true;
                 return ev;
             }
-            int ix;
-            uint64_t tx;
-            if (!exact_step<16, MACRO, false>(it, m, c, rl, 1, 32, g, t, T, natT, ix, tx)) break;
-            t = tx;
+            // both draws the step may make, taken ahead (stepped back when fewer
+            // are committed)
+            const uint64_t b1 = xo_next(g);
+            const uint64_t b2 = xo_next(g);
+            const int i1 = (int)(b1 & 0xff);
+            const uint64_t k1 = b1 >> 12;
+            const uint64_t K1 = ex.zxk[i1].y;
+            const float2 X1 = xdf[i1];
+            DF x = df_mul(df_u53(2 * k1 + 1), DF{X1.x, X1.y});
+            float xerr = kGamma * X1.x;
+            float cum[16];
+            DF tot;
+            bool amb = Ops::props(it, ex, c, sp, NS, rf, 1, cum, tot);
+            const bool slow = !(k1 < K1);
+            uint64_t bu = b2;
+            if (!(tot.h > 0.0f)) {
+                xo_prev(g);  // no reaction can fire: no draw is made
+                xo_prev(g);
+                if (amb) replay = true;
+                break;  // the sample records
+            }
+            if (slow) {
+                x = exp1_df_cont(g, b1, b2, x, ex, xdf, xerr);
+                bu = xo_next(g);
+            }
+            amb |= tot.h < 0x1p-90f || tot.h > 0x1p90f;
+            const float rr = rcp_approx(tot.h);
+            const DF q = df_div(x, tot, rr);
+            const TF tn = tf_add(tc, q);
+            float err_tn = __fadd_ru(err_t, __fmul_ru(c_q, q.h));
+            err_tn = __fadd_ru(err_tn, __fmul_ru(__fmul_ru(xerr, rr), 1.001f));
+            err_tn = __fadd_ru(err_tn, __fmul_ru(0x1p-52f, tn.h));
+            err_tn = __fadd_ru(err_tn, __fmul_ru(0x1p-23f, fabsf(tn.l)));
+            const float d = __fadd_rn(__fsub_rn(Tc.h, tn.h), __fadd_rn(__fsub_rn(Tc.m, tn.m), __fsub_rn(Tc.l, tn.l)));
+            const float mt = __fadd_ru(err_tn, __fmul_ru(0x1p-44f, fmaxf(Tc.h, tn.h)));
+            const float dd = __fmul_rn(d, 1.0f - 0x1p-22f);
+            const bool fire = dd > mt;
+            amb |= !(fire || dd < -mt) || !(err_tn < 1.0e30f) || q.h < 0x1p-100f;
+            if (amb) {
+                replay = true;
+                break;
+            }
+            if (!fire) {
+                xo_prev(g);  // the sample records: the Exp1 draw alone was made
+                break;
+            }
+            const float ch = __fmul_rn(tot.h, f23((uint32_t)(bu >> 41)) * 0x1p-23f);
+            const float msel = c_sel * tot.h;
+            bool close = false;
+            int idx = 0;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                if (r < R) {
+                    const float dr = __fsub_rn(cum[r], ch);
+                    idx += dr < 0.0f ? 1 : 0;
+                    close |= fabsf(dr) <= msel;
+                }
+            }
+            if (close) idx = Ops::exact_choice(it, ex, c, sp, NS, rl, 1, bu >> 11);
+            tc = tn;
+            err_t = err_tn;
             ++ev;
-            if (ix < it.R)
-                for (int k = 0; k < it.Q; ++k) c[it.jmp_sp[ix * it.Q + k] * 32] += it.jmp_d[ix * it.Q + k];
+            Ops::jump(c, it, ex, sp, NS, idx);
         }
-        t = T;  // the sample records at T (gillespie.rs:328-330)
+        if (replay) {
+            // the interval again, exactly, from its saved start
+            ev = replay_interval<16, MACRO>(it, ex, sp, sps, gsv, rl, 1, NS, t0, T, nat, ev0, t_start);
+            if (ev == ~0ull) {
+                late = true;
+                return ev0;
+            }
+            g = Xoshiro{gsv[0], gsv[NS], gsv[2 * NS], gsv[3 * NS]};
+        }
         int64_t *o = it.out + (size_t)i * it.n_save * it.n_traj + traj;
-        for (int k = 0; k < it.n_save; ++k) o[(size_t)k * it.n_traj] = c[it.save_idx[k] * 32];
+        for (int k = 0; k < it.n_save; ++k) o[(size_t)k * it.n_traj] = sp[it.save_idx[k] * NS];
+        t0 = T;  // the sample records at T (gillespie.rs:328-330)
     }
     if (it.events) it.events[traj] = ev;
     return ev;
@@ -366,8 +462,8 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                 else hi = mid - 1;
             }
             bool late = false;
-            unsigned long long ev = thread_unit<MACRO>(a.tbatch[lo], ex, reinterpret_cast<int64_t *>(wbase),
-                                                       (u - a.tbatch_unit[lo]) * 32, t_start, a.budget_ns, late);
+            unsigned long long ev =
+                thread_unit<MACRO>(a.tbatch[lo], ex, xdf, wbase, (u - a.tbatch_unit[lo]) * 32, t_start, late);
             for (int off = 16; off > 0; off >>= 1) ev += __shfl_xor_sync(0xffffffffu, ev, off);
             warp_events += ev;
             if (__any_sync(0xffffffffu, late)) {

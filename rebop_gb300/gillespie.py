@@ -114,6 +114,13 @@ class Gillespie:
                 if v not in self._species:
                     raise ValueError(f"Unknown species {v!r} in var_names")
         save = [self._species[v] for v in names]
+        # Species and reactions are only ever appended, so their counts and
+        # the parameters identify the lowered network: repeated runs reuse it
+        # (and from the second run on get the kernel compiled for it).
+        key = (S, len(self._reactions), tuple(sorted((str(k), float(v)) for k, v in params.items())))
+        cached = getattr(self, "_net_cache", None)
+        if cached is not None and cached[0] == key:
+            return cached[1], x0, names, save
         net = Network(S)
         for prate, reactants, products, _ in self._reactions:
             exps = [0] * S
@@ -129,6 +136,7 @@ class Gillespie:
             else:
                 # Rate::Expr: the expression alone is the propensity (gillespie.rs:88)
                 net.add_reaction(Rate.expression(prate.to_expr(self._species, params)), diff)
+        self._net_cache = (key, net)
         return net, x0, names, save
 
     # -- runs
