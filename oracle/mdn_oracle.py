@@ -28,7 +28,7 @@ def _sigmoid(x):
     return 1.0 / (1.0 + np.exp(-x))
 
 
-def count_head(o, y, NC=32, KT=4):
+def count_head(o, y, NC=32, KT=8):
     """Loss rows and gradient (before the 1/B of the mean) of the count-aware
     head: per species a block of NC class logits, then KT tail weight logits,
     means and raw scales; y rows (n_protein, n_dimer, residual_protein,
@@ -68,7 +68,7 @@ def count_head(o, y, NC=32, KT=4):
     return loss, G
 
 
-def forward_backward(W, b, x, y, x_mean, x_std, K=8, head="mixture"):
+def forward_backward(W, b, x, y, x_mean, x_std, K=8, head="mixture", tail=8):
     """W[i] [out][in], b[i] [out] (float64 copies of the BF16 / FP32 parameters),
     x [B][n_in], y [B][2] (mixture head: residuals) or [B][4] (count head:
     counts, residuals).  Returns (mean loss, dW list, db list)."""
@@ -83,7 +83,7 @@ def forward_backward(W, b, x, y, x_mean, x_std, K=8, head="mixture"):
             H.append(h)
     o = Z[-1]
     if head == "count":
-        rows, G = count_head(o, y)
+        rows, G = count_head(o, y, KT=tail)
         return _backward(W, H, Z, G / B, float(rows.mean()))
     logits, mu1, mu2 = o[:, :K], o[:, K:2 * K], o[:, 2 * K:3 * K]
     s1 = _softplus(o[:, 3 * K:4 * K]) + 1e-3

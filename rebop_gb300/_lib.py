@@ -150,8 +150,8 @@ for _name, _args in {
     "rbg_mdn_adam": [_vp, _vp, _vp, _vp, _vp, C.c_int, _f32, _f32, _f32, _f32, C.c_int, _vp],
     "rbg_mdn_sample": [_vp, C.c_int, C.c_int, _u64, _vp, C.c_int, _vp, _vp],
     "rbg_mdn_rre": [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp, _vp],
-    "rbg_mdn_count_loss": [_vp, _vp, C.c_int, _vp, _vp, _vp],
-    "rbg_mdn_count_sample": [_vp, C.c_int, _u64, _vp, C.c_int, _vp, _vp],
+    "rbg_mdn_count_loss": [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp],
+    "rbg_mdn_count_sample": [_vp, C.c_int, C.c_int, _u64, _vp, C.c_int, _vp, _vp],
 }.items():
     getattr(lib, _name).argtypes = _args
     getattr(lib, _name).restype = C.c_int

@@ -357,17 +357,18 @@ __global__ void mdn_loss_kernel(const float *O, const float *Y, int B, int K, fl
     }
 }
 
-// Count-aware head, per species s a block of kHS outputs at s * kHS:
+// Count-aware head, per species s a block of HS = kNC + 3 KT outputs at s * HS:
 // logits[kNC] (class c < kNC - 1: the count c; class kNC - 1: a count of at
-// least kNC - 1), then the tail's kKT weight logits, means and raw scales
+// least kNC - 1), then the tail's KT (at most kKTMax) weight logits, means and raw scales
 // (sigma = softplus(raw) + 1e-3) over the residual y = log(n + v) - b_s of a
 // tail count n (v ~ U[0, 1), b_s the rate-equation log mean).  Y rows are
 // (n_protein, n_dimer, y_protein, y_dimer).  loss[row] = sum_s -log P_s with
 // P_s = pi_c for a small count c, pi_tail * sum_k w_k N(y; mu_k, sigma_k) for
 // a tail count; G = d(mean loss)/d(raw head outputs).
-constexpr int kNC = 32, kKT = 4, kHS = kNC + 3 * kKT;
+constexpr int kNC = 32, kKTMax = 16;
 
-__global__ void count_loss_kernel(const float *O, const float *Y, int B, float *loss, float *G) {
+__global__ void count_loss_kernel(const float *O, const float *Y, int B, int kKT, float *loss, float *G) {
+    const int kHS = kNC + 3 * kKT;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= B) return;
     const float inv_b = 1.0f / (float)B;
@@ -395,7 +396,7 @@ __global__ void count_loss_kernel(const float *O, const float *Y, int B, float *
         float ws = 0.0f;
         for (int k = 0; k < kKT; ++k) ws += __expf(tw[k] - wmax);
         const float logw = wmax + logf(ws);
-        float lp[kKT], mx = -1e30f;
+        float lp[kKTMax], mx = -1e30f;
         for (int k = 0; k < kKT; ++k) {
             const float sg = softplusf_(ts[k]) + 1e-3f, e = (y - tm[k]) / sg;
             lp[k] = (tw[k] - logw) - 0.5f * e * e - logf(sg) - 0.9189385332f;
@@ -523,8 +524,9 @@ __global__ void rre_kernel(const float *rates, const float *tq, int Q, int S, in
 // -- the count itself -- or for the tail class floor(exp(z + base)), at
 // least kNC - 1, z drawn from the tail mixture.  The two species are drawn
 // independently.
-__global__ void count_sample_kernel(const float *O, int B, uint64_t seed, float *out, int per_query,
+__global__ void count_sample_kernel(const float *O, int B, int kKT, uint64_t seed, float *out, int per_query,
                                     const float *base) {
+    const int kHS = kNC + 3 * kKT;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= B) return;
     const int q = row / per_query;
@@ -580,15 +582,16 @@ extern "C" {
 
 // Count-aware head: loss and gradient, and draws (see count_loss_kernel,
 // count_sample_kernel); device pointers.
-int rbg_mdn_count_loss(const float *O, const float *Y, int B, float *loss, float *G, void *stream) {
-    rbg::count_loss_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, Y, B, loss, G);
+int rbg_mdn_count_loss(const float *O, const float *Y, int B, int KT, float *loss, float *G, void *stream) {
+    if (KT < 1 || KT > rbg::kKTMax) return (int)cudaErrorInvalidValue;
+    rbg::count_loss_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, Y, B, KT, loss, G);
     return (int)cudaGetLastError();
 }
 
-int rbg_mdn_count_sample(const float *O, int B, uint64_t seed, float *out, int per_query, const float *base,
+int rbg_mdn_count_sample(const float *O, int B, int KT, uint64_t seed, float *out, int per_query, const float *base,
                          void *stream) {
-    if (per_query < 1 || !base) return (int)cudaErrorInvalidValue;
-    rbg::count_sample_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, B, seed, out,
+    if (per_query < 1 || !base || KT < 1 || KT > rbg::kKTMax) return (int)cudaErrorInvalidValue;
+    rbg::count_sample_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, B, KT, seed, out,
                                                                                             per_query, base);
     return (int)cudaGetLastError();
 }

@@ -6,9 +6,9 @@ A query (u, t) -- the log10 factors u of the five rate constants and the time
 -- gets the count distributions of protein and dimer.  Their deterministic
 part comes from the network's reaction rate equations (the SSA's mean-field
 limit), integrated per query on the GPU (rbg_mdn_rre): b = log(x_RRE + 1).  A
-multilayer perceptron (8 inputs: u, t, b -> 4 x 256 SiLU -> 88) maps the query
+multilayer perceptron (8 inputs: u, t, b -> 4 x 256 SiLU -> 112) maps the query
 to a count-aware head per species: a categorical over the counts 0 .. 30 and a
-tail class, and for the tail a 4-component Gaussian mixture over the residual
+tail class, and for the tail an 8-component Gaussian mixture over the residual
 log(n + v) - b (v ~ U[0, 1) dequantises the integer n); a tail draw z becomes
 the count floor(exp(z + b)).  Small counts are thus exact classes -- early in a
 trajectory the dimer count is 0, 1 or 2 -- and for large ones the network
@@ -36,10 +36,8 @@ X0 = (1, 0, 0, 0)
 EXPS = ([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 2, 0], [0, 1, 0, 0], [0, 0, 1, 0])
 DIFFS = ([0, 1, 0, 0], [0, 0, 1, 0], [0, 0, -2, 1], [0, -1, 0, 0], [0, 0, -1, 0])
 N_QUERY, N_IN, HIDDEN, LAYERS, K = 6, 8, 256, 4, 8
-NC, KT = 32, 4                # count classes (0 .. 30 and the tail), tail components
-N_OUT_COUNT = 2 * (NC + 3 * KT)
+NC, KT = 32, 8                # count classes (0 .. 30 and the tail), tail components
 N_OUT_MIX = 5 * K
-N_OUT = N_OUT_COUNT
 RRE_STEPS = 128
 
 
@@ -117,7 +115,7 @@ def generate(n_traj: int, seed: int, nb_steps: int = 100, net=None, per_traj: in
 class MDN:
     """The surrogate network; see the module docstring."""
 
-    def __init__(self, seed: int = 0, device: str = "cuda", head: str = "count"):
+    def __init__(self, seed: int = 0, device: str = "cuda", head: str = "count", tail: int = KT):
         import torch
 
         if head not in ("count", "mixture"):
@@ -125,7 +123,8 @@ class MDN:
         self.torch = torch
         self.dev = device
         self.head = head
-        self.n_out = N_OUT_COUNT if head == "count" else N_OUT_MIX
+        self.tail = int(tail)
+        self.n_out = 2 * (NC + 3 * self.tail) if head == "count" else N_OUT_MIX
         g = torch.Generator().manual_seed(seed)
         dims = [N_IN] + [HIDDEN] * LAYERS + [self.n_out]
         self.W, self.b = [], []
@@ -196,7 +195,8 @@ class MDN:
         loss = torch.empty(B, dtype=torch.float32, device=self.dev)
         G = torch.empty_like(o)
         if self.head == "count":
-            check(lib.rbg_mdn_count_loss(o.data_ptr(), y.data_ptr(), B, loss.data_ptr(), G.data_ptr(), self._s()))
+            check(lib.rbg_mdn_count_loss(o.data_ptr(), y.data_ptr(), B, self.tail, loss.data_ptr(), G.data_ptr(),
+                                         self._s()))
         else:
             yr = y[:, 2:].contiguous()
             check(lib.rbg_mdn_loss(o.data_ptr(), yr.data_ptr(), B, K, loss.data_ptr(), G.data_ptr(), self._s()))
@@ -273,7 +273,7 @@ class MDN:
         base = F[:, N_QUERY:].contiguous()
         c = torch.empty(F.shape[0] * n_draws, 2, dtype=torch.float32, device=self.dev)
         if self.head == "count":
-            check(lib.rbg_mdn_count_sample(o.data_ptr(), c.shape[0], int(seed), c.data_ptr(), int(n_draws),
+            check(lib.rbg_mdn_count_sample(o.data_ptr(), c.shape[0], self.tail, int(seed), c.data_ptr(), int(n_draws),
                                            base.data_ptr(), self._s()))
         else:
             check(lib.rbg_mdn_sample(o.data_ptr(), c.shape[0], K, int(seed), c.data_ptr(), int(n_draws),
@@ -305,10 +305,12 @@ class Surrogate:
         self.points = None
         self.ok = None
 
-    def validate(self, n_points: int, n_ssa: int, seed: int, net=None):
+    def validate(self, n_points: int, n_ssa: int, seed: int, net=None, model_draws: int | None = None):
         """Per held-out point: relative W1 and KS of the MDN against a fresh SSA
         batch of n_ssa trajectories, and the same for a second independent SSA
-        batch (the sampling-noise floor of the comparison)."""
+        batch (the sampling-noise floor of the comparison).  The MDN's side is
+        `model_draws` draws (default 10 n_ssa: the surrogate draws cheaply, so
+        its own sampling noise stays small next to the SSA batch's)."""
         rng = np.random.default_rng(seed)
         u = rng.uniform(-1, 1, size=(n_points, 5))
         ti = rng.integers(1, 101, size=n_points)
@@ -324,9 +326,11 @@ class Surrogate:
             res = net.run_ensemble(list(X0), seeds, 1.0, 100, save=[2, 3], rates=rates, want_events=False)
             runs.append((res.counts, time.perf_counter() - t0, res.stats["kernel_ms"]))
         x = np.concatenate([u, t[:, None]], axis=1).astype(np.float32)
-        draws = self.model.sample_counts(x, n_ssa, seed=seed + 1).cpu().numpy()
+        md = model_draws or 10 * n_ssa
+        draws = np.concatenate([self.model.sample_counts(x[k:k + 16], md, seed=seed + 1 + k).cpu().numpy()
+                                for k in range(0, n_points, 16)])
         out = {"w1": np.zeros((n_points, 2)), "ks": np.zeros((n_points, 2)), "w1_floor": np.zeros((n_points, 2)),
-               "mean": np.zeros((n_points, 2)), "t": t}
+               "mean": np.zeros((n_points, 2)), "t": t, "model_draws": md}
         for p in range(n_points):
             sl = slice(p * n_ssa, (p + 1) * n_ssa)
             for s in range(2):
@@ -339,20 +343,42 @@ class Surrogate:
                 out["w1_floor"][p, s] = wasserstein1(b, a) / mean
                 out["ks"][p, s] = ks_distance(m, a)
         self.points = x
+        self.features = features(torch_tensor(x)).cpu().numpy()
         self.ok = (out["w1"] <= self.tol).all(axis=1)
         out["ssa_seconds"] = runs[0][1]
         out["ssa_kernel_ms"] = runs[0][2]
         return out
 
     def answer(self, x):
-        """Which queries of x [Q][6] the MDN answers (True) and which fall back."""
-        d = ((x[:, None, :] - self.points[None, :, :]) ** 2).sum(-1)
-        return self.ok[np.argmin(d, axis=1)]
+        """Which queries of x [Q][6] the MDN answers (True) and which fall back:
+        a query takes the verdict of the nearest validation point in (t, b) --
+        the time and the rate-equation log counts, which set how the count
+        distributions look -- scaled to unit spread."""
+        f = features(torch_tensor(np.asarray(x, dtype=np.float32))).cpu().numpy()[:, N_QUERY - 1:]
+        ref = self.features[:, N_QUERY - 1:]
+        scale = ref.std(0) + 1e-6
+        ok = np.empty(len(f), dtype=bool)
+        for k in range(0, len(f), 4096):
+            d = (((f[k:k + 4096, None, :] - ref[None, :, :]) / scale) ** 2).sum(-1)
+            ok[k:k + 4096] = self.ok[np.argmin(d, axis=1)]
+        return ok
+
+
+def torch_tensor(x):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32))
 
 
 def wasserstein1(a: np.ndarray, b: np.ndarray) -> float:
-    """W1 distance of two equal-size empirical samples (sorted differences)."""
-    return float(np.mean(np.abs(np.sort(a) - np.sort(b))))
+    """W1 distance of two empirical samples: the integral of |F_a - F_b|."""
+    a, b = np.sort(a), np.sort(b)
+    if len(a) == len(b):
+        return float(np.mean(np.abs(a - b)))
+    grid = np.union1d(a, b)
+    fa = np.searchsorted(a, grid[:-1], side="right") / len(a)
+    fb = np.searchsorted(b, grid[:-1], side="right") / len(b)
+    return float(np.sum(np.abs(fa - fb) * np.diff(grid)))
 
 
 def ks_distance(a: np.ndarray, b: np.ndarray) -> float:
