@@ -571,6 +571,8 @@ def run_ours(args, w):
             if name == "batch":
                 subs[name] = measure_batch(args, min(args.steps, 3), min(args.warmup, 2),
                                            cpu=not args.no_cpu_baseline)
+            elif name == "surrogate":
+                subs[name] = measure_surrogate(args)
             else:
                 sw = WORKLOADS[name]
                 st, wu = SUB_STEPS.get(name, (3, 2))
@@ -635,6 +637,7 @@ def measure_batch(args, steps: int, warmup: int, cpu: bool = True) -> dict:
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     dev_ms, wall, events, h2d, d2h, launches = 0.0, 0.0, 0, 0, 0, 0
+    parts = {"in_ms": 0.0, "kernels_ms": 0.0, "out_ms": 0.0}
     for s in range(steps):
         for j in range(len(items)):
             b.seeds(j)[:] = batch_seeds(1 + s, j)
@@ -645,6 +648,8 @@ def measure_batch(args, steps: int, warmup: int, cpu: bool = True) -> dict:
         events += st["events"]
         launches += st["kernel_launches"]
         h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+        for k, v in b.times().items():
+            parts[k] += v / steps
     clk = clocks.stop()
     torch.cuda.synchronize()
     cpu_b = None
@@ -660,6 +665,7 @@ def measure_batch(args, steps: int, warmup: int, cpu: bool = True) -> dict:
                    "events_per_step": events / steps, "own_launches": n_own, "persistent_items": n_persistent,
                    "mode": os.environ.get("RB_BATCH_MODE", "persistent"),
                    "timing": "device time of the replayed graph: input copy, kernels, result copy",
+                   "graph_parts_ms": parts,
                    "l2": "inputs and outputs far above L2 are copied in every step"},
         "e2e": {"value": events / wall, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
@@ -696,21 +702,20 @@ SURROGATE = dict(
     name="surrogate",
     desc=("learned surrogate of the dimer ensemble: 2^20 training tuples generated by the engine, one per "
           "trajectory (5 rate factors 10^U[-1,1] around 25, 1000, 0.001, 0.1, 1; t drawn from the 101-point grid "
-          "of [0, 1]); MLP 6 -> 4 x 256 "
-          "SiLU -> 8-component Gaussian mixture over log1p(protein, dimer), BF16 weights, FP32 accumulation; "
-          "held-out points judged against fresh SSA batches"),
-    n_traj=1 << 20, epochs=30, batch=4096, lr=2e-3, n_points=128, n_ssa=1000, n_points_big=32, n_ssa_big=10000,
+          "of [0, 1]); rate-equation baseline per query; MLP 8 -> 4 x 256 SiLU -> count-aware head per species "
+          "(classes for counts 0..30, an 8-component Gaussian mixture over the log-count residual above), BF16 "
+          "weights, FP32 accumulation; held-out points judged against fresh SSA batches"),
+    n_traj=1 << 20, epochs=15, batch=4096, lr=2e-3, n_points=128, n_ssa=1000, n_points_big=64, n_ssa_big=10000,
     n_queries=1_000_000, draws=1000,
 )
 
 
-def run_surrogate(args):
+def measure_surrogate(args) -> dict:
     import torch
 
     from rebop_gb300 import surrogate as sg
 
     w = SURROGATE
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     t0 = time.perf_counter()
     x, y, _ = sg.generate(w["n_traj"], seed=20260106)
     t_gen = time.perf_counter() - t0
@@ -719,11 +724,12 @@ def run_surrogate(args):
     model.fit(x, y, epochs=w["epochs"], batch=w["batch"], lr=w["lr"])
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
+    val = sg.Surrogate(model, tol=0.01).validate(w["n_points"], w["n_ssa"], seed=7)
     sur = sg.Surrogate(model, tol=0.01)
-    val = sur.validate(w["n_points"], w["n_ssa"], seed=7)
-    big = sg.Surrogate(model, tol=0.01).validate(w["n_points_big"], w["n_ssa_big"], seed=8)
-    # throughput: queries answered by the surrogate (one forward pass and `draws`
-    # samples each) against queries answered by the SSA engine (`draws` trajectories)
+    big = sur.validate(w["n_points_big"], w["n_ssa_big"], seed=8)
+    # throughput: queries answered by the surrogate (rate equations, one forward
+    # pass and `draws` samples each) against queries answered by the SSA engine
+    # (`draws` trajectories each)
     rng = np.random.default_rng(9)
     q = np.concatenate([rng.uniform(-1, 1, (w["n_queries"], 5)), rng.integers(1, 101, (w["n_queries"], 1)) / 100],
                        axis=1).astype(np.float32)
@@ -770,29 +776,42 @@ def run_surrogate(args):
         gemm_tflops[name] = 50 * 2 * 4096 * 256 * 256 / (e0.elapsed_time(e1) / 1e3) / 1e12
     answered = sur.answer(q[:100000]).mean()
     med = lambda a: float(np.median(a))  # noqa: E731
-    line = {
+    ok = (big["w1"] <= 0.01).all(axis=1)
+    return {
         "metric": "surrogate queries/s (1000 draws each) vs plain GPU SSA queries/s (1000 trajectories each)",
-        "value": sur_qps, "unit": "queries/s", "n_gpus": 1, "steps": 1, "warmup": 1,
-        "ms_per_step": 1e3 * n_q / sur_qps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "value": sur_qps, "unit": "queries/s", "steps": 1, "warmup": 1, "ms_per_step": 1e3 * n_q / sur_qps,
         "dtype": "bf16 weights, fp32 accumulation", "data": "synthetic (engine-generated)",
         "config": {"workload": w["desc"], "training_tuples": int(x.shape[0]), "epochs": w["epochs"],
                    "generate_s": t_gen, "train_s": t_train},
         "ssa_queries_per_s": ssa_qps, "speedup_vs_ssa": sur_qps / ssa_qps, "params_only_queries_per_s": param_qps,
         "accuracy_1e3": {
-            "points": w["n_points"], "median_w1_rel": [med(val["w1"][:, 0]), med(val["w1"][:, 1])],
+            "points": w["n_points"], "model_draws": val["model_draws"],
+            "median_w1_rel": [med(val["w1"][:, 0]), med(val["w1"][:, 1])],
             "median_w1_rel_ssa_vs_ssa": [med(val["w1_floor"][:, 0]), med(val["w1_floor"][:, 1])],
             "fraction_w1_within_1pct": float(np.mean((val["w1"] <= 0.01).all(axis=1))),
             "fraction_w1_within_1pct_ssa_vs_ssa": float(np.mean((val["w1_floor"] <= 0.01).all(axis=1))),
             "median_ks": [med(val["ks"][:, 0]), med(val["ks"][:, 1])]},
         "accuracy_1e4": {
-            "points": w["n_points_big"], "median_w1_rel": [med(big["w1"][:, 0]), med(big["w1"][:, 1])],
+            "points": w["n_points_big"], "model_draws": big["model_draws"],
+            "median_w1_rel": [med(big["w1"][:, 0]), med(big["w1"][:, 1])],
             "median_w1_rel_ssa_vs_ssa": [med(big["w1_floor"][:, 0]), med(big["w1_floor"][:, 1])],
-            "fraction_w1_within_1pct": float(np.mean((big["w1"] <= 0.01).all(axis=1))),
+            "fraction_w1_within_1pct": float(np.mean(ok)),
+            "fraction_w1_within_1pct_ssa_vs_ssa": float(np.mean((big["w1_floor"] <= 0.01).all(axis=1))),
+            "fraction_w1_within_1pct_per_species": [float(np.mean(big["w1"][:, 0] <= 0.01)),
+                                                     float(np.mean(big["w1"][:, 1] <= 0.01))],
             "median_ks": [med(big["ks"][:, 0]), med(big["ks"][:, 1])]},
         "answered_by_surrogate": float(answered),
         "gemm_4096x256x256_tflops": gemm_tflops,
-        "gpu_launches": None,
     }
+
+
+def run_surrogate(args):
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    m = measure_surrogate(args)
+    line = {"metric": m.pop("metric"), "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "gpu_launches": None, **m}
     print(json.dumps(line), flush=True)
 
 
@@ -807,7 +826,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner's pilot runs")
-    ap.add_argument("--workloads", default="sir,large,batch",
+    ap.add_argument("--workloads", default="sir,large,batch,surrogate",
                     help="configurations measured beside the headline (comma list, or 'none')")
     args = ap.parse_args()
     if args.workload == "batch":

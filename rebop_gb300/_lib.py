@@ -155,6 +155,8 @@ for _name, _args in {
 }.items():
     getattr(lib, _name).argtypes = _args
     getattr(lib, _name).restype = C.c_int
+lib.rbg_internal_batch_times.argtypes = [_vp, P(C.c_float), P(C.c_float), P(C.c_float)]
+lib.rbg_internal_batch_times.restype = C.c_int
 lib.rbg_internal_jit_source.argtypes = [_vp, _cp, _sz]
 lib.rbg_internal_jit_source.restype = C.c_int
 lib.rbg_internal_jit_compile.argtypes = [_vp, P(_u64)]

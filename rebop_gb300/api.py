@@ -476,6 +476,12 @@ class Batch:
         check(lib.rb_batch_plan(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def times(self) -> dict:
+        """Device time of the last run's graph: input copy, kernels, result copy (ms)."""
+        a, b, c = C.c_float(), C.c_float(), C.c_float()
+        check(lib.rbg_internal_batch_times(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"in_ms": a.value, "kernels_ms": b.value, "out_ms": c.value}
+
     def mapping(self, k: int) -> int:
         m = C.c_int32()
         check(lib.rb_batch_item_mapping(self._h, int(k), C.byref(m)))

@@ -489,13 +489,15 @@ bool Batch::build(cudaStream_t st) {
     if (!cuda_ok(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate") ||
         !cuda_ok(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate") ||
-        !cuda_ok(cudaEventCreate(&t0), "cudaEventCreate") || !cuda_ok(cudaEventCreate(&t1), "cudaEventCreate"))
+        !cuda_ok(cudaEventCreate(&t0), "cudaEventCreate") || !cuda_ok(cudaEventCreate(&t1), "cudaEventCreate") ||
+        !cuda_ok(cudaEventCreate(&e_in), "cudaEventCreate") || !cuda_ok(cudaEventCreate(&e_kern), "cudaEventCreate"))
         return false;
 
     // ---------------- capture: inputs in, kernels on two branches, results out
     if (!cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture")) return false;
     bool ok = cuda_ok(cudaMemcpyAsync(dev, host, in_bytes, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(in)");
     ok = ok && cuda_ok(cudaMemsetAsync(d + o_work, 0, 32, st), "cudaMemsetAsync");
+    ok = ok && cuda_ok(cudaEventRecord(e_in, st), "cudaEventRecord");
     ok = ok && cuda_ok(cudaEventRecord(fork, st), "cudaEventRecord") &&
          cuda_ok(cudaStreamWaitEvent(side, fork, 0), "cudaStreamWaitEvent");
     if (ok && (!warp_items.empty() || !thread_items.empty())) {
@@ -536,6 +538,7 @@ bool Batch::build(cudaStream_t st) {
     }
     ok = ok && cuda_ok(cudaEventRecord(join, side), "cudaEventRecord") &&
          cuda_ok(cudaStreamWaitEvent(st, join, 0), "cudaStreamWaitEvent");
+    ok = ok && cuda_ok(cudaEventRecord(e_kern, st), "cudaEventRecord");
     ok = ok && cuda_ok(cudaMemcpyAsync(h + in_bytes, d + in_bytes, total_bytes - in_bytes, cudaMemcpyDeviceToHost, st),
                        "cudaMemcpyAsync(out)");
     cudaGraph_t graph = nullptr;
@@ -661,6 +664,12 @@ bool Batch::run(rb_stats_out &st_out) {
         return false;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, t0, t1);
+    if (cudaEventElapsedTime(&last_in_ms, t0, e_in) != cudaSuccess ||
+        cudaEventElapsedTime(&last_kern_ms, e_in, e_kern) != cudaSuccess ||
+        cudaEventElapsedTime(&last_out_ms, e_kern, t1) != cudaSuccess) {
+        cudaGetLastError();
+        last_in_ms = last_kern_ms = last_out_ms = -1.f;
+    }
     // timeout flags of every launch
     unsigned long long flag = 0;
     const unsigned long long *wk =
@@ -696,7 +705,7 @@ void Batch::free_device() {
     host = nullptr;
     if (side) cudaStreamDestroy(side);
     side = nullptr;
-    for (cudaEvent_t *e : {&fork, &join, &t0, &t1})
+    for (cudaEvent_t *e : {&fork, &join, &t0, &t1, &e_in, &e_kern})
         if (*e) {
             cudaEventDestroy(*e);
             *e = nullptr;

@@ -74,6 +74,8 @@ struct Batch {
     int64_t warp_traj = 0;
     cudaStream_t stream = nullptr, side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, t0 = nullptr, t1 = nullptr;
+    cudaEvent_t e_in = nullptr, e_kern = nullptr;  // inside the graph: inputs copied, kernels done
+    float last_in_ms = 0.f, last_kern_ms = 0.f, last_out_ms = 0.f;
     cudaGraphExec_t exec = nullptr;
 
     std::string add(const Network *net, const ItemIn &in);

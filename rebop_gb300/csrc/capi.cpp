@@ -800,6 +800,16 @@ int rb_batch_run(rb_batch *b, rb_run_stats *stats) {
     return st.timeout ? RB_ERR_TIMEOUT : RB_ERR_CUDA;
 }
 
+// Device time of the last run's graph in three parts: the input copy, the
+// kernels, the result copy (ms; -1 if not available).
+int rbg_internal_batch_times(const rb_batch *b, float *in_ms, float *kern_ms, float *out_ms) {
+    if (!b || !in_ms || !kern_ms || !out_ms) return fail(RB_ERR_INVALID, "null argument");
+    *in_ms = b->b.last_in_ms;
+    *kern_ms = b->b.last_kern_ms;
+    *out_ms = b->b.last_out_ms;
+    return RB_OK;
+}
+
 int rb_batch_plan(rb_batch *b, int32_t *n_own_launches, int32_t *n_persistent_items) {
     if (!b) return fail(RB_ERR_INVALID, "null batch");
     if (!b->b.planned) b->b.plan();
