@@ -497,7 +497,8 @@ bool Batch::build(cudaStream_t st) {
     if (!cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture")) return false;
     bool ok = cuda_ok(cudaMemcpyAsync(dev, host, in_bytes, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(in)");
     ok = ok && cuda_ok(cudaMemsetAsync(d + o_work, 0, 32, st), "cudaMemsetAsync");
-    ok = ok && cuda_ok(cudaEventRecord(e_in, st), "cudaEventRecord");
+    // external record nodes: the events record as plain timed events on replay
+    ok = ok && cuda_ok(cudaEventRecordWithFlags(e_in, st, cudaEventRecordExternal), "cudaEventRecordWithFlags");
     ok = ok && cuda_ok(cudaEventRecord(fork, st), "cudaEventRecord") &&
          cuda_ok(cudaStreamWaitEvent(side, fork, 0), "cudaStreamWaitEvent");
     if (ok && (!warp_items.empty() || !thread_items.empty())) {
@@ -538,7 +539,7 @@ bool Batch::build(cudaStream_t st) {
     }
     ok = ok && cuda_ok(cudaEventRecord(join, side), "cudaEventRecord") &&
          cuda_ok(cudaStreamWaitEvent(st, join, 0), "cudaStreamWaitEvent");
-    ok = ok && cuda_ok(cudaEventRecord(e_kern, st), "cudaEventRecord");
+    ok = ok && cuda_ok(cudaEventRecordWithFlags(e_kern, st, cudaEventRecordExternal), "cudaEventRecordWithFlags");
     ok = ok && cuda_ok(cudaMemcpyAsync(h + in_bytes, d + in_bytes, total_bytes - in_bytes, cudaMemcpyDeviceToHost, st),
                        "cudaMemcpyAsync(out)");
     cudaGraph_t graph = nullptr;
