@@ -111,15 +111,20 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
 // ---------------------------------------------------------------- tcgen05
 // The same product on the 5th-generation tensor cores: one CTA of four warps
 // owns a 128 x 32 tile of C in tensor memory (32 columns of 32-bit
-// accumulators); K advances in chunks of 64 staged in shared memory in the
-// canonical K-major layout without swizzle (8 x 16-byte core matrices,
-// adjacent along K at 128 B, along M/N at 1 KiB); one thread issues four
-// tcgen05.mma (K = 16 each) per chunk and commits them to an mbarrier that
-// every thread waits on, with an iteration limit, before the next chunk
-// overwrites the operands.  Each warp then reads its 32 rows from its own
-// tensor-memory lane quadrant.  A wait that runs out sets *err and the tile
-// is left unwritten; tensor memory is always freed.
-constexpr int kTcM = 128, kTcN = 32, kTcK = 64;
+// accumulators).  K advances in rounds of up to kTcSlabs slabs of 64: every
+// slab of a round is staged in shared memory at once (dynamic shared memory,
+// the canonical K-major layout without swizzle: 8 x 16-byte core matrices,
+// adjacent along K at 128 B, along M/N at 1 KiB), the loads of a round issued
+// eight at a time ahead of their stores; one thread then issues four
+// tcgen05.mma (K = 16 each) per slab and commits them to an mbarrier that
+// every thread waits on, with an iteration limit, before the next round
+// overwrites the operands.  For K <= 256 -- every product of the surrogate's
+// forward pass -- that is one round: one latency of loads, 16 MMAs, one wait.
+// Each warp then reads its 32 rows from its own tensor-memory lane quadrant.
+// A wait that runs out sets *err and the tile is left unwritten; tensor
+// memory is always freed.
+constexpr int kTcM = 128, kTcN = 32, kTcK = 64, kTcSlabs = 4;
+constexpr size_t kTcSmem = (size_t)kTcSlabs * (kTcM + kTcN) * kTcK * 2;  // 80 KB
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -145,13 +150,64 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return false;
 }
 
+// Stage rows [r0, r0 + ROWS) x K range [k0, k0 + 64 * slabs) of op(X) into the
+// canonical layout of `dst` ([slab][ROWS * kTcK] elements).  X K-contiguous
+// (VEC): 16-byte loads, eight in flight per thread; otherwise element by
+// element.  Out-of-range elements are zero.
+template <int ROWS, bool T>
+__device__ __forceinline__ void tc_stage(__nv_bfloat16 *dst, const __nv_bfloat16 *__restrict__ X, int ld, int r0,
+                                         int R, int k0, int K, int slabs, bool vec) {
+    const int tid = threadIdx.x;
+    const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+    if (vec) {
+        const int n8 = slabs * (kTcK / 8);  // 16-byte pieces per row
+        const int total = ROWS * n8;
+        for (int e0 = 0; e0 < total; e0 += 128 * 8) {
+            uint4 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int e = e0 + u * 128 + tid;
+                v[u] = make_uint4(0, 0, 0, 0);
+                if (e < total) {
+                    const int r = e / n8, kk = k0 + (e % n8) * 8, m = r0 + r;
+                    if (m < R && kk + 8 <= K) {
+                        v[u] = *reinterpret_cast<const uint4 *>(X + (size_t)m * ld + kk);
+                    } else if (m < R) {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j)
+                            reinterpret_cast<__nv_bfloat16 *>(&v[u])[j] =
+                                kk + j < K ? X[(size_t)m * ld + kk + j] : zero;
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int e = e0 + u * 128 + tid;
+                if (e < total) {
+                    const int r = e / n8, g = e % n8, s = g >> 3, k8 = g & 7;
+                    *reinterpret_cast<uint4 *>(&dst[(size_t)s * ROWS * kTcK + ((r >> 3) * (kTcK / 8) + k8) * 64 +
+                                                    (r & 7) * 8]) = v[u];
+                }
+            }
+        }
+    } else {
+        const int kw = slabs * kTcK;
+        for (int e = tid; e < ROWS * kw; e += 128) {
+            const int r = e / kw, kg = e % kw, s = kg / kTcK, k = kg % kTcK, m = r0 + r, kk = k0 + kg;
+            const __nv_bfloat16 v = (m < R && kk < K) ? (T ? X[(size_t)kk * ld + m] : X[(size_t)m * ld + kk]) : zero;
+            dst[(size_t)s * ROWS * kTcK + ((r >> 3) * (kTcK / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7)] = v;
+        }
+    }
+}
+
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__restrict__ A, int lda,
                                                         const __nv_bfloat16 *__restrict__ B, int ldb,
                                                         float *__restrict__ C, int ldc, int M, int N, int K,
                                                         float beta, int *err) {
-    __shared__ __align__(1024) __nv_bfloat16 As[kTcM * kTcK];
-    __shared__ __align__(1024) __nv_bfloat16 Bs[kTcN * kTcK];
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __nv_bfloat16 *As = reinterpret_cast<__nv_bfloat16 *>(tc_smem);            // [slab][kTcM * kTcK]
+    __nv_bfloat16 *Bs = As + (size_t)kTcSlabs * kTcM * kTcK;                    // [slab][kTcN * kTcK]
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     __shared__ int failed;
@@ -174,64 +230,29 @@ __global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__r
     // idesc: F32 accumulator, BF16 A and B, both K-major, N >> 3, M >> 4
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
                            ((uint32_t)(kTcM >> 4) << 24);
-    const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+    const bool a_vec = !TA && (lda % 8) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+    const bool b_vec = TB && (ldb % 8) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
     uint32_t parity = 0;
-    int chunk = 0;
-    for (int k0 = 0; k0 < K; k0 += kTcK, ++chunk) {
-        // operands -> canonical layout: (r, k) at ((r/8)*(kTcK/8) + k/8)*64 + (r%8)*8 + k%8 elements
-        // K-contiguous rows with 16-byte aligned starts move 8 elements at a
-        // time (one core-matrix row); anything else element by element
-        const bool a_vec = !TA && (lda % 8) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
-        const bool b_vec = TB && (ldb % 8) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
-        if (a_vec) {
-            for (int e = tid; e < kTcM * kTcK / 8; e += 128) {
-                const int r = e / (kTcK / 8), k8 = e % (kTcK / 8), m = m0 + r, kk = k0 + k8 * 8;
-                uint4 v = make_uint4(0, 0, 0, 0);
-                if (m < M && kk + 8 <= K) v = *reinterpret_cast<const uint4 *>(A + (size_t)m * lda + kk);
-                else if (m < M)
-                    for (int j = 0; j < 8; ++j)
-                        reinterpret_cast<__nv_bfloat16 *>(&v)[j] = kk + j < K ? A[(size_t)m * lda + kk + j] : zero;
-                *reinterpret_cast<uint4 *>(&As[((r >> 3) * (kTcK / 8) + k8) * 64 + (r & 7) * 8]) = v;
-            }
-        } else {
-            for (int e = tid; e < kTcM * kTcK; e += 128) {
-                const int r = e / kTcK, k = e % kTcK, m = m0 + r, kk = k0 + k;
-                const __nv_bfloat16 v =
-                    (m < M && kk < K) ? (TA ? A[(size_t)kk * lda + m] : A[(size_t)m * lda + kk]) : zero;
-                As[((r >> 3) * (kTcK / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7)] = v;
-            }
-        }
-        if (b_vec) {
-            for (int e = tid; e < kTcN * kTcK / 8; e += 128) {
-                const int r = e / (kTcK / 8), k8 = e % (kTcK / 8), n = n0 + r, kk = k0 + k8 * 8;
-                uint4 v = make_uint4(0, 0, 0, 0);
-                if (n < N && kk + 8 <= K) v = *reinterpret_cast<const uint4 *>(B + (size_t)n * ldb + kk);
-                else if (n < N)
-                    for (int j = 0; j < 8; ++j)
-                        reinterpret_cast<__nv_bfloat16 *>(&v)[j] = kk + j < K ? B[(size_t)n * ldb + kk + j] : zero;
-                *reinterpret_cast<uint4 *>(&Bs[((r >> 3) * (kTcK / 8) + k8) * 64 + (r & 7) * 8]) = v;
-            }
-        } else {
-            for (int e = tid; e < kTcN * kTcK; e += 128) {
-                const int r = e / kTcK, k = e % kTcK, n = n0 + r, kk = k0 + k;
-                const __nv_bfloat16 v =
-                    (n < N && kk < K) ? (TB ? B[(size_t)n * ldb + kk] : B[(size_t)kk * ldb + n]) : zero;
-                Bs[((r >> 3) * (kTcK / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7)] = v;
-            }
-        }
+    for (int k0 = 0; k0 < K; k0 += kTcSlabs * kTcK) {
+        const int slabs = min(kTcSlabs, (K - k0 + kTcK - 1) / kTcK);
+        tc_stage<kTcM, TA>(As, A, lda, m0, M, k0, K, slabs, a_vec);
+        tc_stage<kTcN, !TB>(Bs, B, ldb, n0, N, k0, K, slabs, b_vec);
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
         if (tid == 0 && !failed) {
             asm volatile("tcgen05.fence::after_thread_sync;\n");
-            for (int s = 0; s < kTcK / 16; ++s) {
-                const uint64_t ad = smem_desc(smem_u32(As) + s * 256, 128, (kTcK / 8) * 128);
-                const uint64_t bd = smem_desc(smem_u32(Bs) + s * 256, 128, (kTcK / 8) * 128);
-                const uint32_t acc = (chunk > 0 || s > 0) ? 1u : 0u;
-                asm volatile(
-                    "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-            }
+            for (int sl = 0; sl < slabs; ++sl)
+                for (int s = 0; s < kTcK / 16; ++s) {
+                    const uint64_t ad =
+                        smem_desc(smem_u32(As + (size_t)sl * kTcM * kTcK) + s * 256, 128, (kTcK / 8) * 128);
+                    const uint64_t bd =
+                        smem_desc(smem_u32(Bs + (size_t)sl * kTcN * kTcK) + s * 256, 128, (kTcK / 8) * 128);
+                    const uint32_t acc = (k0 > 0 || sl > 0 || s > 0) ? 1u : 0u;
+                    asm volatile(
+                        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
                          : "memory");
         }
@@ -631,10 +652,18 @@ int rbg_mdn_gemm_tc05(const void *A, int lda, int ta, const void *B, int ldb, in
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto a = static_cast<const __nv_bfloat16 *>(A);
     auto b = static_cast<const __nv_bfloat16 *>(B);
-    if (ta && tb) gemm_tc05_kernel<true, true><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
-    else if (ta) gemm_tc05_kernel<true, false><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
-    else if (tb) gemm_tc05_kernel<false, true><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
-    else gemm_tc05_kernel<false, false><<<grid, 128, 0, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
+    auto kern = ta && tb ? gemm_tc05_kernel<true, true>
+                : ta     ? gemm_tc05_kernel<true, false>
+                : tb     ? gemm_tc05_kernel<false, true>
+                         : gemm_tc05_kernel<false, false>;
+    static bool opted[4] = {false, false, false, false};  // per variant: dynamic shared memory above 48 KB
+    bool &o = opted[(ta ? 2 : 0) + (tb ? 1 : 0)];
+    if (!o) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+        if (e != cudaSuccess) return (int)e;
+        o = true;
+    }
+    kern<<<grid, 128, kTcSmem, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
     return (int)cudaGetLastError();
 }
 

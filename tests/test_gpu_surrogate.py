@@ -83,7 +83,8 @@ def test_gemm_tcgen05_matches_float64(torch):
 
     rng = np.random.default_rng(2)
     err_flag = torch.zeros(1, dtype=torch.int32, device="cuda")
-    for (M, N, K) in [(128, 64, 64), (200, 100, 80), (4096, 256, 256), (40, 256, 4096), (256, 40, 256)]:
+    for (M, N, K) in [(128, 64, 64), (200, 100, 80), (4096, 256, 256), (40, 256, 4096), (256, 40, 256),
+                      (130, 72, 300), (64, 33, 27), (300, 96, 520)]:
         for ta in (0, 1):
             for tb in (0, 1):
                 a = torch.tensor(rng.standard_normal((K, M) if ta else (M, K)), dtype=torch.bfloat16).cuda()
