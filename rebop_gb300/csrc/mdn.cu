@@ -19,7 +19,9 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 namespace rbg {
 
@@ -114,15 +116,23 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
 // accumulators).  K advances in rounds of up to kTcSlabs slabs of 64: every
 // slab of a round is staged in shared memory at once (dynamic shared memory,
 // the canonical K-major layout without swizzle: 8 x 16-byte core matrices,
-// adjacent along K at 128 B, along M/N at 1 KiB), the loads of a round issued
-// eight at a time ahead of their stores; one thread then issues four
-// tcgen05.mma (K = 16 each) per slab and commits them to an mbarrier that
+// adjacent along K at 128 B, along M/N at 1 KiB).  Both orientations of an
+// operand load 16-byte vectors, eight in flight per thread, coalesced along
+// the dimension that is contiguous in memory; a K-contiguous operand stores
+// each vector as one core-matrix row, an M/N-contiguous one scatters its
+// eight elements over eight rows (lane groups rotate the order so the
+// scattered stores of a warp fall in distinct banks).  One thread then issues
+// four tcgen05.mma (K = 16 each) per slab and commits them to an mbarrier that
 // every thread waits on, with an iteration limit, before the next round
 // overwrites the operands.  For K <= 256 -- every product of the surrogate's
 // forward pass -- that is one round: one latency of loads, 16 MMAs, one wait.
-// Each warp then reads its 32 rows from its own tensor-memory lane quadrant.
-// A wait that runs out sets *err and the tile is left unwritten; tensor
-// memory is always freed.
+// Each warp then reads its 32 rows from its own tensor-memory lane quadrant,
+// transposes them through shared memory and writes C one 128-byte row segment
+// per store.  Products with few tiles and a long K (the weight gradients,
+// K = the batch) split K over gridDim.z; each split writes its partial tile to
+// a workspace and split_reduce_kernel adds the splits in a fixed order, so
+// the result does not depend on scheduling.  A wait that runs out sets *err
+// and the tile is left unwritten; tensor memory is always freed.
 constexpr int kTcM = 128, kTcN = 32, kTcK = 64, kTcSlabs = 4;
 constexpr size_t kTcSmem = (size_t)kTcSlabs * (kTcM + kTcN) * kTcK * 2;  // 80 KB
 
@@ -150,52 +160,91 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return false;
 }
 
+// Element index of (row r, k) of slab s in the canonical layout.
+template <int ROWS>
+__device__ __forceinline__ int tc_index(int s, int r, int k) {
+    return s * ROWS * kTcK + ((r >> 3) * (kTcK / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+}
+
 // Stage rows [r0, r0 + ROWS) x K range [k0, k0 + 64 * slabs) of op(X) into the
-// canonical layout of `dst` ([slab][ROWS * kTcK] elements).  X K-contiguous
-// (VEC): 16-byte loads, eight in flight per thread; otherwise element by
-// element.  Out-of-range elements are zero.
+// canonical layout of `dst` ([slab][ROWS * kTcK] elements).  T = false: X is
+// [rows][K] (K contiguous); T = true: X is [K][rows].  vec: ld a multiple of 8
+// and X 16-byte aligned, so every 16-byte piece is one aligned vector load;
+// pieces that cross the edge of X load element by element.  Out-of-range
+// elements are zero.
 template <int ROWS, bool T>
 __device__ __forceinline__ void tc_stage(__nv_bfloat16 *dst, const __nv_bfloat16 *__restrict__ X, int ld, int r0,
                                          int R, int k0, int K, int slabs, bool vec) {
     const int tid = threadIdx.x;
     const __nv_bfloat16 zero = __float2bfloat16(0.0f);
-    if (vec) {
-        const int n8 = slabs * (kTcK / 8);  // 16-byte pieces per row
-        const int total = ROWS * n8;
-        for (int e0 = 0; e0 < total; e0 += 128 * 8) {
-            uint4 v[8];
+    if (!vec) {
+        const int kw = slabs * kTcK;
+        for (int e = tid; e < ROWS * kw; e += 128) {
+            // T: consecutive threads take consecutive rows (contiguous in X)
+            const int r = T ? e % ROWS : e / kw, kg = T ? e / ROWS : e % kw, m = r0 + r, kk = k0 + kg;
+            const __nv_bfloat16 v = (m < R && kk < K) ? (T ? X[(size_t)kk * ld + m] : X[(size_t)m * ld + kk]) : zero;
+            dst[tc_index<ROWS>(kg / kTcK, r, kg % kTcK)] = v;
+        }
+        return;
+    }
+    const int total = ROWS * slabs * (kTcK / 8);  // 16-byte pieces
+    for (int e0 = 0; e0 < total; e0 += 128 * 8) {
+        uint4 v[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int e = e0 + u * 128 + tid;
-                v[u] = make_uint4(0, 0, 0, 0);
-                if (e < total) {
-                    const int r = e / n8, kk = k0 + (e % n8) * 8, m = r0 + r;
-                    if (m < R && kk + 8 <= K) {
-                        v[u] = *reinterpret_cast<const uint4 *>(X + (size_t)m * ld + kk);
-                    } else if (m < R) {
+        for (int u = 0; u < 8; ++u) {
+            const int e = e0 + u * 128 + tid;
+            v[u] = make_uint4(0, 0, 0, 0);
+            if (e >= total) continue;
+            __nv_bfloat16 *w = reinterpret_cast<__nv_bfloat16 *>(&v[u]);
+            if (!T) {
+                // piece = 8 consecutive k of one row
+                const int n8 = slabs * (kTcK / 8), m = r0 + e / n8, kk = k0 + (e % n8) * 8;
+                if (m >= R) continue;
+                if (kk + 8 <= K) {
+                    v[u] = *reinterpret_cast<const uint4 *>(X + (size_t)m * ld + kk);
+                } else {
 #pragma unroll
-                        for (int j = 0; j < 8; ++j)
-                            reinterpret_cast<__nv_bfloat16 *>(&v[u])[j] =
-                                kk + j < K ? X[(size_t)m * ld + kk + j] : zero;
-                    }
+                    for (int j = 0; j < 8; ++j) w[j] = kk + j < K ? X[(size_t)m * ld + kk + j] : zero;
                 }
-            }
+            } else {
+                // piece = 8 consecutive rows at one k; eight neighbouring
+                // threads take eight consecutive k
+                const int kl = e & 7, rest = e >> 3, r8 = rest % (ROWS / 8), kk = k0 + (rest / (ROWS / 8)) * 8 + kl;
+                const int m = r0 + r8 * 8;
+                if (kk >= K) continue;
+                if (m + 8 <= R) {
+                    v[u] = *reinterpret_cast<const uint4 *>(X + (size_t)kk * ld + m);
+                } else {
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int e = e0 + u * 128 + tid;
-                if (e < total) {
-                    const int r = e / n8, g = e % n8, s = g >> 3, k8 = g & 7;
-                    *reinterpret_cast<uint4 *>(&dst[(size_t)s * ROWS * kTcK + ((r >> 3) * (kTcK / 8) + k8) * 64 +
-                                                    (r & 7) * 8]) = v[u];
+                    for (int j = 0; j < 8; ++j) w[j] = m + j < R ? X[(size_t)kk * ld + m + j] : zero;
                 }
             }
         }
-    } else {
-        const int kw = slabs * kTcK;
-        for (int e = tid; e < ROWS * kw; e += 128) {
-            const int r = e / kw, kg = e % kw, s = kg / kTcK, k = kg % kTcK, m = r0 + r, kk = k0 + kg;
-            const __nv_bfloat16 v = (m < R && kk < K) ? (T ? X[(size_t)kk * ld + m] : X[(size_t)m * ld + kk]) : zero;
-            dst[(size_t)s * ROWS * kTcK + ((r >> 3) * (kTcK / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7)] = v;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int e = e0 + u * 128 + tid;
+            if (e >= total) continue;
+            if (!T) {
+                const int n8 = slabs * (kTcK / 8), r = e / n8, g = e % n8;
+                *reinterpret_cast<uint4 *>(&dst[tc_index<ROWS>(g >> 3, r, (g & 7) * 8)]) = v[u];
+            } else {
+                const int kl = e & 7, rest = e >> 3, r8 = rest % (ROWS / 8), kg = (rest / (ROWS / 8)) * 8 + kl;
+                // rotate the four words by the lane group so that the four
+                // groups of a warp write rows 2 apart: distinct banks
+                const int g = (tid >> 3) & 3;
+                const uint32_t w0 = v[u].x, w1 = v[u].y, w2 = v[u].z, w3 = v[u].w;
+                const uint32_t a0 = (g & 1) ? w1 : w0, a1 = (g & 1) ? w2 : w1, a2 = (g & 1) ? w3 : w2,
+                               a3 = (g & 1) ? w0 : w3;
+                const uint32_t q[4] = {(g & 2) ? a2 : a0, (g & 2) ? a3 : a1, (g & 2) ? a0 : a2, (g & 2) ? a1 : a3};
+                const int base = tc_index<ROWS>(kg / kTcK, r8 * 8, kg % kTcK);
+                uint16_t *d16 = reinterpret_cast<uint16_t *>(dst);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int j = (2 * (i + g)) & 7;  // q[i] holds elements j, j + 1
+                    d16[base + j * 8] = (uint16_t)(q[i] & 0xFFFFu);
+                    d16[base + (j + 1) * 8] = (uint16_t)(q[i] >> 16);
+                }
+            }
         }
     }
 }
@@ -204,7 +253,7 @@ template <bool TA, bool TB>
 __global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__restrict__ A, int lda,
                                                         const __nv_bfloat16 *__restrict__ B, int ldb,
                                                         float *__restrict__ C, int ldc, int M, int N, int K,
-                                                        float beta, int *err) {
+                                                        int k_split, float beta, int *err) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __nv_bfloat16 *As = reinterpret_cast<__nv_bfloat16 *>(tc_smem);            // [slab][kTcM * kTcK]
     __nv_bfloat16 *Bs = As + (size_t)kTcSlabs * kTcM * kTcK;                    // [slab][kTcN * kTcK]
@@ -213,6 +262,9 @@ __global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__r
     __shared__ int failed;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+    // this CTA's K range; with splits, C is the split's own partial tile
+    const int kb = blockIdx.z * k_split, ke = min(K, kb + k_split);
+    if (gridDim.z > 1) C += (size_t)blockIdx.z * M * ldc;
     const uint32_t mb = smem_u32(&mbar);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
@@ -230,13 +282,14 @@ __global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__r
     // idesc: F32 accumulator, BF16 A and B, both K-major, N >> 3, M >> 4
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
                            ((uint32_t)(kTcM >> 4) << 24);
-    const bool a_vec = !TA && (lda % 8) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
-    const bool b_vec = TB && (ldb % 8) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
+    const bool a_vec = (lda % 8) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+    const bool b_vec = (ldb % 8) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
     uint32_t parity = 0;
-    for (int k0 = 0; k0 < K; k0 += kTcSlabs * kTcK) {
-        const int slabs = min(kTcSlabs, (K - k0 + kTcK - 1) / kTcK);
-        tc_stage<kTcM, TA>(As, A, lda, m0, M, k0, K, slabs, a_vec);
-        tc_stage<kTcN, !TB>(Bs, B, ldb, n0, N, k0, K, slabs, b_vec);
+    bool any = false;
+    for (int k0 = kb; k0 < ke; k0 += kTcSlabs * kTcK) {
+        const int slabs = min(kTcSlabs, (ke - k0 + kTcK - 1) / kTcK);
+        tc_stage<kTcM, TA>(As, A, lda, m0, M, k0, ke, slabs, a_vec);
+        tc_stage<kTcN, !TB>(Bs, B, ldb, n0, N, k0, ke, slabs, b_vec);
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
         if (tid == 0 && !failed) {
@@ -247,7 +300,7 @@ __global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__r
                         smem_desc(smem_u32(As + (size_t)sl * kTcM * kTcK) + s * 256, 128, (kTcK / 8) * 128);
                     const uint64_t bd =
                         smem_desc(smem_u32(Bs + (size_t)sl * kTcN * kTcK) + s * 256, 128, (kTcK / 8) * 128);
-                    const uint32_t acc = (k0 > 0 || sl > 0 || s > 0) ? 1u : 0u;
+                    const uint32_t acc = (any || sl > 0 || s > 0) ? 1u : 0u;
                     asm volatile(
                         "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
                         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
@@ -256,6 +309,7 @@ __global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__r
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
                          : "memory");
         }
+        any = true;
         __syncthreads();
         if (!failed) {
             if (!mbar_wait(mb, parity)) failed = 1;
@@ -267,27 +321,36 @@ __global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__r
     asm volatile("tcgen05.fence::after_thread_sync;\n");
     if (!failed) {
         // warp w reads tensor-memory lanes 32w .. 32w+31 = rows of its quadrant
-        const int row = m0 + warp * 32 + lane;
+        // (an empty K range leaves the accumulator unwritten: the tile is 0)
+        uint32_t v[kTcN];
+#pragma unroll
         for (int c0 = 0; c0 < kTcN; c0 += 16) {
-            uint32_t v[16];
             const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
                 "[%16];\n"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                  "=r"(v[15])
+                : "=r"(v[c0 + 0]), "=r"(v[c0 + 1]), "=r"(v[c0 + 2]), "=r"(v[c0 + 3]), "=r"(v[c0 + 4]),
+                  "=r"(v[c0 + 5]), "=r"(v[c0 + 6]), "=r"(v[c0 + 7]), "=r"(v[c0 + 8]), "=r"(v[c0 + 9]),
+                  "=r"(v[c0 + 10]), "=r"(v[c0 + 11]), "=r"(v[c0 + 12]), "=r"(v[c0 + 13]), "=r"(v[c0 + 14]),
+                  "=r"(v[c0 + 15])
                 : "r"(addr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            if (row < M)
-                for (int j = 0; j < 16; ++j) {
-                    const int n = n0 + c0 + j;
-                    if (n < N) {
-                        float *c = C + (size_t)row * ldc + n;
-                        const float x = __uint_as_float(v[j]);
-                        *c = beta == 0.0f ? x : __fmaf_rn(beta, *c, x);
-                    }
-                }
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        // transpose through the (now idle) operand buffer: tile[row][col], row
+        // pitch 33 words, so both the row writes and the column reads are
+        // free of bank conflicts
+        float *tile = reinterpret_cast<float *>(tc_smem) + warp * 32 * 33;
+#pragma unroll
+        for (int j = 0; j < kTcN; ++j) tile[lane * 33 + j] = any ? __uint_as_float(v[j]) : 0.0f;
+        __syncwarp();
+        const int n = n0 + lane;
+        for (int rr = 0; rr < 32; ++rr) {
+            const int row = m0 + warp * 32 + rr;
+            if (row < M && n < N) {
+                float *c = C + (size_t)row * ldc + n;
+                const float x = tile[rr * 33 + lane];
+                *c = beta == 0.0f ? x : __fmaf_rn(beta, *c, x);
+            }
         }
     } else if (tid == 0) {
         atomicExch(err, 1);
@@ -295,6 +358,18 @@ __global__ void __launch_bounds__(128) gemm_tc05_kernel(const __nv_bfloat16 *__r
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTcN));
+}
+
+// C[m][n] = beta * C[m][n] + sum over splits s (in order) of P[s][m][n].
+__global__ void split_reduce_kernel(const float *__restrict__ P, int splits, float *__restrict__ C, int ldc, int M,
+                                    int N, float beta) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)M * N) return;
+    const int m = (int)(i / N), n = (int)(i % N);
+    float acc = 0.0f;
+    for (int s = 0; s < splits; ++s) acc += P[((size_t)s * M + m) * N + n];
+    float *c = C + (size_t)m * ldc + n;
+    *c = beta == 0.0f ? acc : __fmaf_rn(beta, *c, acc);
 }
 
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + __expf(-x)); }
@@ -644,11 +719,20 @@ int rbg_mdn_gemm(const void *A, int lda, int ta, const void *B, int ldb, int tb,
 }
 
 // The same product on tcgen05 (see gemm_tc05_kernel); *err (device int) is set
-// if a completion wait ran out.
+// if a completion wait ran out.  K is split over gridDim.z when the product
+// has fewer than 64 tiles and K >= 1024; the splits' partial tiles go to a
+// workspace owned by this function (grown on demand, released at exit), so
+// split products on different streams must not overlap.
 int rbg_mdn_gemm_tc05(const void *A, int lda, int ta, const void *B, int ldb, int tb, float *C, int ldc, int M,
                       int N, int K, float beta, int *err, void *stream) {
     using namespace rbg;
-    const dim3 grid((N + kTcN - 1) / kTcN, (M + kTcM - 1) / kTcM);
+    if (M <= 0 || N <= 0 || K < 0) return (int)cudaErrorInvalidValue;
+    const int gx = (N + kTcN - 1) / kTcN, gy = (M + kTcM - 1) / kTcM, round = kTcSlabs * kTcK;
+    const int rounds = (K + round - 1) / round;
+    int splits = 1;
+    if (gx * gy < 64 && K >= 1024) splits = std::max(1, std::min(rounds, 256 / (gx * gy)));
+    const int k_split = splits > 1 ? ((rounds + splits - 1) / splits) * round : std::max(K, 1);
+    if (splits > 1) splits = (K + k_split - 1) / k_split;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto a = static_cast<const __nv_bfloat16 *>(A);
     auto b = static_cast<const __nv_bfloat16 *>(B);
@@ -656,14 +740,35 @@ int rbg_mdn_gemm_tc05(const void *A, int lda, int ta, const void *B, int ldb, in
                 : ta     ? gemm_tc05_kernel<true, false>
                 : tb     ? gemm_tc05_kernel<false, true>
                          : gemm_tc05_kernel<false, false>;
+    static std::mutex mu;
     static bool opted[4] = {false, false, false, false};  // per variant: dynamic shared memory above 48 KB
+    static float *work = nullptr;
+    static size_t work_n = 0;
+    std::lock_guard<std::mutex> lk(mu);
     bool &o = opted[(ta ? 2 : 0) + (tb ? 1 : 0)];
     if (!o) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
         if (e != cudaSuccess) return (int)e;
         o = true;
     }
-    kern<<<grid, 128, kTcSmem, st>>>(a, lda, b, ldb, C, ldc, M, N, K, beta, err);
+    if (splits == 1) {
+        kern<<<dim3(gx, gy, 1), 128, kTcSmem, st>>>(a, lda, b, ldb, C, ldc, M, N, K, k_split, beta, err);
+        return (int)cudaGetLastError();
+    }
+    const size_t need = (size_t)splits * M * N;
+    if (need > work_n) {
+        if (work) cudaFree(work);  // synchronises the device: no launch still reads the old workspace
+        work = nullptr;
+        work_n = 0;
+        cudaError_t e = cudaMalloc(&work, need * sizeof(float));
+        if (e != cudaSuccess) return (int)e;
+        work_n = need;
+    }
+    kern<<<dim3(gx, gy, splits), 128, kTcSmem, st>>>(a, lda, b, ldb, work, N, M, N, K, k_split, 0.0f, err);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+    const size_t n = (size_t)M * N;
+    split_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(work, splits, C, ldc, M, N, beta);
     return (int)cudaGetLastError();
 }
 

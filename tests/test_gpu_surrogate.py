@@ -83,23 +83,28 @@ def test_gemm_tcgen05_matches_float64(torch):
 
     rng = np.random.default_rng(2)
     err_flag = torch.zeros(1, dtype=torch.int32, device="cuda")
-    for (M, N, K) in [(128, 64, 64), (200, 100, 80), (4096, 256, 256), (40, 256, 4096), (256, 40, 256),
-                      (130, 72, 300), (64, 33, 27), (300, 96, 520)]:
+    # (40, 256, 4096) and (130, 72, 1100) split K over the grid; the others
+    # run one K range per tile; beta != 0 checks the accumulate epilogues
+    shapes = [(128, 64, 64), (200, 100, 80), (4096, 256, 256), (40, 256, 4096), (256, 40, 256),
+              (130, 72, 300), (64, 33, 27), (300, 96, 520), (130, 72, 1100), (256, 8, 4096)]
+    for (M, N, K) in shapes:
         for ta in (0, 1):
             for tb in (0, 1):
-                a = torch.tensor(rng.standard_normal((K, M) if ta else (M, K)), dtype=torch.bfloat16).cuda()
-                b = torch.tensor(rng.standard_normal((N, K) if tb else (K, N)), dtype=torch.bfloat16).cuda()
-                c = torch.empty(M, N, dtype=torch.float32, device="cuda")
-                check(lib.rbg_mdn_gemm_tc05(a.data_ptr(), a.shape[1], ta, b.data_ptr(), b.shape[1], tb, c.data_ptr(),
-                                            N, M, N, K, 0.0, err_flag.data_ptr(),
-                                            torch.cuda.current_stream().cuda_stream))
-                torch.cuda.synchronize()
-                assert int(err_flag.item()) == 0
-                A = a.double().cpu().numpy()
-                B = b.double().cpu().numpy()
-                ref = (A.T if ta else A) @ (B.T if tb else B)
-                err = np.abs(c.cpu().numpy() - ref).max() / (np.abs(ref).max() + 1e-30)
-                assert err < 1e-5, (M, N, K, ta, tb, err)
+                for beta in ((0.0, 0.5) if (ta, tb) == (1, 0) else (0.0,)):
+                    a = torch.tensor(rng.standard_normal((K, M) if ta else (M, K)), dtype=torch.bfloat16).cuda()
+                    b = torch.tensor(rng.standard_normal((N, K) if tb else (K, N)), dtype=torch.bfloat16).cuda()
+                    c0 = rng.standard_normal((M, N))
+                    c = torch.tensor(c0, dtype=torch.float32, device="cuda")
+                    check(lib.rbg_mdn_gemm_tc05(a.data_ptr(), a.shape[1], ta, b.data_ptr(), b.shape[1], tb,
+                                                c.data_ptr(), N, M, N, K, beta, err_flag.data_ptr(),
+                                                torch.cuda.current_stream().cuda_stream))
+                    torch.cuda.synchronize()
+                    assert int(err_flag.item()) == 0
+                    A = a.double().cpu().numpy()
+                    B = b.double().cpu().numpy()
+                    ref = (A.T if ta else A) @ (B.T if tb else B) + beta * c0.astype(np.float32)
+                    err = np.abs(c.cpu().numpy() - ref).max() / (np.abs(ref).max() + 1e-30)
+                    assert err < 1e-5, (M, N, K, ta, tb, beta, err)
 
 
 def test_rate_equation_kernel_matches_scipy(torch):
