@@ -383,32 +383,54 @@ __global__ void bias_act_kernel(float *Z, const float *b, __nv_bfloat16 *H, int 
     if (H) H[i] = __float2bfloat16(act ? z * sigmoidf_(z) : z);
 }
 
-// dZ = dH * silu'(Z) as BF16 for the next GEMMs; db[n] += sum_m dZ[m][n].
-__global__ void silu_backward_kernel(const float *Z, const float *dH, __nv_bfloat16 *dZ, float *db, int M, int N) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
+// Column sums of the backward pass: a block of 32 x 32 threads owns 32
+// columns; thread (x, y) walks rows y, y + 32, ... of column x (a warp reads
+// 128 contiguous bytes per row), then the 32 partial sums of a column are
+// added in a fixed order, so db does not depend on scheduling.
+constexpr int kColX = 32, kColY = 32;
+
+// dZ = dH * silu'(Z) as BF16 for the next GEMMs; db[n] = sum_m dZ[m][n].
+__global__ void __launch_bounds__(kColX *kColY) silu_backward_kernel(const float *Z, const float *dH,
+                                                                     __nv_bfloat16 *dZ, float *db, int M, int N) {
+    __shared__ float part[kColY][kColX + 1];
+    const int n = blockIdx.x * kColX + threadIdx.x;
     float s = 0.0f;
-    for (int m = 0; m < M; ++m) {
-        const size_t i = (size_t)m * N + n;
-        const float z = Z[i], sg = sigmoidf_(z);
-        const float d = dH[i] * sg * (1.0f + z * (1.0f - sg));
-        dZ[i] = __float2bfloat16(d);
-        s += d;
+    if (n < N)
+        for (int m = threadIdx.y; m < M; m += kColY) {
+            const size_t i = (size_t)m * N + n;
+            const float z = Z[i], sg = sigmoidf_(z);
+            const float d = dH[i] * sg * (1.0f + z * (1.0f - sg));
+            dZ[i] = __float2bfloat16(d);
+            s += d;
+        }
+    part[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && n < N) {
+        float t = 0.0f;
+        for (int j = 0; j < kColY; ++j) t += part[j][threadIdx.x];
+        db[n] = t;
     }
-    db[n] = s;
 }
 
 // Bias gradient of the head and its BF16 copy: db[n] = sum_m G[m][n].
-__global__ void head_backward_kernel(const float *G, __nv_bfloat16 *Gb, float *db, int M, int N) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
+__global__ void __launch_bounds__(kColX *kColY) head_backward_kernel(const float *G, __nv_bfloat16 *Gb, float *db,
+                                                                     int M, int N) {
+    __shared__ float part[kColY][kColX + 1];
+    const int n = blockIdx.x * kColX + threadIdx.x;
     float s = 0.0f;
-    for (int m = 0; m < M; ++m) {
-        const float v = G[(size_t)m * N + n];
-        Gb[(size_t)m * N + n] = __float2bfloat16(v);
-        s += v;
+    if (n < N)
+        for (int m = threadIdx.y; m < M; m += kColY) {
+            const float v = G[(size_t)m * N + n];
+            Gb[(size_t)m * N + n] = __float2bfloat16(v);
+            s += v;
+        }
+    part[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && n < N) {
+        float t = 0.0f;
+        for (int j = 0; j < kColY; ++j) t += part[j][threadIdx.x];
+        db[n] = t;
     }
-    db[n] = s;
 }
 
 __device__ __forceinline__ float softplusf_(float x) { return x > 20.0f ? x : log1pf(__expf(x)); }
@@ -780,13 +802,15 @@ int rbg_mdn_bias_act(float *Z, const float *b, void *H, int M, int N, int act, v
 }
 
 int rbg_mdn_silu_backward(const float *Z, const float *dH, void *dZ, float *db, int M, int N, void *stream) {
-    rbg::silu_backward_kernel<<<(N + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+    rbg::silu_backward_kernel<<<(N + rbg::kColX - 1) / rbg::kColX, dim3(rbg::kColX, rbg::kColY), 0,
+                                static_cast<cudaStream_t>(stream)>>>(
         Z, dH, static_cast<__nv_bfloat16 *>(dZ), db, M, N);
     return (int)cudaGetLastError();
 }
 
 int rbg_mdn_head_backward(const float *G, void *Gb, float *db, int M, int N, void *stream) {
-    rbg::head_backward_kernel<<<(N + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+    rbg::head_backward_kernel<<<(N + rbg::kColX - 1) / rbg::kColX, dim3(rbg::kColX, rbg::kColY), 0,
+                                static_cast<cudaStream_t>(stream)>>>(
         G, static_cast<__nv_bfloat16 *>(Gb), db, M, N);
     return (int)cudaGetLastError();
 }
