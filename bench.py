@@ -700,12 +700,12 @@ def run_batch(args):
 
 SURROGATE = dict(
     name="surrogate",
-    desc=("learned surrogate of the dimer ensemble: 2^20 training tuples generated by the engine, one per "
+    desc=("learned surrogate of the dimer ensemble: 2^22 training tuples generated by the engine, one per "
           "trajectory (5 rate factors 10^U[-1,1] around 25, 1000, 0.001, 0.1, 1; t drawn from the 101-point grid "
           "of [0, 1]); rate-equation baseline per query; MLP 8 -> 4 x 256 SiLU -> count-aware head per species "
           "(classes for counts 0..30, an 8-component Gaussian mixture over the log-count residual above), BF16 "
           "weights, FP32 accumulation; held-out points judged against fresh SSA batches"),
-    n_traj=1 << 20, epochs=15, batch=4096, lr=2e-3, n_points=128, n_ssa=1000, n_points_big=64, n_ssa_big=10000,
+    n_traj=1 << 22, epochs=20, batch=4096, lr=2e-3, n_points=128, n_ssa=1000, n_points_big=64, n_ssa_big=10000,
     n_queries=1_000_000, draws=1000,
 )
 

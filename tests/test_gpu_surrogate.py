@@ -138,23 +138,26 @@ def test_surrogate_accuracy_and_gain_over_ssa(torch):
     # on held-out (rates, t) points judged by fresh 1e4-trajectory SSA batches:
     # at the stated tolerance (W1 <= 1 % of the mean count) it answers queries
     # more than 50x faster than the SSA answers them with 1000 trajectories,
-    # and where its W1 meets the tolerance the gate lets it answer.
+    # the majority of held-out points meet the tolerance for both species, the
+    # gate answers the majority of random queries, and it answers exactly where
+    # validation met the tolerance.
     import time
 
     from rebop_gb300 import surrogate as sg
 
-    x, y, _ = sg.generate(1 << 20, seed=20260106)
+    x, y, _ = sg.generate(1 << 22, seed=20260106)
     model = sg.MDN(seed=0)
-    model.fit(x, y, epochs=15, batch=4096, lr=2e-3)
+    model.fit(x, y, epochs=20, batch=4096, lr=2e-3)
     sur = sg.Surrogate(model, tol=0.01)
     big = sur.validate(64, 10000, seed=8)
     w1 = big["w1"]
-    # median relative W1 within the tolerance for both species; the fraction of
-    # points within it for both at once near the SSA-vs-SSA floor of the judge
-    assert np.median(w1[:, 0]) <= 0.01 and np.median(w1[:, 1]) <= 0.0125, np.median(w1, axis=0)
+    assert np.median(w1[:, 0]) <= 0.01 and np.median(w1[:, 1]) <= 0.01, np.median(w1, axis=0)
     ok = (w1 <= 0.01).all(axis=1)
-    floor_ok = (big["w1_floor"] <= 0.01).all(axis=1)
-    assert ok.mean() >= 0.3 and ok.mean() >= 0.55 * floor_ok.mean(), (ok.mean(), floor_ok.mean())
+    assert ok.mean() >= 0.5, (ok.mean(), (big["w1_floor"] <= 0.01).all(axis=1).mean())
+    rng = np.random.default_rng(9)
+    qa = np.concatenate([rng.uniform(-1, 1, (100000, 5)), rng.integers(1, 101, (100000, 1)) / 100],
+                        axis=1).astype(np.float32)
+    assert sur.answer(qa).mean() >= 0.5
     # speed: 1000 draws per query against 1000 SSA trajectories per query
     rng = np.random.default_rng(3)
     q = np.concatenate([rng.uniform(-1, 1, (32768, 5)), rng.integers(1, 101, (32768, 1)) / 100],
