@@ -17,7 +17,9 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <map>
+#include <thread>
 
 #include "ssa_jit.hpp"
 
@@ -610,9 +612,48 @@ void Batch::stage_inputs() {
     }
 }
 
+namespace {
+
+struct CopyTask {
+    void *dst;
+    const void *src;
+    size_t bytes;
+};
+
+// Copy every task's bytes; above 64 MB in total the tasks are cut into 16 MB
+// pieces shared out to up to 16 host threads (the page-locked staging buffer
+// is read at the host's memory bandwidth, not at one core's copy rate).
+void parallel_copy(const std::vector<CopyTask> &tasks) {
+    size_t total = 0;
+    for (const CopyTask &t : tasks) total += t.bytes;
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (total < ((size_t)64 << 20) || hw == 1) {
+        for (const CopyTask &t : tasks)
+            if (t.bytes) std::memcpy(t.dst, t.src, t.bytes);
+        return;
+    }
+    constexpr size_t kPiece = (size_t)16 << 20;
+    std::vector<CopyTask> pieces;
+    for (const CopyTask &t : tasks)
+        for (size_t o = 0; o < t.bytes; o += kPiece)
+            pieces.push_back({static_cast<unsigned char *>(t.dst) + o, static_cast<const unsigned char *>(t.src) + o,
+                              std::min(kPiece, t.bytes - o)});
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t i; (i = next.fetch_add(1)) < pieces.size();) std::memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
+    };
+    std::vector<std::thread> th;
+    for (unsigned k = 1; k < hw; ++k) th.emplace_back(work);
+    work();
+    for (std::thread &t : th) t.join();
+}
+
+}  // namespace
+
 void Batch::unstage_outputs(uint64_t &events) {
     const unsigned char *h = static_cast<const unsigned char *>(host);
     events = 0;
+    std::vector<CopyTask> tasks;
     for (Class &c : classes) {
         int64_t base = 0;
         const int64_t *out = reinterpret_cast<const int64_t *>(h + c.o_out);
@@ -623,10 +664,10 @@ void Batch::unstage_outputs(uint64_t &events) {
             if (it.in.out)
                 for (int64_t s = 0; s < c.n_samples; s++)
                     for (int32_t k = 0; k < c.n_save; k++)
-                        std::memcpy(it.in.out + (s * c.n_save + k) * n, out + (s * c.n_save + k) * c.n_traj + base,
-                                    8 * (size_t)n);
+                        tasks.push_back({it.in.out + (s * c.n_save + k) * n,
+                                         out + (s * c.n_save + k) * c.n_traj + base, 8 * (size_t)n});
             for (int64_t k = 0; k < n; k++) events += ev[base + k];
-            if (it.in.events) std::memcpy(it.in.events, ev + base, 8 * (size_t)n);
+            if (it.in.events) tasks.push_back({it.in.events, ev + base, 8 * (size_t)n});
             base += n;
         }
     }
@@ -635,11 +676,12 @@ void Batch::unstage_outputs(uint64_t &events) {
         const Item &it = items[i];
         const int64_t n = it.in.n_traj;
         const size_t ob = 8 * (size_t)(it.in.nb_steps + 1) * it.save.size() * n;
-        if (it.in.out && ob) std::memcpy(it.in.out, h + it.o_out, ob);
+        if (it.in.out && ob) tasks.push_back({it.in.out, h + it.o_out, ob});
         const uint64_t *ev = reinterpret_cast<const uint64_t *>(h + it.o_events);
         for (int64_t k = 0; k < n; k++) events += ev[k];
-        if (it.in.events) std::memcpy(it.in.events, ev, 8 * (size_t)n);
+        if (it.in.events) tasks.push_back({it.in.events, ev, 8 * (size_t)n});
     }
+    parallel_copy(tasks);
 }
 
 bool Batch::run(rb_stats_out &st_out) {
