@@ -665,7 +665,8 @@ def measure_batch(args, steps: int, warmup: int, cpu: bool = True) -> dict:
     return {
         "value": events / (kern_ms / 1e3), "unit": "events/s", "steps": steps, "warmup": warmup,
         "ms_per_step": kern_ms / steps,
-        "config": {"workload": BATCH["desc"], "items": len(items), "trajectories": len(items) * BATCH["traj"],
+        "config": {"workload": BATCH["desc"], "items": len(items), "traj_per_item": BATCH["traj"],
+                   "trajectories": len(items) * BATCH["traj"],
                    "events_per_step": events / steps, "own_launches": n_own, "persistent_items": n_persistent,
                    "mode": os.environ.get("RB_BATCH_MODE", "persistent"),
                    "timing": ("value: device time of the graph's kernels (CUDA events recorded as graph nodes); "
@@ -699,6 +700,8 @@ def run_batch(args):
                                   "d2h_bytes_per_step": 0}}), flush=True)
         return
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if args.n_traj:
+        BATCH["traj"] = args.n_traj  # trajectories per item (a smaller case for profiling)
     m = measure_batch(args, args.steps, args.warmup, cpu=not args.no_cpu_baseline)
     line = {"metric": "SSA reaction events/sec", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64+int64", "data": "synthetic", **m}
