@@ -771,11 +771,15 @@ def measure_surrogate(args) -> dict:
     gc = torch.empty(4096, 256, device="cuda")
     gemm_tflops = {}
     st = torch.cuda.current_stream().cuda_stream
-    for name in ("tc05", "mma"):
+    # tc05_tma: operands loaded by cp.async.bulk.tensor; tc05_staged: the same
+    # MMAs with operands staged by vector loads (RB_GEMM_TMA=0); mma: mma.sync
+    for name in ("tc05_tma", "tc05_staged", "mma"):
+        if name == "tc05_staged":
+            os.environ["RB_GEMM_TMA"] = "0"
         for rep in range(60):
             if rep == 10:
                 e0.record()
-            if name == "tc05":
+            if name != "mma":
                 check(lib.rbg_mdn_gemm_tc05(ga.data_ptr(), 256, 0, gb.data_ptr(), 256, 1, gc.data_ptr(), 256, 4096, 256,
                                             256, 0.0, model.tc_err.data_ptr(), st))
             else:
@@ -783,7 +787,9 @@ def measure_surrogate(args) -> dict:
                                        0.0, st))
         e1.record()
         torch.cuda.synchronize()
+        os.environ.pop("RB_GEMM_TMA", None)
         gemm_tflops[name] = 50 * 2 * 4096 * 256 * 256 / (e0.elapsed_time(e1) / 1e3) / 1e12
+    model.check_errors()
     answered = sur.answer(q[:100000]).mean()
     med = lambda a: float(np.median(a))  # noqa: E731
     ok = (big["w1"] <= 0.01).all(axis=1)

@@ -16,11 +16,15 @@
 //     dimensions.
 //   * adam: FP32 master weights, BF16 copies refreshed in place.
 //   * mdn_sample / count_sample: draws from each row's distribution.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 namespace rbg {
@@ -370,6 +374,170 @@ __global__ void split_reduce_kernel(const float *__restrict__ P, int splits, flo
     for (int s = 0; s < splits; ++s) acc += P[((size_t)s * M + m) * N + n];
     float *c = C + (size_t)m * ldc + n;
     *c = beta == 0.0f ? acc : __fmaf_rn(beta, *c, acc);
+}
+
+// ---------------------------------------------------------------- TMA-fed tcgen05
+// C = A B^T for K-contiguous A [M][K] and B [N][K] (the forward pass: inputs
+// times weights) with operands that TMA can address (row pitch a multiple of
+// 16 bytes, 16-byte aligned base).  One CTA of four warps owns a 128 x 64
+// tile of C in tensor memory.  A ring of four stages holds 64-wide K slices
+// of A (128 rows) and B (64 rows) in the 128-byte-swizzle layout that the
+// tensor map writes and the MMA descriptors read (8-row atoms of 1 KiB).
+// Thread 0 of warp 0 issues the cp.async.bulk.tensor loads (the box's bytes
+// counted on the stage's full barrier), thread 0 of warp 1 the MMAs (K = 16
+// each, the descriptor start advanced 32 bytes per step inside the atom) and
+// a commit to the stage's empty barrier; the producer waits on that before
+// reloading the stage.  A last commit releases the four warps to drain tensor
+// memory and write C through a shared-memory transpose.  Every wait has an
+// iteration limit: one that runs out sets *err, no further copy or MMA is
+// issued, copies already issued are waited for (again with a limit), and
+// tensor memory is freed.
+constexpr int kTmM = 128, kTmN = 64, kTmK = 64, kTmStages = 4;
+constexpr int kTmABytes = kTmM * kTmK * 2, kTmBBytes = kTmN * kTmK * 2, kTmStage = kTmABytes + kTmBBytes;
+constexpr size_t kTmSmem = (size_t)kTmStages * kTmStage + 1024;  // + alignment slack to 1 KiB
+
+// Shared-memory descriptor of a K-major operand in the 128-byte swizzle:
+// stride between 8-row atoms 1024 B, leading offset unused (1), version 1,
+// layout type 2 (128-byte swizzle) in bits 61-63.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
+           (2ull << 61);
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
+            "r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(128) gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                       const __grid_constant__ CUtensorMap tmB, float *__restrict__ C,
+                                                       int ldc, int M, int N, int K, float beta, int *err) {
+    extern __shared__ unsigned char tm_raw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tm_raw) + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t full[kTmStages], empty[kTmStages], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int failed;
+    __shared__ int issued;  // k slices whose loads were issued
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * kTmM, n0 = blockIdx.x * kTmN;
+    const int nk = (K + kTmK - 1) / kTmK;
+    const uint32_t sbase = smem_u32(sm);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "r"(kTmN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kTmStages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[s])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        failed = 0;
+        issued = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_base;
+    // idesc: F32 accumulator, BF16 A and B, both K-major, N >> 3, M >> 4
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTmN >> 3) << 17) |
+                           ((uint32_t)(kTmM >> 4) << 24);
+    if (tid == 0) {
+        // producer
+        for (int kb = 0; kb < nk && !failed; ++kb) {
+            const int s = kb % kTmStages;
+            if (kb >= kTmStages && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((kb / kTmStages - 1) & 1))) {
+                failed = 1;
+                break;
+            }
+            const uint32_t fb = smem_u32(&full[s]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(kTmStage)
+                         : "memory");
+            const uint32_t a_dst = sbase + s * kTmStage;
+            tma_load_2d(a_dst, &tmA, kb * kTmK, m0, fb);
+            tma_load_2d(a_dst + kTmABytes, &tmB, kb * kTmK, n0, fb);
+            issued = kb + 1;
+        }
+    } else if (tid == 32) {
+        // MMA issuer
+        int kb = 0;
+        for (; kb < nk; ++kb) {
+            const int s = kb % kTmStages;
+            if (failed || !mbar_wait(smem_u32(&full[s]), (uint32_t)((kb / kTmStages) & 1))) {
+                failed = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            const uint32_t a_addr = sbase + s * kTmStage, b_addr = a_addr + kTmABytes;
+            for (int k = 0; k < kTmK / 16; ++k) {
+                const uint64_t ad = smem_desc_sw128(a_addr + k * 32), bd = smem_desc_sw128(b_addr + k * 32);
+                const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&empty[s]))
+                         : "memory");
+        }
+        // the last commit: every MMA issued so far has completed when it fires
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                         smem_u32(&done))
+                     : "memory");
+    }
+    __syncwarp();
+    if (!mbar_wait(smem_u32(&done), 0u)) failed = 1;
+    __syncthreads();
+    if (failed) {
+        // let every copy already issued land before the CTA's shared memory goes
+        if (tid == 0)
+            for (int kb = max(0, issued - kTmStages); kb < issued; ++kb)
+                mbar_wait(smem_u32(&full[kb % kTmStages]), (uint32_t)((kb / kTmStages) & 1));
+        if (tid == 0) atomicExch(err, 1);
+    } else {
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        // warp w drains tensor-memory lanes 32w .. 32w+31 (rows of its quadrant),
+        // 32 columns at a time, through a [32][33] transpose in shared memory
+        float *tile = reinterpret_cast<float *>(sm) + warp * 32 * 33;
+        for (int c0 = 0; c0 < kTmN; c0 += 32) {
+            uint32_t v[32];
+#pragma unroll
+            for (int h = 0; h < 32; h += 16) {
+                const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c0 + h);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(v[h + 0]), "=r"(v[h + 1]), "=r"(v[h + 2]), "=r"(v[h + 3]), "=r"(v[h + 4]), "=r"(v[h + 5]),
+                      "=r"(v[h + 6]), "=r"(v[h + 7]), "=r"(v[h + 8]), "=r"(v[h + 9]), "=r"(v[h + 10]),
+                      "=r"(v[h + 11]), "=r"(v[h + 12]), "=r"(v[h + 13]), "=r"(v[h + 14]), "=r"(v[h + 15])
+                    : "r"(addr));
+            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 32; ++j) tile[lane * 33 + j] = __uint_as_float(v[j]);
+            __syncwarp();
+            const int n = n0 + c0 + lane;
+            for (int rr = 0; rr < 32; ++rr) {
+                const int row = m0 + warp * 32 + rr;
+                if (row < M && n < N) {
+                    float *c = C + (size_t)row * ldc + n;
+                    const float x = tile[rr * 33 + lane];
+                    *c = beta == 0.0f ? x : __fmaf_rn(beta, *c, x);
+                }
+            }
+            __syncwarp();
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmN));
 }
 
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + __expf(-x)); }
@@ -740,6 +908,58 @@ int rbg_mdn_gemm(const void *A, int lda, int ta, const void *B, int ldb, int tb,
     return (int)cudaGetLastError();
 }
 
+namespace {
+
+// The TMA-fed kernel takes C = A B^T with both operands K-contiguous, rows
+// 16-byte multiples apart from a 16-byte aligned base (what a tensor map can
+// address) and K >= 8; RB_GEMM_TMA=0 sends every product to the staged kernel.
+bool tma_gemm_ok(const void *A, int lda, int ta, const void *B, int ldb, int tb, int K) {
+    const char *e = std::getenv("RB_GEMM_TMA");
+    const bool off = e && std::strcmp(e, "0") == 0;
+    return !off && !ta && tb && K >= 8 && lda % 8 == 0 && ldb % 8 == 0 &&
+           (reinterpret_cast<uintptr_t>(A) & 15) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
+}
+
+// 2-D tensor map of a row-major BF16 matrix [rows][K] (row pitch ld elements)
+// read in boxes of 64 (K) x box_rows with the 128-byte swizzle; false if the
+// driver has no encoder or refuses the operands.
+bool encode_rows(CUtensorMap &map, const void *base, int rows, int K, int ld, int box_rows) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }();
+    if (!encode) return false;
+    const cuuint64_t dim[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    const cuuint64_t stride[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)rbg::kTmK, (cuuint32_t)box_rows};
+    const cuuint32_t elem[2] = {1, 1};
+    return encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dim, stride, box, elem,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Launch gemm_tma_kernel; returns a CUDA error code, or -1 when no tensor map
+// could be made (nothing launched).
+int gemm_tma(const void *A, int lda, const void *B, int ldb, float *C, int ldc, int M, int N, int K, float beta,
+             int *err, cudaStream_t st) {
+    using namespace rbg;
+    CUtensorMap ma, mb;
+    if (!encode_rows(ma, A, M, K, lda, kTmM) || !encode_rows(mb, B, N, K, ldb, kTmN)) return -1;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmSmem);
+    if (attr != cudaSuccess) return (int)attr;
+    const dim3 grid((N + kTmN - 1) / kTmN, (M + kTmM - 1) / kTmM);
+    gemm_tma_kernel<<<grid, 128, kTmSmem, st>>>(ma, mb, C, ldc, M, N, K, beta, err);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace
+
 // The same product on tcgen05 (see gemm_tc05_kernel); *err (device int) is set
 // if a completion wait ran out.  K is split over gridDim.z when the product
 // has fewer than 64 tiles and K >= 1024; the splits' partial tiles go to a
@@ -758,6 +978,10 @@ int rbg_mdn_gemm_tc05(const void *A, int lda, int ta, const void *B, int ldb, in
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto a = static_cast<const __nv_bfloat16 *>(A);
     auto b = static_cast<const __nv_bfloat16 *>(B);
+    if (splits == 1 && tma_gemm_ok(A, lda, ta, B, ldb, tb, K)) {
+        const int e = gemm_tma(A, lda, B, ldb, C, ldc, M, N, K, beta, err, st);
+        if (e >= 0) return e;  // < 0: no tensor map for these operands; the staged kernel runs
+    }
     auto kern = ta && tb ? gemm_tc05_kernel<true, true>
                 : ta     ? gemm_tc05_kernel<true, false>
                 : tb     ? gemm_tc05_kernel<false, true>

@@ -83,14 +83,19 @@ def test_gemm_tcgen05_matches_float64(torch):
 
     rng = np.random.default_rng(2)
     err_flag = torch.zeros(1, dtype=torch.int32, device="cuda")
-    # (40, 256, 4096) and (130, 72, 1100) split K over the grid; the others
-    # run one K range per tile; beta != 0 checks the accumulate epilogues
+    # (40, 256, 4096), (130, 72, 1100) and (256, 8, 4096) split K over the
+    # grid; products of K-contiguous operands with rows 16-byte multiples apart
+    # (ta = 0, tb = 1, K % 8 == 0) take the TMA-fed kernel -- (520, 200, 1000)
+    # cycles its four-stage ring four times, (1000, 256, 8) reads one 8-wide
+    # K slice, (4096, 112, 256) ends in a partial tile; beta != 0 checks the
+    # accumulate epilogues
     shapes = [(128, 64, 64), (200, 100, 80), (4096, 256, 256), (40, 256, 4096), (256, 40, 256),
-              (130, 72, 300), (64, 33, 27), (300, 96, 520), (130, 72, 1100), (256, 8, 4096)]
+              (130, 72, 300), (64, 33, 27), (300, 96, 520), (130, 72, 1100), (256, 8, 4096),
+              (520, 200, 1000), (1000, 256, 8), (4096, 112, 256)]
     for (M, N, K) in shapes:
         for ta in (0, 1):
             for tb in (0, 1):
-                for beta in ((0.0, 0.5) if (ta, tb) == (1, 0) else (0.0,)):
+                for beta in ((0.0, 0.5) if (ta, tb) in ((1, 0), (0, 1)) else (0.0,)):
                     a = torch.tensor(rng.standard_normal((K, M) if ta else (M, K)), dtype=torch.bfloat16).cuda()
                     b = torch.tensor(rng.standard_normal((N, K) if tb else (K, N)), dtype=torch.bfloat16).cuda()
                     c0 = rng.standard_normal((M, N))
