@@ -763,32 +763,7 @@ def measure_surrogate(args) -> dict:
     torch.cuda.synchronize()
     param_qps = w["n_queries"] / (e0.elapsed_time(e1) / 1e3)
     ssa_qps = w["n_points"] / (val["ssa_kernel_ms"] / 1e3)
-    # the training GEMM shape (4096 x 256 x 256, BF16 in, FP32 out) on both tensor-core kernels
-    from rebop_gb300._lib import check, lib
-
-    ga = torch.randn(4096, 256, device="cuda").to(torch.bfloat16)
-    gb = torch.randn(256, 256, device="cuda").to(torch.bfloat16)
-    gc = torch.empty(4096, 256, device="cuda")
-    gemm_tflops = {}
-    st = torch.cuda.current_stream().cuda_stream
-    # tc05_tma: operands loaded by cp.async.bulk.tensor; tc05_staged: the same
-    # MMAs with operands staged by vector loads (RB_GEMM_TMA=0); mma: mma.sync
-    for name in ("tc05_tma", "tc05_staged", "mma"):
-        if name == "tc05_staged":
-            os.environ["RB_GEMM_TMA"] = "0"
-        for rep in range(60):
-            if rep == 10:
-                e0.record()
-            if name != "mma":
-                check(lib.rbg_mdn_gemm_tc05(ga.data_ptr(), 256, 0, gb.data_ptr(), 256, 1, gc.data_ptr(), 256, 4096, 256,
-                                            256, 0.0, model.tc_err.data_ptr(), st))
-            else:
-                check(lib.rbg_mdn_gemm(ga.data_ptr(), 256, 0, gb.data_ptr(), 256, 1, gc.data_ptr(), 256, 4096, 256, 256,
-                                       0.0, st))
-        e1.record()
-        torch.cuda.synchronize()
-        os.environ.pop("RB_GEMM_TMA", None)
-        gemm_tflops[name] = 50 * 2 * 4096 * 256 * 256 / (e0.elapsed_time(e1) / 1e3) / 1e12
+    gemm_tflops = gemm_figures(model.tc_err)
     model.check_errors()
     answered = sur.answer(q[:100000]).mean()
     med = lambda a: float(np.median(a))  # noqa: E731
@@ -821,6 +796,84 @@ def measure_surrogate(args) -> dict:
     }
 
 
+def gemm_figures(err_flag, reps: int = 50) -> dict:
+    """TFLOP/s of the training GEMM shape (4096 x 256 x 256, BF16 in, FP32 out)
+    on each tensor-core path: tc05_tma (operands by cp.async.bulk.tensor),
+    tc05_staged (the same MMAs, operands staged by vector loads,
+    RB_GEMM_TMA=0) and mma (mma.sync); `reps` back-to-back launches each,
+    CUDA events on the launching stream."""
+    import torch
+
+    from rebop_gb300._lib import check, lib
+
+    ga = torch.randn(4096, 256, device="cuda").to(torch.bfloat16)
+    gb = torch.randn(256, 256, device="cuda").to(torch.bfloat16)
+    gc = torch.empty(4096, 256, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    st = torch.cuda.current_stream().cuda_stream
+    out = {}
+    for name in ("tc05_tma", "tc05_staged", "mma"):
+        if name == "tc05_staged":
+            os.environ["RB_GEMM_TMA"] = "0"
+        for rep in range(reps + 10):
+            if rep == 10:
+                e0.record()
+            if name != "mma":
+                check(lib.rbg_mdn_gemm_tc05(ga.data_ptr(), 256, 0, gb.data_ptr(), 256, 1, gc.data_ptr(), 256, 4096,
+                                            256, 256, 0.0, err_flag.data_ptr(), st))
+            else:
+                check(lib.rbg_mdn_gemm(ga.data_ptr(), 256, 0, gb.data_ptr(), 256, 1, gc.data_ptr(), 256, 4096, 256,
+                                       256, 0.0, st))
+        e1.record()
+        torch.cuda.synchronize()
+        os.environ.pop("RB_GEMM_TMA", None)
+        out[name] = reps * 2 * 4096 * 256 * 256 / (e0.elapsed_time(e1) / 1e3) / 1e12
+    return out
+
+
+def run_gemm(args):
+    """The surrogate's GEMM alone: one JSON line of TFLOP/s per tensor-core path."""
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    reps = max(args.steps, 1) * 50
+    f = gemm_figures(err, reps)
+    if int(err.item()):
+        raise RuntimeError("tcgen05 GEMM: a completion wait ran out")
+    try:
+        peak, src = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"]), \
+            "MEASURED_PEAKS.json bf16_tflops (burst, of measured)"
+    except (OSError, ValueError, KeyError):
+        peak, src = 1900.0, "fallback 1.9 PFLOP/s (of fallback)"
+    # the fused inference kernel on the same network shape (random weights):
+    # 65 536 queries per launch, the whole MLP in one kernel
+    from rebop_gb300 import surrogate as sg
+
+    model = sg.MDN(seed=0)
+    F = torch.randn(65536, sg.N_IN, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for rep in range(reps // 10 + 5):
+        if rep == 5:
+            e0.record()
+        model.infer(F)
+    e1.record()
+    torch.cuda.synchronize()
+    model.check_errors()
+    n_inf = reps // 10
+    inf_s = e0.elapsed_time(e1) / 1e3 / n_inf
+    flop = 2.0 * 65536 * (sg.N_IN * 256 + 3 * 256 * 256 + 256 * model.n_out)
+    f["fused_inference"] = {"queries_per_s": 65536 / inf_s, "us_per_launch": inf_s * 1e6, "tflops": flop / inf_s / 1e12}
+    v = f["tc05_tma"]
+    print(json.dumps({"metric": "BF16 GEMM TFLOP/s, 4096 x 256 x 256, FP32 accumulate", "value": v,
+                      "unit": "TFLOP/s", "n_gpus": 1, "steps": reps, "warmup": 10, "higher_is_better": True,
+                      "dtype": "bf16", "data": "synthetic", "paths": f,
+                      "roofline": {"bound": "tensor", "achieved": v, "peak": peak, "unit": "TFLOP/s",
+                                   "frac": v / peak, "peak_source": src,
+                                   "note": "0.54 GFLOP per launch: launch- and latency-bound at this size"}}),
+          flush=True)
+
+
 def run_surrogate(args):
     import torch
 
@@ -837,7 +890,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch", "surrogate"], default="dimer")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch", "surrogate", "gemm"], default="dimer")
     ap.add_argument("--n-traj", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -847,6 +900,12 @@ def main():
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "gemm":
+        if args.impl == "ours":
+            run_gemm(args)
+        elif int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no GEMM"}), flush=True)
         return
     if args.workload == "surrogate":
         if args.impl == "reference":

@@ -152,6 +152,8 @@ for _name, _args in {
     "rbg_mdn_rre": [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp, _vp],
     "rbg_mdn_count_loss": [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp],
     "rbg_mdn_count_sample": [_vp, C.c_int, C.c_int, _u64, _vp, C.c_int, _vp, _vp],
+    "rbg_mdn_infer": [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int,
+                      _vp, _vp, _vp],
 }.items():
     getattr(lib, _name).argtypes = _args
     getattr(lib, _name).restype = C.c_int

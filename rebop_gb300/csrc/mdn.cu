@@ -542,6 +542,250 @@ __global__ void __launch_bounds__(128) gemm_tma_kernel(const __grid_constant__ C
 
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + __expf(-x)); }
 
+// ---------------------------------------------------------------- fused inference
+// The whole forward pass of the surrogate for 128 queries per tile, in one
+// kernel: features -> 4 x (256, SiLU) -> head.  The activations of a tile
+// stay in shared memory as the next layer's A operand (128 x 256 BF16, the
+// 128-byte-swizzle K-major layout: four 64-wide K slices of 16 KB); the
+// weights stream through a three-stage ring by cp.async.bulk.tensor (one
+// 64-wide K slice of a layer's [N][K] matrix per stage, issued by a producer
+// warp that runs ahead across layers and tiles); the accumulator is a
+// 128 x 256 FP32 tile in tensor memory.  Per layer thread 0 issues the MMAs
+// (K = 16 each) and commits; the four warps then drain their lane quadrants,
+// add the bias and apply SiLU (the forward pass's formula) and write BF16
+// back into the activation buffer, or the head's FP32 outputs to global
+// memory.  Waits are bounded; one that runs out sets *err, the tile loop ends
+// at the next layer boundary, issued copies are waited for, tensor memory is
+// freed.
+constexpr int kInfHid = 256, kInfLayers = 5, kInfStages = 3, kInfWarps = 5;
+constexpr int kInfHBytes = 128 * kInfHid * 2;              // activations, 64 KB
+constexpr int kInfStageBytes = kInfHid * 128;              // one weight K slice of up to 256 rows
+constexpr size_t kInfSmem = (size_t)kInfHBytes + (size_t)kInfStages * kInfStageBytes + 1024;
+
+struct InferMaps {
+    CUtensorMap w[kInfLayers];
+};
+
+// OR of v over the 128 threads of warps 0-3 at named barrier 1: every one of
+// them gets the same answer, so a loop they leave on it is left by all.
+__device__ __forceinline__ bool bar_or_128(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
+}
+
+__global__ void __launch_bounds__(32 * kInfWarps, 1) mlp_infer_kernel(const __grid_constant__ InferMaps maps,
+                                                                      const float *__restrict__ F, int Q, int n_in,
+                                                                      const float *__restrict__ x_mean,
+                                                                      const float *__restrict__ x_std,
+                                                                      const float *__restrict__ b0,
+                                                                      const float *__restrict__ b1,
+                                                                      const float *__restrict__ b2,
+                                                                      const float *__restrict__ b3,
+                                                                      const float *__restrict__ b4, int n_out,
+                                                                      float *__restrict__ O, int *err) {
+    extern __shared__ unsigned char inf_raw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(inf_raw) + 1023) & ~(uintptr_t)1023);
+    unsigned char *H = sm;                     // [4 slices][128 rows][128 B], swizzled
+    unsigned char *ring = sm + kInfHBytes;     // [stage][up to 256 rows][128 B]
+    __shared__ float bias[kInfLayers - 1][kInfHid];
+    __shared__ float bias_out[kInfHid];
+    __shared__ __align__(8) uint64_t full[kInfStages], empty[kInfStages], layer_done;
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int failed;
+    __shared__ int issued;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n_tiles = (Q + 127) / 128;
+    const int n_mma = (n_out + 15) & ~15;  // head MMA width (the tensor map zero-fills rows >= n_out)
+    // K slices and weight rows per layer
+    auto slices = [&](int l) { return l == 0 ? 1 : kInfHid / 64; };
+    auto rows = [&](int l) { return l == kInfLayers - 1 ? n_mma : kInfHid; };
+    for (int k = tid; k < kInfHid; k += blockDim.x) {
+        bias[0][k] = b0[k];
+        bias[1][k] = b1[k];
+        bias[2][k] = b2[k];
+        bias[3][k] = b3[k];
+        bias_out[k] = k < n_out ? b4[k] : 0.0f;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "r"(kInfHid));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kInfStages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[s])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&layer_done)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        failed = 0;
+        issued = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_base;
+    const uint32_t h_addr = smem_u32(H), ring_addr = smem_u32(ring);
+
+    if (warp == kInfWarps - 1) {
+        // ---- producer: every weight slice of every layer of every tile, in order
+        if (lane == 0) {
+            int seq = 0;
+            for (int tile = blockIdx.x; tile < n_tiles && !failed; tile += gridDim.x)
+                for (int l = 0; l < kInfLayers && !failed; ++l)
+                    for (int ks = 0; ks < slices(l); ++ks, ++seq) {
+                        const int st = seq % kInfStages;
+                        if (seq >= kInfStages &&
+                            !mbar_wait(smem_u32(&empty[st]), (uint32_t)((seq / kInfStages - 1) & 1))) {
+                            failed = 1;
+                            break;
+                        }
+                        const uint32_t fb = smem_u32(&full[st]);
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb),
+                                     "r"(rows(l) * 128)
+                                     : "memory");
+                        tma_load_2d(ring_addr + st * kInfStageBytes, &maps.w[l], ks * 64, 0, fb);
+                        issued = seq + 1;
+                    }
+        }
+    } else {
+        // ---- four warps: stage inputs, issue MMAs (thread 0), drain and activate
+        const int r = tid;  // this thread's row of the tile (tensor-memory lane)
+        const float *mean = x_mean, *sd = x_std;
+        int seq = 0, layers_run = 0;
+        bool stop = false;
+        for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+            // features of row r, normalised, as BF16 in K slice 0 (zeros beyond n_in)
+            const int q = tile * 128 + r;
+            uint32_t w4[4] = {0u, 0u, 0u, 0u};
+            if (q < Q)
+                for (int j = 0; j < 8 && j < n_in; j += 2) {
+                    const float v0 = (F[(size_t)q * n_in + j] - mean[j]) / sd[j];
+                    const float v1 = j + 1 < n_in ? (F[(size_t)q * n_in + j + 1] - mean[j + 1]) / sd[j + 1] : 0.0f;
+                    const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
+                    w4[j >> 1] = *reinterpret_cast<const uint32_t *>(&h2);
+                }
+            for (int c = 0; c < 8; ++c) {
+                const uint4 v = c == 0 ? make_uint4(w4[0], w4[1], w4[2], w4[3]) : make_uint4(0u, 0u, 0u, 0u);
+                *reinterpret_cast<uint4 *>(H + r * 128 + ((c ^ (r & 7)) << 4)) = v;
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            asm volatile("bar.sync 1, 128;\n" ::: "memory");
+            for (int l = 0; l < kInfLayers; ++l) {
+                if (tid == 0) {
+                    asm volatile("tcgen05.fence::after_thread_sync;\n");
+                    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) |
+                                           ((uint32_t)(rows(l) >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+                    const int ksteps = l == 0 ? (n_in + 15) / 16 : 4;  // 16-wide K steps per slice
+                    for (int ks = 0; ks < slices(l); ++ks, ++seq) {
+                        const int st = seq % kInfStages;
+                        if (failed || !mbar_wait(smem_u32(&full[st]), (uint32_t)((seq / kInfStages) & 1))) {
+                            failed = 1;
+                            break;
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;\n");
+                        for (int k = 0; k < ksteps; ++k) {
+                            const uint64_t ad = smem_desc_sw128(h_addr + ks * 16384 + k * 32);
+                            const uint64_t bd = smem_desc_sw128(ring_addr + st * kInfStageBytes + k * 32);
+                            const uint32_t acc = (ks > 0 || k > 0) ? 1u : 0u;
+                            asm volatile(
+                                "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                        }
+                        asm volatile(
+                            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                smem_u32(&empty[st]))
+                            : "memory");
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                     smem_u32(&layer_done))
+                                 : "memory");
+                }
+                __syncwarp();
+                bool bad = !mbar_wait(smem_u32(&layer_done), (uint32_t)(layers_run & 1));
+                ++layers_run;
+                // one decision for all four warps (the producer may set failed
+                // at any moment; the epilogue's tensor-memory loads are
+                // warp-collective and its barriers count all 128 threads)
+                stop = bar_or_128(bad || failed != 0);
+                if (stop) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+                const bool last = l == kInfLayers - 1;
+                const int ncol = last ? n_mma : kInfHid;
+                for (int c0 = 0; c0 < ncol; c0 += 16) {
+                    uint32_t v[16];
+                    const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                        "[%16];\n"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(addr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    if (last) {
+                        if (q < Q)
+                            for (int j = 0; j < 16; j += 4) {
+                                const int n = c0 + j;
+                                if (n + 4 <= n_out) {
+                                    *reinterpret_cast<float4 *>(O + (size_t)q * n_out + n) = make_float4(
+                                        __uint_as_float(v[j]) + bias_out[n], __uint_as_float(v[j + 1]) + bias_out[n + 1],
+                                        __uint_as_float(v[j + 2]) + bias_out[n + 2],
+                                        __uint_as_float(v[j + 3]) + bias_out[n + 3]);
+                                } else {
+                                    for (int u = 0; u < 4 && n + u < n_out; ++u)
+                                        O[(size_t)q * n_out + n + u] = __uint_as_float(v[j + u]) + bias_out[n + u];
+                                }
+                            }
+                    } else {
+                        uint32_t pk[8];
+#pragma unroll
+                        for (int j = 0; j < 16; j += 2) {
+                            const float z0 = __uint_as_float(v[j]) + bias[l][c0 + j];
+                            const float z1 = __uint_as_float(v[j + 1]) + bias[l][c0 + j + 1];
+                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(z0 * sigmoidf_(z0), z1 * sigmoidf_(z1));
+                            pk[j >> 1] = *reinterpret_cast<const uint32_t *>(&h2);
+                        }
+                        // columns c0 .. c0+15: K slice c0 / 64, chunks (c0 % 64) / 8 and + 1
+                        unsigned char *row = H + (c0 >> 6) * 16384 + r * 128;
+                        const int ch = (c0 & 63) >> 3;
+                        *reinterpret_cast<uint4 *>(row + ((ch ^ (r & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                        *reinterpret_cast<uint4 *>(row + (((ch + 1) ^ (r & 7)) << 4)) =
+                            make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                    }
+                }
+                // the accumulator is read and the activations written before the
+                // next layer's MMAs start
+                asm volatile("tcgen05.fence::before_thread_sync;\n");
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                asm volatile("bar.sync 1, 128;\n" ::: "memory");
+            }
+            if (stop) break;
+        }
+        if (stop && tid == 0) failed = 1;
+    }
+    __syncthreads();
+    if (failed) {
+        if (tid == 0) {
+            // copies already issued land before the shared memory is released
+            const int n = issued;
+            for (int sq = max(0, n - kInfStages); sq < n; ++sq)
+                mbar_wait(smem_u32(&full[sq % kInfStages]), (uint32_t)((sq / kInfStages) & 1));
+            atomicExch(err, 1);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kInfHid));
+}
+
 // Z[m][n] += b[n]; H = bf16(silu(Z)) (act = 1) or bf16(Z) (act = 0).
 __global__ void bias_act_kernel(float *Z, const float *b, __nv_bfloat16 *H, int M, int N, int act) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1015,6 +1259,42 @@ int rbg_mdn_gemm_tc05(const void *A, int lda, int ta, const void *B, int ldb, in
     if (e != cudaSuccess) return (int)e;
     const size_t n = (size_t)M * N;
     split_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(work, splits, C, ldc, M, N, beta);
+    return (int)cudaGetLastError();
+}
+
+// The surrogate's whole forward pass in one launch (mlp_infer_kernel): F
+// [Q][n_in] raw features (n_in = 8), normalised by x_mean / x_std; W0 [256][8],
+// W1..W3 [256][256], W4 [n_out][256] BF16 weights (row-major [out][in]); b0..b4
+// FP32 biases; O [Q][n_out] FP32 head outputs.  n_out <= 256 and a multiple of
+// 4.  Returns a CUDA error code (cudaErrorInvalidValue for shapes it does not
+// cover, cudaErrorNotSupported without a tensor-map encoder).
+int rbg_mdn_infer(const float *F, int Q, int n_in, const float *x_mean, const float *x_std, const void *W0,
+                  const void *W1, const void *W2, const void *W3, const void *W4, const float *b0, const float *b1,
+                  const float *b2, const float *b3, const float *b4, int n_out, float *O, int *err, void *stream) {
+    using namespace rbg;
+    if (Q < 0 || n_in != 8 || n_out <= 0 || n_out > kInfHid || n_out % 4 != 0) return (int)cudaErrorInvalidValue;
+    if (Q == 0) return 0;
+    for (const void *w : {W0, W1, W2, W3, W4})
+        if (reinterpret_cast<uintptr_t>(w) & 15) return (int)cudaErrorInvalidValue;
+    if ((reinterpret_cast<uintptr_t>(O) & 15) != 0) return (int)cudaErrorInvalidValue;
+    const int n_mma = (n_out + 15) & ~15;
+    InferMaps maps;
+    if (!encode_rows(maps.w[0], W0, kInfHid, n_in, n_in, kInfHid) ||
+        !encode_rows(maps.w[1], W1, kInfHid, kInfHid, kInfHid, kInfHid) ||
+        !encode_rows(maps.w[2], W2, kInfHid, kInfHid, kInfHid, kInfHid) ||
+        !encode_rows(maps.w[3], W3, kInfHid, kInfHid, kInfHid, kInfHid) ||
+        !encode_rows(maps.w[4], W4, n_out, kInfHid, kInfHid, n_mma))
+        return (int)cudaErrorNotSupported;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInfSmem);
+    if (attr != cudaSuccess) return (int)attr;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = (Q + 127) / 128;
+    const int grid = std::max(1, std::min(tiles, sms));
+    mlp_infer_kernel<<<grid, 32 * kInfWarps, kInfSmem, static_cast<cudaStream_t>(stream)>>>(
+        maps, F, Q, n_in, x_mean, x_std, b0, b1, b2, b3, b4, n_out, O, err);
     return (int)cudaGetLastError();
 }
 

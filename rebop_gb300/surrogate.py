@@ -263,13 +263,31 @@ class MDN:
                 log(f"epoch {ep}: loss {tot / max(cnt, 1):.4f}")
         self.check_errors()
 
+    def infer(self, F):
+        """Head outputs [Q][n_out] for feature rows F [Q][8] (unnormalised), by the
+        fused inference kernel: the whole MLP in one launch, activations kept
+        in shared memory (``rbg_mdn_infer``).  Falls back to the layer-by-layer
+        forward pass for heads it does not cover (n_out not a multiple of 4) or
+        with RB_GEMM=mma."""
+        torch = self.torch
+        F = F.contiguous()
+        if not self.use_tc05 or self.n_out % 4 != 0 or self.n_out > HIDDEN or LAYERS != 4 or HIDDEN != 256:
+            return self.forward(F)
+        O = torch.empty(F.shape[0], self.n_out, dtype=torch.float32, device=self.dev)
+        W, b = self.Wb, self.b
+        check(lib.rbg_mdn_infer(F.data_ptr(), F.shape[0], F.shape[1], self.x_mean.data_ptr(), self.x_std.data_ptr(),
+                                W[0].data_ptr(), W[1].data_ptr(), W[2].data_ptr(), W[3].data_ptr(), W[4].data_ptr(),
+                                b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr(), b[3].data_ptr(), b[4].data_ptr(),
+                                self.n_out, O.data_ptr(), self.tc_err.data_ptr(), self._s()))
+        return O
+
     def sample_counts(self, x, n_draws: int, seed: int = 1):
         """n_draws samples of (protein, dimer) counts at each query row of x [Q][6]:
         the rate equations and one forward pass per query, then n_draws draws
         from its head, each turned into a count by the sampler kernel."""
         F = features(self._queries(x))
         torch = self.torch
-        o = self.forward(F)
+        o = self.infer(F)
         base = F[:, N_QUERY:].contiguous()
         c = torch.empty(F.shape[0] * n_draws, 2, dtype=torch.float32, device=self.dev)
         if self.head == "count":
@@ -282,7 +300,7 @@ class MDN:
 
     def predict_params(self, x):
         """Head outputs at each query row (one forward pass): [Q][n_out]."""
-        return self.forward(features(self._queries(x)))
+        return self.infer(features(self._queries(x)))
 
     def _queries(self, x):
         torch = self.torch

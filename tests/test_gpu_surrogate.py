@@ -112,6 +112,30 @@ def test_gemm_tcgen05_matches_float64(torch):
                     assert err < 1e-5, (M, N, K, ta, tb, beta, err)
 
 
+@pytest.mark.parametrize("head", ["count", "mixture"])
+def test_fused_inference_matches_layer_by_layer(torch, head):
+    # rbg_mdn_infer (the whole MLP in one launch, activations in shared memory,
+    # weights by TMA) against the layer-by-layer forward pass of the same
+    # weights: one partial tile, several tiles, and more tiles than SMs
+    from rebop_gb300 import surrogate as sg
+
+    rng = np.random.default_rng(6)
+    model = sg.MDN(seed=4, head=head)
+    # non-trivial biases and input normalisation
+    for b in model.b:
+        b.copy_(torch.tensor(rng.normal(0, 0.1, b.shape[0]), dtype=torch.float32))
+    model.x_mean = torch.tensor(rng.normal(0, 0.3, sg.N_IN), dtype=torch.float32).cuda()
+    model.x_std = torch.tensor(rng.uniform(0.5, 2.0, sg.N_IN), dtype=torch.float32).cuda()
+    for Q in (5, 1000, 70001):
+        F = torch.tensor(rng.uniform(-2, 2, (Q, sg.N_IN)), dtype=torch.float32).cuda()
+        fused = model.infer(F).cpu().numpy()
+        ref = model.forward(F).cpu().numpy()
+        model.check_errors()
+        assert fused.shape == ref.shape == (Q, model.n_out)
+        scale = np.abs(ref).max()
+        assert np.abs(fused - ref).max() <= 1e-3 * scale, (Q, np.abs(fused - ref).max(), scale)
+
+
 def test_rate_equation_kernel_matches_scipy(torch):
     # rbg_mdn_rre (float32 RK4, the surrogate's deterministic part) against an
     # adaptive float64 solution of the same rate equations
