@@ -551,13 +551,13 @@ __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + __ex
 // 64-wide K slice of a layer's [N][K] matrix per stage, issued by a producer
 // warp that runs ahead across layers and tiles); the accumulator is a
 // 128 x 256 FP32 tile in tensor memory.  Per layer thread 0 issues the MMAs
-// (K = 16 each) and commits; the four warps then drain their lane quadrants,
-// add the bias and apply SiLU (the forward pass's formula) and write BF16
+// (K = 16 each) and commits; eight warps then drain the accumulator (two per
+// lane quadrant), add the bias and apply SiLU and write BF16
 // back into the activation buffer, or the head's FP32 outputs to global
 // memory.  Waits are bounded; one that runs out sets *err, the tile loop ends
 // at the next layer boundary, issued copies are waited for, tensor memory is
 // freed.
-constexpr int kInfHid = 256, kInfLayers = 5, kInfStages = 3, kInfWarps = 5;
+constexpr int kInfHid = 256, kInfLayers = 5, kInfStages = 3, kInfWarps = 9;  // 8 compute + 1 producer
 constexpr int kInfHBytes = 128 * kInfHid * 2;              // activations, 64 KB
 constexpr int kInfStageBytes = kInfHid * 128;              // one weight K slice of up to 256 rows
 constexpr size_t kInfSmem = (size_t)kInfHBytes + (size_t)kInfStages * kInfStageBytes + 1024;
@@ -566,12 +566,12 @@ struct InferMaps {
     CUtensorMap w[kInfLayers];
 };
 
-// OR of v over the 128 threads of warps 0-3 at named barrier 1: every one of
+// OR of v over the 256 threads of warps 0-7 at named barrier 1: every one of
 // them gets the same answer, so a loop they leave on it is left by all.
-__device__ __forceinline__ bool bar_or_128(bool v) {
+__device__ __forceinline__ bool bar_or_256(bool v) {
     uint32_t r;
     asm volatile(
-        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, 256, p;\n selp.u32 %0, 1, 0, q;\n}\n"
         : "=r"(r)
         : "r"((uint32_t)v)
         : "memory");
@@ -655,28 +655,35 @@ __global__ void __launch_bounds__(32 * kInfWarps, 1) mlp_infer_kernel(const __gr
                     }
         }
     } else {
-        // ---- four warps: stage inputs, issue MMAs (thread 0), drain and activate
-        const int r = tid;  // this thread's row of the tile (tensor-memory lane)
-        const float *mean = x_mean, *sd = x_std;
+        // ---- eight warps: stage inputs, issue MMAs (thread 0), drain and
+        // activate.  Warp w reads tensor-memory lanes 32 (w % 4) .. + 31 (rows
+        // of its quadrant); warps w and w + 4 split the columns in 32-wide
+        // chunks.
+        const int r = (warp & 3) * 32 + lane;  // this thread's row of the tile (tensor-memory lane)
+        const int half = warp >> 2;
+        const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
         int seq = 0, layers_run = 0;
         bool stop = false;
         for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-            // features of row r, normalised, as BF16 in K slice 0 (zeros beyond n_in)
             const int q = tile * 128 + r;
-            uint32_t w4[4] = {0u, 0u, 0u, 0u};
-            if (q < Q)
-                for (int j = 0; j < 8 && j < n_in; j += 2) {
-                    const float v0 = (F[(size_t)q * n_in + j] - mean[j]) / sd[j];
-                    const float v1 = j + 1 < n_in ? (F[(size_t)q * n_in + j + 1] - mean[j + 1]) / sd[j + 1] : 0.0f;
-                    const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
-                    w4[j >> 1] = *reinterpret_cast<const uint32_t *>(&h2);
+            if (half == 0) {
+                // features of row r, normalised, as BF16 in K slice 0 (zeros beyond n_in)
+                uint32_t w4[4] = {0u, 0u, 0u, 0u};
+                if (q < Q)
+                    for (int j = 0; j < 8 && j < n_in; j += 2) {
+                        const float v0 = (F[(size_t)q * n_in + j] - x_mean[j]) / x_std[j];
+                        const float v1 =
+                            j + 1 < n_in ? (F[(size_t)q * n_in + j + 1] - x_mean[j + 1]) / x_std[j + 1] : 0.0f;
+                        const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
+                        w4[j >> 1] = *reinterpret_cast<const uint32_t *>(&h2);
+                    }
+                for (int c = 0; c < 8; ++c) {
+                    const uint4 v = c == 0 ? make_uint4(w4[0], w4[1], w4[2], w4[3]) : make_uint4(0u, 0u, 0u, 0u);
+                    *reinterpret_cast<uint4 *>(H + r * 128 + ((c ^ (r & 7)) << 4)) = v;
                 }
-            for (int c = 0; c < 8; ++c) {
-                const uint4 v = c == 0 ? make_uint4(w4[0], w4[1], w4[2], w4[3]) : make_uint4(0u, 0u, 0u, 0u);
-                *reinterpret_cast<uint4 *>(H + r * 128 + ((c ^ (r & 7)) << 4)) = v;
             }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            asm volatile("bar.sync 1, 128;\n" ::: "memory");
+            asm volatile("bar.sync 1, 256;\n" ::: "memory");
             for (int l = 0; l < kInfLayers; ++l) {
                 if (tid == 0) {
                     asm volatile("tcgen05.fence::after_thread_sync;\n");
@@ -711,28 +718,31 @@ __global__ void __launch_bounds__(32 * kInfWarps, 1) mlp_infer_kernel(const __gr
                 __syncwarp();
                 bool bad = !mbar_wait(smem_u32(&layer_done), (uint32_t)(layers_run & 1));
                 ++layers_run;
-                // one decision for all four warps (the producer may set failed
+                // one decision for all eight warps (the producer may set failed
                 // at any moment; the epilogue's tensor-memory loads are
-                // warp-collective and its barriers count all 128 threads)
-                stop = bar_or_128(bad || failed != 0);
+                // warp-collective and its barriers count all 256 threads)
+                stop = bar_or_256(bad || failed != 0);
                 if (stop) break;
                 asm volatile("tcgen05.fence::after_thread_sync;\n");
                 const bool last = l == kInfLayers - 1;
                 const int ncol = last ? n_mma : kInfHid;
-                for (int c0 = 0; c0 < ncol; c0 += 16) {
-                    uint32_t v[16];
-                    const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                        "[%16];\n"
-                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-                          "=r"(v[14]), "=r"(v[15])
-                        : "r"(addr));
+                for (int c0 = half * 32; c0 < ncol; c0 += 64) {
+                    uint32_t v[32];
+#pragma unroll
+                    for (int h = 0; h < 32; h += 16)
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                            "%15}, [%16];\n"
+                            : "=r"(v[h + 0]), "=r"(v[h + 1]), "=r"(v[h + 2]), "=r"(v[h + 3]), "=r"(v[h + 4]),
+                              "=r"(v[h + 5]), "=r"(v[h + 6]), "=r"(v[h + 7]), "=r"(v[h + 8]), "=r"(v[h + 9]),
+                              "=r"(v[h + 10]), "=r"(v[h + 11]), "=r"(v[h + 12]), "=r"(v[h + 13]), "=r"(v[h + 14]),
+                              "=r"(v[h + 15])
+                            : "r"(lane_base + (uint32_t)(c0 + h)));
                     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
                     if (last) {
                         if (q < Q)
-                            for (int j = 0; j < 16; j += 4) {
+#pragma unroll
+                            for (int j = 0; j < 32; j += 4) {
                                 const int n = c0 + j;
                                 if (n + 4 <= n_out) {
                                     *reinterpret_cast<float4 *>(O + (size_t)q * n_out + n) = make_float4(
@@ -745,27 +755,30 @@ __global__ void __launch_bounds__(32 * kInfWarps, 1) mlp_infer_kernel(const __gr
                                 }
                             }
                     } else {
-                        uint32_t pk[8];
+                        // bias, SiLU (z / (1 + e^-z) with the fast reciprocal), BF16
+                        uint32_t pk[16];
 #pragma unroll
-                        for (int j = 0; j < 16; j += 2) {
+                        for (int j = 0; j < 32; j += 2) {
                             const float z0 = __uint_as_float(v[j]) + bias[l][c0 + j];
                             const float z1 = __uint_as_float(v[j + 1]) + bias[l][c0 + j + 1];
-                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(z0 * sigmoidf_(z0), z1 * sigmoidf_(z1));
+                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(__fdividef(z0, 1.0f + __expf(-z0)),
+                                                                            __fdividef(z1, 1.0f + __expf(-z1)));
                             pk[j >> 1] = *reinterpret_cast<const uint32_t *>(&h2);
                         }
-                        // columns c0 .. c0+15: K slice c0 / 64, chunks (c0 % 64) / 8 and + 1
+                        // columns c0 .. c0+31: K slice c0 / 64, 16-byte chunks (c0 % 64) / 8 .. + 3
                         unsigned char *row = H + (c0 >> 6) * 16384 + r * 128;
                         const int ch = (c0 & 63) >> 3;
-                        *reinterpret_cast<uint4 *>(row + ((ch ^ (r & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                        *reinterpret_cast<uint4 *>(row + (((ch + 1) ^ (r & 7)) << 4)) =
-                            make_uint4(pk[4], pk[5], pk[6], pk[7]);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            *reinterpret_cast<uint4 *>(row + (((ch + i) ^ (r & 7)) << 4)) =
+                                make_uint4(pk[4 * i], pk[4 * i + 1], pk[4 * i + 2], pk[4 * i + 3]);
                     }
                 }
                 // the accumulator is read and the activations written before the
                 // next layer's MMAs start
                 asm volatile("tcgen05.fence::before_thread_sync;\n");
                 asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                asm volatile("bar.sync 1, 128;\n" ::: "memory");
+                asm volatile("bar.sync 1, 256;\n" ::: "memory");
             }
             if (stop) break;
         }
