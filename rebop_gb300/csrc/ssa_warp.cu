@@ -52,6 +52,10 @@ __host__ __device__ inline int warp_chunk(int R) { return (R + 31) / 32; }
 __host__ __device__ inline int warp_group(int C) { return C > 256 ? (C + 31) / 32 : 8; }
 __host__ __device__ inline int warp_ngroups(int C) { return (C + warp_group(C) - 1) / warp_group(C); }
 
+// Every reaction of order <= 2 over fewer than 32767 species: propensities
+// come from two-slot shapes (shape_word) and the factor list is not needed.
+__host__ __device__ inline bool warp_shape2(const SsaArgs &a) { return a.max_mults <= 2 && a.S < 32767; }
+
 // Shared memory: block tables (Exp1 tables, float-pair rates when shared,
 // reactant factors in both layouts, jumps), then per warp: counts,
 // float-pair propensities (and float-pair rates when per trajectory).  The
@@ -62,9 +66,9 @@ __host__ __device__ inline WarpLayout warp_layout(const SsaArgs &a) {
     size_t b = 16 * 256 + 8 * 257 + 8 * 256 + 8 * 256;  // zxk, zf, zd, xdf
     if (!a.batch) {  // a batch's networks stay in global memory
         b += 8 * RP;                                        // shared float-pair rates (lane-major)
-        b += 4 * RP * a.P;                                  // factors (lane-major)
+        if (!warp_shape2(a)) b += 4 * RP * a.P;             // factors (lane-major), when shapes do not cover
         b += 4 * RP;                                        // two-slot reaction shapes (lane-major)
-        b += 2 * (size_t)a.R * a.Q + 4 * (size_t)a.R * a.Q; // jumps: species (16 bit), deltas (32 bit)
+        b += 2 * (size_t)a.R * a.Q + 2 * (size_t)a.R * a.Q; // jumps: species, deltas (16 bit each)
         b += 16;                                            // alignment of the jump deltas
     }
     l.block_bytes = (b + 15) & ~(size_t)15;
@@ -240,11 +244,13 @@ __host__ __device__ inline uint32_t shape_word(const int32_t *fac_sp, const int3
 // counts at the interval start [S][32] and the generator there [4][32].
 // Returns the lane's event count; sets `late` if the wall-clock budget ran
 // out (the trajectory is then incomplete).
-template <bool MACRO>
+// MAXR bounds the item's reactions (4, 8 or 16): the per-reaction loops are
+// unrolled to it.
+template <bool MACRO, int MAXR>
 __device__ __noinline__ unsigned long long thread_unit(const SsaArgs &it, const ExactTables &zt, const float2 *xdf,
                                                        unsigned char *wreg, long long first, int64_t t_start,
                                                        bool &late) {
-    using Ops = TableOps<16, MACRO>;
+    using Ops = TableOps<MAXR, MACRO>;
     constexpr int NS = 32;  // column stride of the per-lane arrays
     const int lane = threadIdx.x & 31;
     const long long traj = first + lane;
@@ -302,7 +308,7 @@ __device__ __noinline__ unsigned long long thread_unit(const SsaArgs &it, const 
             const float2 X1 = xdf[i1];
             DF x = df_mul(df_u53(2 * k1 + 1), DF{X1.x, X1.y});
             float xerr = kGamma * X1.x;
-            float cum[16];
+            float cum[MAXR];
             DF tot;
             bool amb = Ops::props(it, ex, c, sp, NS, rf, 1, cum, tot);
             const bool slow = !(k1 < K1);
@@ -343,7 +349,7 @@ __device__ __noinline__ unsigned long long thread_unit(const SsaArgs &it, const 
             bool close = false;
             int idx = 0;
 #pragma unroll
-            for (int r = 0; r < 16; ++r) {
+            for (int r = 0; r < MAXR; ++r) {
                 if (r < R) {
                     const float dr = __fsub_rn(cum[r], ch);
                     idx += dr < 0.0f ? 1 : 0;
@@ -358,7 +364,7 @@ __device__ __noinline__ unsigned long long thread_unit(const SsaArgs &it, const 
         }
         if (replay) {
             // the interval again, exactly, from its saved start
-            ev = replay_interval<16, MACRO>(it, ex, sp, sps, gsv, rl, 1, NS, t0, T, nat, ev0, t_start);
+            ev = replay_interval<MAXR, MACRO>(it, ex, sp, sps, gsv, rl, 1, NS, t0, T, nat, ev0, t_start);
             if (ev == ~0ull) {
                 late = true;
                 return ev0;
@@ -389,12 +395,13 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
     float2 *xdf = reinterpret_cast<float2 *>(zd + 256);
     float2 *rdf_sh = xdf + 256;
     const int C0 = warp_chunk(a.R), RP0 = 32 * C0;
-    int32_t *facl_sh = reinterpret_cast<int32_t *>(rdf_sh + RP0);
-    uint32_t *shape_sh = reinterpret_cast<uint32_t *>(facl_sh + (size_t)RP0 * a.P);
+    const bool shape2 = warp_shape2(a);
+    int32_t *facl_sh = reinterpret_cast<int32_t *>(rdf_sh + RP0);  // absent (size 0) when shape2
+    uint32_t *shape_sh = reinterpret_cast<uint32_t *>(facl_sh + (shape2 ? 0 : (size_t)RP0 * a.P));
     // jumps of the one network: species as 16-bit indices (S < 65536), deltas
-    // as 32-bit values when every one fits (else read from the descriptor)
+    // as 16-bit values when every one fits (else read from the descriptor)
     uint16_t *jsp_sh = reinterpret_cast<uint16_t *>(shape_sh + RP0);
-    int32_t *jd_sh = reinterpret_cast<int32_t *>(
+    int16_t *jd_sh = reinterpret_cast<int16_t *>(
         (reinterpret_cast<uintptr_t>(jsp_sh + (size_t)a.R * a.Q) + 15) & ~(uintptr_t)15);
     for (int k = tid; k < 256; k += blockDim.x) {
         zxk[k] = make_ulonglong2((uint64_t)__double_as_longlong(a.zig[k]),
@@ -407,20 +414,22 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
         for (int k = tid; k < a.R * a.Q; k += blockDim.x) {
             const int64_t dlt = a.jmp_d[k];
             jsp_sh[k] = (uint16_t)a.jmp_sp[k];
-            jd_sh[k] = (int32_t)dlt;
-            jd_wide |= dlt != (int64_t)(int32_t)dlt;
+            jd_sh[k] = (int16_t)dlt;
+            jd_wide |= dlt != (int64_t)(int16_t)dlt;
         }
-        const bool shape2 = a.max_mults <= 2 && a.S < 32767;
         for (int q = tid; q < RP0; q += blockDim.x) {
             const int i = q >> 5, l = q & 31, r = l * C0 + i;
             if (!a.rate_stride) {
                 const DF d = r < a.R ? df_from_double(a.rate[r]) : DF{0.f, 0.f};
                 rdf_sh[q] = make_float2(d.h, d.l);
             }
-            for (int p = 0; p < a.P; ++p)
-                facl_sh[(i * a.P + p) * 32 + l] =
-                    r < a.R ? (a.fac_sp[r * a.P + p] | (a.fac_ord[r * a.P + p] << 16)) : 0;
-            if (shape2) shape_sh[q] = r < a.R ? shape_word(a.fac_sp, a.fac_ord, a.P, a.S, r) : (uint32_t)a.S << 16 | a.S;
+            if (shape2) {
+                shape_sh[q] = r < a.R ? shape_word(a.fac_sp, a.fac_ord, a.P, a.S, r) : (uint32_t)a.S << 16 | a.S;
+            } else {
+                for (int p = 0; p < a.P; ++p)
+                    facl_sh[(i * a.P + p) * 32 + l] =
+                        r < a.R ? (a.fac_sp[r * a.P + p] | (a.fac_ord[r * a.P + p] << 16)) : 0;
+            }
         }
     }
     for (int k = tid; k < 256; k += blockDim.x) {
@@ -462,8 +471,11 @@ __global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const _
                 else hi = mid - 1;
             }
             bool late = false;
-            unsigned long long ev =
-                thread_unit<MACRO>(a.tbatch[lo], ex, xdf, wbase, (u - a.tbatch_unit[lo]) * 32, t_start, late);
+            const SsaArgs &ti = a.tbatch[lo];
+            const long long first = (u - a.tbatch_unit[lo]) * 32;
+            unsigned long long ev = ti.R <= 4   ? thread_unit<MACRO, 4>(ti, ex, xdf, wbase, first, t_start, late)
+                                    : ti.R <= 8 ? thread_unit<MACRO, 8>(ti, ex, xdf, wbase, first, t_start, late)
+                                                : thread_unit<MACRO, 16>(ti, ex, xdf, wbase, first, t_start, late);
             for (int off = 16; off > 0; off >>= 1) ev += __shfl_xor_sync(0xffffffffu, ev, off);
             warp_events += ev;
             if (__any_sync(0xffffffffu, late)) {
