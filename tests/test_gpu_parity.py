@@ -535,6 +535,30 @@ def test_warp_kernel_exact_choice_path(rb, O):
     np.testing.assert_array_equal(res.events, ev)
 
 
+def test_warp_kernel_wide_jump_deltas(rb, O):
+    # A jump delta beyond 16 bits (a burst of 40 000 molecules) in a network the
+    # warp kernel runs: its block tables keep 16-bit deltas and read wider ones
+    # from the descriptor.
+    import bench
+
+    reactions, x0 = bench.random_network(74, 12, 40, x0_mean=50.0)
+    net, onet = rb.Network(12), O.OracleNet(12)
+    for k, e, d in reactions:
+        net.add_reaction(rb.Rate.lma(k, e), d)
+        onet.add_lma_sparse(k, [(i, x) for i, x in enumerate(e) if x], d)
+    burst = [0] * 12
+    burst[3] = 40_000
+    net.add_reaction(rb.Rate.lma(20.0, [0] * 12), burst)
+    onet.add_lma_sparse(20.0, [], burst)
+    seeds = _seeds(64, 74)
+    res = net.run_ensemble(x0, seeds, 1e-2, 8)
+    ref, ev, _, _ = onet.run_ensemble(x0, seeds, 1e-2, 8)
+    assert res.stats["mapping"] == 5
+    assert ref[:, 3].max() >= 40_000  # some trajectories took the burst
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
+
+
 def test_warp_kernel_matches_oracle(rb, O):
     # Warp per trajectory: a random network beyond the thread kernels (chosen
     # by the dispatcher), then small networks forced onto it.
