@@ -151,7 +151,7 @@ for _name, _args in {
     "rbg_mdn_sample": [_vp, C.c_int, C.c_int, _u64, _vp, C.c_int, _vp, _vp],
     "rbg_mdn_rre": [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp, _vp],
     "rbg_mdn_count_loss": [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp],
-    "rbg_mdn_count_sample": [_vp, C.c_int, C.c_int, _u64, _vp, C.c_int, _vp, _vp],
+    "rbg_mdn_count_sample": [_vp, C.c_int, C.c_int, _u64, _vp, C.c_int, _vp, _vp, _vp],
     "rbg_mdn_infer": [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int,
                       _vp, _vp, _vp],
 }.items():

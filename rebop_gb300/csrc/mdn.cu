@@ -1062,57 +1062,78 @@ __global__ void rre_kernel(const float *rates, const float *tq, int Q, int S, in
     for (int j = 0; j < n_out; ++j) out[(size_t)q * n_out + j] = x[out_idx[j]];
 }
 
-// Draws of the count-aware head: row r of out takes query r / per_query's
-// distributions and receives, per species, the class drawn from the logits
-// -- the count itself -- or for the tail class floor(exp(z + base)), at
-// least kNC - 1, z drawn from the tail mixture.  The two species are drawn
-// independently.
-__global__ void count_sample_kernel(const float *O, int B, int kKT, uint64_t seed, float *out, int per_query,
-                                    const float *base) {
+// Draws from the count-aware head, in two passes.  count_prep_kernel turns
+// each (query, species) head block into what the draws need: the running sums
+// of the class probabilities (softmax in the block's order, as the loss
+// computes it), the running sums of the tail weights, the tail means and the
+// tail scales softplus(s) + 1e-3.  count_draw_kernel then takes one draw per
+// thread: class c = the first class whose running sum exceeds u0 (a binary
+// search over the non-decreasing sums: #{k : cum_k <= u0}), a count below 31
+// returned as is; the tail class picks a component by the same rule on u1
+// and draws z = mu + sigma * N(0, 1) (Box-Muller on u2, u3), returning
+// max(floor(exp(z + b)), 31).  The uniforms come from a SplitMix64-style
+// hash of (seed, draw, species).  P has O's layout: per species 32 + 3 KT
+// floats.
+__global__ void count_prep_kernel(const float *O, int Q, int kKT, float *P) {
+    const int kHS = kNC + 3 * kKT;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * Q) return;
+    const float *o = O + (size_t)i * kHS;
+    float *p = P + (size_t)i * kHS;
+    float lmax = -1e30f;
+    for (int k = 0; k < kNC; ++k) lmax = fmaxf(lmax, o[k]);
+    float zs = 0.0f;
+    for (int k = 0; k < kNC; ++k) zs += __expf(o[k] - lmax);
+    float acc = 0.0f;
+    for (int k = 0; k < kNC; ++k) {
+        acc += __expf(o[k] - lmax) / zs;
+        p[k] = acc;
+    }
+    const float *tw = o + kNC, *tm = tw + kKT, *ts = tm + kKT;
+    float wmax = -1e30f;
+    for (int k = 0; k < kKT; ++k) wmax = fmaxf(wmax, tw[k]);
+    float ws = 0.0f;
+    for (int k = 0; k < kKT; ++k) ws += __expf(tw[k] - wmax);
+    acc = 0.0f;
+    for (int k = 0; k < kKT; ++k) {
+        acc += __expf(tw[k] - wmax) / ws;
+        p[kNC + k] = acc;
+        p[kNC + kKT + k] = tm[k];
+        p[kNC + 2 * kKT + k] = softplusf_(ts[k]) + 1e-3f;
+    }
+}
+
+// #{k < n : cum[k] <= u} for non-decreasing cum (binary search)
+__device__ __forceinline__ int count_le(const float *cum, int n, float u) {
+    int c = 0;
+    int step = 1;
+    while (step * 2 <= n) step *= 2;
+    for (; step > 0; step >>= 1)
+        if (c + step <= n && cum[c + step - 1] <= u) c += step;
+    return c;
+}
+
+__global__ void count_draw_kernel(const float *P, int B, int kKT, uint64_t seed, float *out, int per_query,
+                                  const float *base) {
     const int kHS = kNC + 3 * kKT;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= B) return;
     const int q = row / per_query;
     for (int sp = 0; sp < 2; ++sp) {
-        const float *o = O + (size_t)q * 2 * kHS + sp * kHS;
+        const float *p = P + (size_t)q * 2 * kHS + sp * kHS;
         uint64_t h = mix64(seed ^ mix64(((uint64_t)row << 1 | (uint64_t)sp) + 0x9E3779B97F4A7C15ull));
         const float u0 = (float)(h >> 40) * 0x1p-24f;
-        h = mix64(h);
-        const float u1 = (float)(h >> 40) * 0x1p-24f, u2 = ((float)((h >> 16) & 0xFFFFFF) + 0.5f) * 0x1p-24f;
-        h = mix64(h);
-        const float u3 = (float)(h >> 40) * 0x1p-24f;
-        float lmax = -1e30f;
-        for (int k = 0; k < kNC; ++k) lmax = fmaxf(lmax, o[k]);
-        float zs = 0.0f;
-        for (int k = 0; k < kNC; ++k) zs += __expf(o[k] - lmax);
-        int c = kNC - 1;
-        float acc = 0.0f;
-        for (int k = 0; k < kNC; ++k) {
-            acc += __expf(o[k] - lmax) / zs;
-            if (u0 < acc) {
-                c = k;
-                break;
-            }
-        }
+        const int c = min(count_le(p, kNC, u0), kNC - 1);
         if (c < kNC - 1) {
             out[2 * row + sp] = (float)c;
             continue;
         }
-        const float *tw = o + kNC, *tm = tw + kKT, *ts = tm + kKT;
-        float wmax = -1e30f;
-        for (int k = 0; k < kKT; ++k) wmax = fmaxf(wmax, tw[k]);
-        float ws = 0.0f;
-        for (int k = 0; k < kKT; ++k) ws += __expf(tw[k] - wmax);
-        int t = kKT - 1;
-        acc = 0.0f;
-        for (int k = 0; k < kKT; ++k) {
-            acc += __expf(tw[k] - wmax) / ws;
-            if (u1 < acc) {
-                t = k;
-                break;
-            }
-        }
-        const float z = tm[t] + (softplusf_(ts[t]) + 1e-3f) * sqrtf(-2.0f * logf(u2)) * cosf(6.2831853f * u3);
+        h = mix64(h);
+        const float u1 = (float)(h >> 40) * 0x1p-24f, u2 = ((float)((h >> 16) & 0xFFFFFF) + 0.5f) * 0x1p-24f;
+        h = mix64(h);
+        const float u3 = (float)(h >> 40) * 0x1p-24f;
+        const int t = min(count_le(p + kNC, kKT, u1), kKT - 1);
+        const float z = p[kNC + kKT + t] + p[kNC + 2 * kKT + t] * sqrtf(-2.0f * logf(u2)) * cosf(6.2831853f * u3);
         out[2 * row + sp] = fmaxf(floorf(expf(z + base[2 * q + sp])), (float)(kNC - 1));
     }
 }
@@ -1124,7 +1145,8 @@ __global__ void count_sample_kernel(const float *O, int B, int kKT, uint64_t see
 extern "C" {
 
 // Count-aware head: loss and gradient, and draws (see count_loss_kernel,
-// count_sample_kernel); device pointers.
+// count_prep_kernel, count_draw_kernel); device pointers; `work` holds the
+// prepared distributions, as many floats as O has for the queries drawn from.
 int rbg_mdn_count_loss(const float *O, const float *Y, int B, int KT, float *loss, float *G, void *stream) {
     if (KT < 1 || KT > rbg::kKTMax) return (int)cudaErrorInvalidValue;
     rbg::count_loss_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, Y, B, KT, loss, G);
@@ -1132,10 +1154,13 @@ int rbg_mdn_count_loss(const float *O, const float *Y, int B, int KT, float *los
 }
 
 int rbg_mdn_count_sample(const float *O, int B, int KT, uint64_t seed, float *out, int per_query, const float *base,
-                         void *stream) {
-    if (per_query < 1 || !base || KT < 1 || KT > rbg::kKTMax) return (int)cudaErrorInvalidValue;
-    rbg::count_sample_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(O, B, KT, seed, out,
-                                                                                            per_query, base);
+                         float *work, void *stream) {
+    if (per_query < 1 || !base || !work || KT < 1 || KT > rbg::kKTMax || B < 0) return (int)cudaErrorInvalidValue;
+    if (B == 0) return 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int Q = (B + per_query - 1) / per_query;
+    rbg::count_prep_kernel<<<(2 * Q + 127) / 128, 128, 0, st>>>(O, Q, KT, work);
+    rbg::count_draw_kernel<<<(B + 255) / 256, 256, 0, st>>>(work, B, KT, seed, out, per_query, base);
     return (int)cudaGetLastError();
 }
 

@@ -291,8 +291,9 @@ class MDN:
         base = F[:, N_QUERY:].contiguous()
         c = torch.empty(F.shape[0] * n_draws, 2, dtype=torch.float32, device=self.dev)
         if self.head == "count":
+            work = torch.empty_like(o)  # the prepared per-query distributions
             check(lib.rbg_mdn_count_sample(o.data_ptr(), c.shape[0], self.tail, int(seed), c.data_ptr(), int(n_draws),
-                                           base.data_ptr(), self._s()))
+                                           base.data_ptr(), work.data_ptr(), self._s()))
         else:
             check(lib.rbg_mdn_sample(o.data_ptr(), c.shape[0], K, int(seed), c.data_ptr(), int(n_draws),
                                      base.data_ptr(), self._s()))

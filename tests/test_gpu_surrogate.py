@@ -141,6 +141,56 @@ def test_fused_inference_matches_layer_by_layer(torch, head):
         assert d.max() <= 5e-3 * scale and d.mean() <= 1e-4 * scale, (Q, d.max(), d.mean(), scale)
 
 
+def _mix64(z):
+    # SplitMix64's output function (Steele, Lea and Flood 2014), as the sampler hashes
+    M = (1 << 64) - 1
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+    return z ^ (z >> 31)
+
+
+def test_count_sampler_follows_its_rule(torch):
+    # rbg_mdn_count_sample: the prepared running sums equal the softmax's, every
+    # below-tail draw is exactly #{k : cum_k <= u0} for its hashed uniform, and
+    # tail draws are >= 31.
+    from rebop_gb300._lib import check, lib
+    from rebop_gb300 import surrogate as sg
+
+    rng = np.random.default_rng(8)
+    Q, per, KT = 24, 200, sg.KT
+    HS = sg.NC + 3 * KT
+    O = rng.normal(0, 2, (Q, 2 * HS)).astype(np.float32)
+    O[:, sg.NC - 1] += 2.0  # a tail class that is drawn now and then
+    o = torch.tensor(O).cuda()
+    base = torch.tensor(rng.uniform(3, 5, (Q, 2)), dtype=torch.float32).cuda()
+    out = torch.empty(Q * per, 2, dtype=torch.float32, device="cuda")
+    work = torch.empty_like(o)
+    seed = 12345
+    check(lib.rbg_mdn_count_sample(o.data_ptr(), Q * per, KT, seed, out.data_ptr(), per, base.data_ptr(),
+                                   work.data_ptr(), torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    W = work.cpu().numpy().reshape(Q, 2, HS)
+    X = out.cpu().numpy()
+    for q in range(Q):
+        for sp in range(2):
+            lg = O[q, sp * HS:sp * HS + sg.NC].astype(np.float64)
+            pr = np.exp(lg - lg.max())
+            np.testing.assert_allclose(W[q, sp, :sg.NC], np.cumsum(pr / pr.sum()), atol=2e-6)
+    tails = 0
+    for row in range(0, Q * per, 7):
+        q = row // per
+        for sp in range(2):
+            h = _mix64(seed ^ _mix64(((row << 1 | sp) + 0x9E3779B97F4A7C15) & ((1 << 64) - 1)))
+            u0 = np.float32((h >> 40) * 2.0 ** -24)
+            c = min(int((W[q, sp, :sg.NC] <= u0).sum()), sg.NC - 1)
+            if c < sg.NC - 1:
+                assert X[row, sp] == c, (row, sp, X[row, sp], c)
+            else:
+                assert X[row, sp] >= sg.NC - 1
+                tails += 1
+    assert tails > 0
+
+
 def test_rate_equation_kernel_matches_scipy(torch):
     # rbg_mdn_rre (float32 RK4, the surrogate's deterministic part) against an
     # adaptive float64 solution of the same rate equations
