@@ -50,6 +50,25 @@ def dimer_network(rates=RATES0):
     return net
 
 
+_RRE_CONST: dict = {}
+
+
+def _rre_constants(device):
+    """The rate equations' constant tensors on `device`, made once: a copy from
+    pageable host memory waits for the stream, which would serialise every
+    query batch with the previous one's kernels."""
+    import torch
+
+    key = str(device)
+    if key not in _RRE_CONST:
+        _RRE_CONST[key] = (torch.tensor(RATES0, dtype=torch.float32, device=device),
+                           torch.tensor(EXPS, dtype=torch.int32, device=device),
+                           torch.tensor(DIFFS, dtype=torch.float32, device=device),
+                           torch.tensor(X0, dtype=torch.float32, device=device),
+                           torch.tensor([2, 3], dtype=torch.int32, device=device))
+    return _RRE_CONST[key]
+
+
 def rre_log_means(x):
     """b = log(x_RRE + 1) of (protein, dimer) at each query row of x [Q][6]
     (u, t) on the GPU: the reaction rate equations integrated from the initial
@@ -58,13 +77,10 @@ def rre_log_means(x):
 
     x = x.to("cuda", torch.float32).contiguous()
     Q = x.shape[0]
-    rates = (torch.tensor(RATES0, device="cuda") * torch.pow(10.0, x[:, :5])).contiguous()
+    r0, E, N, x0, idx = _rre_constants(x.device)
+    rates = (r0 * torch.pow(10.0, x[:, :5])).contiguous()
     t = x[:, 5].contiguous()
-    E = torch.tensor(EXPS, dtype=torch.int32, device="cuda")
-    N = torch.tensor(DIFFS, dtype=torch.float32, device="cuda")
-    x0 = torch.tensor(X0, dtype=torch.float32, device="cuda")
-    idx = torch.tensor([2, 3], dtype=torch.int32, device="cuda")
-    out = torch.empty(Q, 2, dtype=torch.float32, device="cuda")
+    out = torch.empty(Q, 2, dtype=torch.float32, device=x.device)
     check(lib.rbg_mdn_rre(rates.data_ptr(), t.data_ptr(), Q, 4, 5, E.data_ptr(), N.data_ptr(), x0.data_ptr(),
                           RRE_STEPS, idx.data_ptr(), 2, out.data_ptr(), torch.cuda.current_stream().cuda_stream))
     return torch.log1p(out)
