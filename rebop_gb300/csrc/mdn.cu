@@ -1062,6 +1062,69 @@ __global__ void rre_kernel(const float *rates, const float *tq, int Q, int S, in
     for (int j = 0; j < n_out; ++j) out[(size_t)q * n_out + j] = x[out_idx[j]];
 }
 
+// The same integration for a network of exactly S_ species and R_ reactions:
+// the loops over species and reactions unrolled, the exponents and changes in
+// registers -- the same operations in the same order, so the same results.
+template <int S_, int R_>
+__device__ __forceinline__ void rre_rhs_fixed(const int (&e)[R_][S_], const float (&nn)[R_][S_], const float (&k)[R_],
+                                              const float (&x)[S_], float (&dx)[S_]) {
+#pragma unroll
+    for (int s = 0; s < S_; ++s) dx[s] = 0.0f;
+#pragma unroll
+    for (int r = 0; r < R_; ++r) {
+        float a = k[r];
+#pragma unroll
+        for (int s = 0; s < S_; ++s) {
+            for (int j = 0; j < e[r][s]; ++j) a *= fmaxf(x[s] - (float)j, 0.0f);
+        }
+#pragma unroll
+        for (int s = 0; s < S_; ++s) dx[s] += nn[r][s] * a;
+    }
+}
+
+template <int S_, int R_>
+__global__ void rre_fixed_kernel(const float *rates, const float *tq, int Q, const int *E, const float *N,
+                                 const float *x0, int n_steps, const int *out_idx, int n_out, float *out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Q) return;
+    int e[R_][S_];
+    float nn[R_][S_], k[R_], x[S_], xt[S_], k1[S_], k2[S_], k3[S_], k4[S_];
+#pragma unroll
+    for (int r = 0; r < R_; ++r) {
+        k[r] = rates[(size_t)q * R_ + r];
+#pragma unroll
+        for (int s = 0; s < S_; ++s) {
+            e[r][s] = E[r * S_ + s];
+            nn[r][s] = N[r * S_ + s];
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < S_; ++s) x[s] = x0[s];
+    const float h = tq[q] / (float)n_steps;
+    for (int n = 0; n < n_steps; ++n) {
+        rre_rhs_fixed<S_, R_>(e, nn, k, x, k1);
+#pragma unroll
+        for (int s = 0; s < S_; ++s) xt[s] = x[s] + 0.5f * h * k1[s];
+        rre_rhs_fixed<S_, R_>(e, nn, k, xt, k2);
+#pragma unroll
+        for (int s = 0; s < S_; ++s) xt[s] = x[s] + 0.5f * h * k2[s];
+        rre_rhs_fixed<S_, R_>(e, nn, k, xt, k3);
+#pragma unroll
+        for (int s = 0; s < S_; ++s) xt[s] = x[s] + h * k3[s];
+        rre_rhs_fixed<S_, R_>(e, nn, k, xt, k4);
+#pragma unroll
+        for (int s = 0; s < S_; ++s)
+            x[s] = fmaxf(x[s] + h / 6.0f * (k1[s] + 2.0f * k2[s] + 2.0f * k3[s] + k4[s]), 0.0f);
+    }
+    for (int j = 0; j < n_out; ++j) {
+        float v = 0.0f;
+#pragma unroll
+        for (int s = 0; s < S_; ++s)
+            if (s == out_idx[j]) v = x[s];
+        out[(size_t)q * n_out + j] = v;
+    }
+}
+
 // Draws from the count-aware head, in two passes.  count_prep_kernel turns
 // each (query, species) head block into what the draws need: the running sums
 // of the class probabilities (softmax in the block's order, as the loss
@@ -1169,8 +1232,12 @@ int rbg_mdn_rre(const float *rates, const float *tq, int Q, int S, int R, const 
                 const float *x0, int n_steps, const int *out_idx, int n_out, float *out, void *stream) {
     if (S < 1 || S > rbg::kRreMaxS || R < 1 || R > rbg::kRreMaxR || n_steps < 1) return (int)cudaErrorInvalidValue;
     if (Q == 0) return 0;
-    rbg::rre_kernel<<<(Q + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(rates, tq, Q, S, R, E, N, x0,
-                                                                                   n_steps, out_idx, n_out, out);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (S == 4 && R == 5)  // the surrogate's dimer network
+        rbg::rre_fixed_kernel<4, 5><<<(Q + 127) / 128, 128, 0, st>>>(rates, tq, Q, E, N, x0, n_steps, out_idx,
+                                                                     n_out, out);
+    else
+        rbg::rre_kernel<<<(Q + 127) / 128, 128, 0, st>>>(rates, tq, Q, S, R, E, N, x0, n_steps, out_idx, n_out, out);
     return (int)cudaGetLastError();
 }
 

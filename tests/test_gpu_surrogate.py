@@ -141,6 +141,34 @@ def test_fused_inference_matches_layer_by_layer(torch, head):
         assert d.max() <= 5e-3 * scale and d.mean() <= 1e-4 * scale, (Q, d.max(), d.mean(), scale)
 
 
+def test_rate_equation_unrolled_kernel_equals_generic(torch):
+    # The dimer's rate equations run on a kernel unrolled for 4 species and 5
+    # reactions; the generic kernel on the same network with an idle fifth
+    # species (no exponent, no change) must give the same bits.
+    from rebop_gb300._lib import check, lib
+    from rebop_gb300 import surrogate as sg
+
+    rng = np.random.default_rng(9)
+    Q = 3000
+    rates = torch.tensor(np.asarray(sg.RATES0) * 10 ** rng.uniform(-1, 1, (Q, 5)), dtype=torch.float32).cuda()
+    t = torch.tensor(rng.uniform(0.01, 1, Q), dtype=torch.float32).cuda()
+    outs = []
+    for S in (4, 5):
+        E = np.zeros((5, S), np.int32)
+        N = np.zeros((5, S), np.float32)
+        E[:, :4], N[:, :4] = sg.EXPS, sg.DIFFS
+        x0 = np.zeros(S, np.float32)
+        x0[:4] = sg.X0
+        Ed, Nd, x0d = (torch.tensor(v).cuda() for v in (E, N, x0))
+        idx = torch.tensor([2, 3], dtype=torch.int32).cuda()
+        out = torch.empty(Q, 2, dtype=torch.float32, device="cuda")
+        check(lib.rbg_mdn_rre(rates.data_ptr(), t.data_ptr(), Q, S, 5, Ed.data_ptr(), Nd.data_ptr(), x0d.data_ptr(),
+                              sg.RRE_STEPS, idx.data_ptr(), 2, out.data_ptr(),
+                              torch.cuda.current_stream().cuda_stream))
+        outs.append(out.cpu().numpy())
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
 def _mix64(z):
     # SplitMix64's output function (Steele, Lea and Flood 2014), as the sampler hashes
     M = (1 << 64) - 1
