@@ -37,6 +37,8 @@ namespace rbg {
 namespace {
 
 constexpr int kWarpMaxWarps = 16;
+// batch launches: small per-warp regions, so registers set the warps per SM
+constexpr int kWarpMaxWarpsBatch = 20;
 
 struct WarpLayout {
     size_t block_bytes, warp_bytes;
@@ -383,7 +385,8 @@ __device__ __noinline__ unsigned long long thread_unit(const SsaArgs &it, const 
 // memory, lane-major) and a.tbatch's thread units; otherwise the one network
 // of `a`, whose tables the block copies to shared memory.
 template <bool MACRO, bool BATCH>
-__global__ void __launch_bounds__(32 * kWarpMaxWarps, 1) ssa_warp_kernel(const __grid_constant__ SsaArgs a) {
+__global__ void __launch_bounds__(32 * (BATCH ? kWarpMaxWarpsBatch : kWarpMaxWarps), 1)
+    ssa_warp_kernel(const __grid_constant__ SsaArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
     const WarpLayout L = warp_layout(a);  // sized for the largest network of the launch
 
@@ -877,7 +880,7 @@ int warp_launch(const SsaArgs &a, int block, int grid, size_t smem, cudaStream_t
 int ssa_warp_warps(const SsaArgs &a, size_t smem_limit) {
     const WarpLayout l = warp_layout(a);
     if (l.block_bytes + l.warp_bytes > smem_limit) return 0;
-    return (int)std::min<size_t>(kWarpMaxWarps, (smem_limit - l.block_bytes) / l.warp_bytes);
+    return (int)std::min<size_t>(a.batch ? kWarpMaxWarpsBatch : kWarpMaxWarps, (smem_limit - l.block_bytes) / l.warp_bytes);
 }
 
 size_t ssa_warp_smem(const SsaArgs &a, int warps) {
@@ -891,9 +894,11 @@ bool ssa_warp_supported(const SsaArgs &a, int max_order) {
 
 int ssa_warp_occupancy(const SsaArgs &a, int warps, size_t smem) {
     int n = 0;
-    // all instances share the block shape and shared memory use
-    cudaFuncSetAttribute(ssa_warp_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_warp_kernel<false, false>, 32 * warps, smem);
+    // the arithmetic variants share the block shape and shared memory use;
+    // batch launches have their own register budget
+    const auto k = a.batch ? ssa_warp_kernel<false, true> : ssa_warp_kernel<false, false>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 32 * warps, smem);
     return n;
 }
 
