@@ -744,12 +744,12 @@ def measure_surrogate(args) -> dict:
     q = np.concatenate([rng.uniform(-1, 1, (w["n_queries"], 5)), rng.integers(1, 101, (w["n_queries"], 1)) / 100],
                        axis=1).astype(np.float32)
     Q = torch.from_numpy(q).cuda()
-    chunk = 8192
-    for s in range(0, 3 * chunk, chunk):  # warm-up
+    chunk = 65536  # queries per call (1000 draws each: 524 MB of draws)
+    for s in range(0, 2 * chunk, chunk):  # warm-up
         model.sample_counts(Q[s:s + chunk], w["draws"])
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    n_q = 131072
+    n_q = 262144
     e0.record()
     for s in range(0, n_q, chunk):
         model.sample_counts(Q[s:s + chunk], w["draws"])

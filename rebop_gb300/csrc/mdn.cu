@@ -1075,7 +1075,10 @@ __device__ __forceinline__ void rre_rhs_fixed(const int (&e)[R_][S_], const floa
         float a = k[r];
 #pragma unroll
         for (int s = 0; s < S_; ++s) {
-            for (int j = 0; j < e[r][s]; ++j) a *= fmaxf(x[s] - (float)j, 0.0f);
+            // the generic loop's factors, the first two without a loop
+            if (e[r][s] > 0) a *= fmaxf(x[s] - 0.0f, 0.0f);
+            if (e[r][s] > 1) a *= fmaxf(x[s] - 1.0f, 0.0f);
+            for (int j = 2; j < e[r][s]; ++j) a *= fmaxf(x[s] - (float)j, 0.0f);
         }
 #pragma unroll
         for (int s = 0; s < S_; ++s) dx[s] += nn[r][s] * a;
@@ -1101,20 +1104,21 @@ __global__ void rre_fixed_kernel(const float *rates, const float *tq, int Q, con
 #pragma unroll
     for (int s = 0; s < S_; ++s) x[s] = x0[s];
     const float h = tq[q] / (float)n_steps;
+    const float h2 = 0.5f * h, h6 = h / 6.0f;  // the generic kernel's (0.5f * h) and (h / 6.0f)
     for (int n = 0; n < n_steps; ++n) {
         rre_rhs_fixed<S_, R_>(e, nn, k, x, k1);
 #pragma unroll
-        for (int s = 0; s < S_; ++s) xt[s] = x[s] + 0.5f * h * k1[s];
+        for (int s = 0; s < S_; ++s) xt[s] = x[s] + h2 * k1[s];
         rre_rhs_fixed<S_, R_>(e, nn, k, xt, k2);
 #pragma unroll
-        for (int s = 0; s < S_; ++s) xt[s] = x[s] + 0.5f * h * k2[s];
+        for (int s = 0; s < S_; ++s) xt[s] = x[s] + h2 * k2[s];
         rre_rhs_fixed<S_, R_>(e, nn, k, xt, k3);
 #pragma unroll
         for (int s = 0; s < S_; ++s) xt[s] = x[s] + h * k3[s];
         rre_rhs_fixed<S_, R_>(e, nn, k, xt, k4);
 #pragma unroll
         for (int s = 0; s < S_; ++s)
-            x[s] = fmaxf(x[s] + h / 6.0f * (k1[s] + 2.0f * k2[s] + 2.0f * k3[s] + k4[s]), 0.0f);
+            x[s] = fmaxf(x[s] + h6 * (k1[s] + 2.0f * k2[s] + 2.0f * k3[s] + k4[s]), 0.0f);
     }
     for (int j = 0; j < n_out; ++j) {
         float v = 0.0f;
@@ -1166,8 +1170,18 @@ __global__ void count_prep_kernel(const float *O, int Q, int kKT, float *P) {
     }
 }
 
-// #{k < n : cum[k] <= u} for non-decreasing cum (binary search)
-__device__ __forceinline__ int count_le(const float *cum, int n, float u) {
+// #{k < N : cum[k] <= u} for non-decreasing cum (binary search, N a power of 2)
+template <int N>
+__device__ __forceinline__ int count_le(const float *cum, float u) {
+    int c = 0;
+#pragma unroll
+    for (int step = N / 2; step > 0; step >>= 1)
+        if (cum[c + step - 1] <= u) c += step;
+    return c + (cum[c] <= u ? 1 : 0);
+}
+
+// #{k < n : cum[k] <= u} for any n (binary search)
+__device__ __forceinline__ int count_le_n(const float *cum, int n, float u) {
     int c = 0;
     int step = 1;
     while (step * 2 <= n) step *= 2;
@@ -1176,17 +1190,23 @@ __device__ __forceinline__ int count_le(const float *cum, int n, float u) {
     return c;
 }
 
-__global__ void count_draw_kernel(const float *P, int B, int kKT, uint64_t seed, float *out, int per_query,
+// grid: x over the queries, y over the draws of one query; KT_ the tail
+// components when a power of two (the search unrolled), else 0 (kt at run time)
+template <int KT_>
+__global__ void count_draw_kernel(const float *P, int Q, int kt, uint64_t seed, float *out, int per_query,
                                   const float *base) {
-    const int kHS = kNC + 3 * kKT;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= B) return;
-    const int q = row / per_query;
+    const int KT = KT_ > 0 ? KT_ : kt;
+    const int kHS = kNC + 3 * KT;
+    const int q = blockIdx.x;
+    const int d = blockIdx.y * blockDim.x + threadIdx.x;
+    if (d >= per_query || q >= Q) return;
+    const long long row = (long long)q * per_query + d;
+#pragma unroll
     for (int sp = 0; sp < 2; ++sp) {
         const float *p = P + (size_t)q * 2 * kHS + sp * kHS;
         uint64_t h = mix64(seed ^ mix64(((uint64_t)row << 1 | (uint64_t)sp) + 0x9E3779B97F4A7C15ull));
         const float u0 = (float)(h >> 40) * 0x1p-24f;
-        const int c = min(count_le(p, kNC, u0), kNC - 1);
+        const int c = min(count_le<kNC>(p, u0), kNC - 1);
         if (c < kNC - 1) {
             out[2 * row + sp] = (float)c;
             continue;
@@ -1195,8 +1215,8 @@ __global__ void count_draw_kernel(const float *P, int B, int kKT, uint64_t seed,
         const float u1 = (float)(h >> 40) * 0x1p-24f, u2 = ((float)((h >> 16) & 0xFFFFFF) + 0.5f) * 0x1p-24f;
         h = mix64(h);
         const float u3 = (float)(h >> 40) * 0x1p-24f;
-        const int t = min(count_le(p + kNC, kKT, u1), kKT - 1);
-        const float z = p[kNC + kKT + t] + p[kNC + 2 * kKT + t] * sqrtf(-2.0f * logf(u2)) * cosf(6.2831853f * u3);
+        const int t = min(KT_ > 0 ? count_le<(KT_ > 0 ? KT_ : 1)>(p + kNC, u1) : count_le_n(p + kNC, KT, u1), KT - 1);
+        const float z = p[kNC + KT + t] + p[kNC + 2 * KT + t] * sqrtf(-2.0f * logf(u2)) * cosf(6.2831853f * u3);
         out[2 * row + sp] = fmaxf(floorf(expf(z + base[2 * q + sp])), (float)(kNC - 1));
     }
 }
@@ -1221,9 +1241,16 @@ int rbg_mdn_count_sample(const float *O, int B, int KT, uint64_t seed, float *ou
     if (per_query < 1 || !base || !work || KT < 1 || KT > rbg::kKTMax || B < 0) return (int)cudaErrorInvalidValue;
     if (B == 0) return 0;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int Q = (B + per_query - 1) / per_query;
+    const int Q = B / per_query;
+    if (B % per_query != 0 || (per_query + 255) / 256 > 65535) return (int)cudaErrorInvalidValue;
     rbg::count_prep_kernel<<<(2 * Q + 127) / 128, 128, 0, st>>>(O, Q, KT, work);
-    rbg::count_draw_kernel<<<(B + 255) / 256, 256, 0, st>>>(work, B, KT, seed, out, per_query, base);
+    const dim3 grid(Q, (per_query + 255) / 256);
+    switch (KT) {
+    case 4: rbg::count_draw_kernel<4><<<grid, 256, 0, st>>>(work, Q, KT, seed, out, per_query, base); break;
+    case 8: rbg::count_draw_kernel<8><<<grid, 256, 0, st>>>(work, Q, KT, seed, out, per_query, base); break;
+    case 16: rbg::count_draw_kernel<16><<<grid, 256, 0, st>>>(work, Q, KT, seed, out, per_query, base); break;
+    default: rbg::count_draw_kernel<0><<<grid, 256, 0, st>>>(work, Q, KT, seed, out, per_query, base);
+    }
     return (int)cudaGetLastError();
 }
 
