@@ -1062,24 +1062,33 @@ __global__ void rre_kernel(const float *rates, const float *tq, int Q, int S, in
     for (int j = 0; j < n_out; ++j) out[(size_t)q * n_out + j] = x[out_idx[j]];
 }
 
-// The same integration for a network of exactly S_ species and R_ reactions:
-// the loops over species and reactions unrolled, the exponents and changes in
-// registers -- the same operations in the same order, so the same results.
+// The same integration for a network of exactly S_ species and R_ reactions
+// whose propensities have at most two factors each (mass action of order
+// <= 2): reaction r's factors are the slots (species, offset) in the generic
+// loop's order -- species ascending, offsets 0 then 1 -- so a = k * f1 * f2
+// with f = max(x[species] - offset, 0) (an unused slot multiplies by 1) is
+// the generic product, factor for factor; the changes are applied to every
+// species as there.  Same operations in the same order, same results.  A
+// network outside that form takes the generic loops.
+template <int S_>
+__device__ __forceinline__ float rre_pick(const float (&x)[S_], int s) {
+    float v = 1.0f;  // s == S_: the constant factor of an unused slot
+#pragma unroll
+    for (int i = 0; i < S_; ++i) v = s == i ? x[i] : v;
+    return v;
+}
+
 template <int S_, int R_>
-__device__ __forceinline__ void rre_rhs_fixed(const int (&e)[R_][S_], const float (&nn)[R_][S_], const float (&k)[R_],
+__device__ __forceinline__ void rre_rhs_fixed(const int (&s1)[R_], const float (&o1)[R_], const int (&s2)[R_],
+                                              const float (&o2)[R_], const float (&nn)[R_][S_], const float (&k)[R_],
                                               const float (&x)[S_], float (&dx)[S_]) {
 #pragma unroll
     for (int s = 0; s < S_; ++s) dx[s] = 0.0f;
 #pragma unroll
     for (int r = 0; r < R_; ++r) {
         float a = k[r];
-#pragma unroll
-        for (int s = 0; s < S_; ++s) {
-            // the generic loop's factors, the first two without a loop
-            if (e[r][s] > 0) a *= fmaxf(x[s] - 0.0f, 0.0f);
-            if (e[r][s] > 1) a *= fmaxf(x[s] - 1.0f, 0.0f);
-            for (int j = 2; j < e[r][s]; ++j) a *= fmaxf(x[s] - (float)j, 0.0f);
-        }
+        if (s1[r] < S_) a *= fmaxf(rre_pick<S_>(x, s1[r]) - o1[r], 0.0f);
+        if (s2[r] < S_) a *= fmaxf(rre_pick<S_>(x, s2[r]) - o2[r], 0.0f);
 #pragma unroll
         for (int s = 0; s < S_; ++s) dx[s] += nn[r][s] * a;
     }
@@ -1090,32 +1099,65 @@ __global__ void rre_fixed_kernel(const float *rates, const float *tq, int Q, con
                                  const float *x0, int n_steps, const int *out_idx, int n_out, float *out) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= Q) return;
-    int e[R_][S_];
-    float nn[R_][S_], k[R_], x[S_], xt[S_], k1[S_], k2[S_], k3[S_], k4[S_];
+    int s1[R_], s2[R_];
+    float o1[R_], o2[R_], nn[R_][S_], k[R_], x[S_], xt[S_], k1[S_], k2[S_], k3[S_], k4[S_];
+    bool two = true;  // every reaction of order <= 2
 #pragma unroll
     for (int r = 0; r < R_; ++r) {
         k[r] = rates[(size_t)q * R_ + r];
+        s1[r] = s2[r] = S_;
+        o1[r] = o2[r] = 0.0f;
+        int n_f = 0;
 #pragma unroll
         for (int s = 0; s < S_; ++s) {
-            e[r][s] = E[r * S_ + s];
             nn[r][s] = N[r * S_ + s];
+            const int e = E[r * S_ + s];
+            for (int j = 0; j < e; ++j, ++n_f) {
+                if (n_f == 0) {
+                    s1[r] = s;
+                    o1[r] = (float)j;
+                } else if (n_f == 1) {
+                    s2[r] = s;
+                    o2[r] = (float)j;
+                }
+            }
         }
+        two = two && n_f <= 2;
+    }
+    if (!two) {  // higher orders: the generic loops
+        float kk[kRreMaxR], xg[kRreMaxS], xtg[kRreMaxS], g1[kRreMaxS], g2[kRreMaxS], g3[kRreMaxS], g4[kRreMaxS];
+        for (int r = 0; r < R_; ++r) kk[r] = k[r];
+        for (int s = 0; s < S_; ++s) xg[s] = x0[s];
+        const float h = tq[q] / (float)n_steps;
+        for (int n = 0; n < n_steps; ++n) {
+            rre_rhs(E, N, kk, S_, R_, xg, g1);
+            for (int s = 0; s < S_; ++s) xtg[s] = xg[s] + 0.5f * h * g1[s];
+            rre_rhs(E, N, kk, S_, R_, xtg, g2);
+            for (int s = 0; s < S_; ++s) xtg[s] = xg[s] + 0.5f * h * g2[s];
+            rre_rhs(E, N, kk, S_, R_, xtg, g3);
+            for (int s = 0; s < S_; ++s) xtg[s] = xg[s] + h * g3[s];
+            rre_rhs(E, N, kk, S_, R_, xtg, g4);
+            for (int s = 0; s < S_; ++s)
+                xg[s] = fmaxf(xg[s] + h / 6.0f * (g1[s] + 2.0f * g2[s] + 2.0f * g3[s] + g4[s]), 0.0f);
+        }
+        for (int j = 0; j < n_out; ++j) out[(size_t)q * n_out + j] = xg[out_idx[j]];
+        return;
     }
 #pragma unroll
     for (int s = 0; s < S_; ++s) x[s] = x0[s];
     const float h = tq[q] / (float)n_steps;
     const float h2 = 0.5f * h, h6 = h / 6.0f;  // the generic kernel's (0.5f * h) and (h / 6.0f)
     for (int n = 0; n < n_steps; ++n) {
-        rre_rhs_fixed<S_, R_>(e, nn, k, x, k1);
+        rre_rhs_fixed<S_, R_>(s1, o1, s2, o2, nn, k, x, k1);
 #pragma unroll
         for (int s = 0; s < S_; ++s) xt[s] = x[s] + h2 * k1[s];
-        rre_rhs_fixed<S_, R_>(e, nn, k, xt, k2);
+        rre_rhs_fixed<S_, R_>(s1, o1, s2, o2, nn, k, xt, k2);
 #pragma unroll
         for (int s = 0; s < S_; ++s) xt[s] = x[s] + h2 * k2[s];
-        rre_rhs_fixed<S_, R_>(e, nn, k, xt, k3);
+        rre_rhs_fixed<S_, R_>(s1, o1, s2, o2, nn, k, xt, k3);
 #pragma unroll
         for (int s = 0; s < S_; ++s) xt[s] = x[s] + h * k3[s];
-        rre_rhs_fixed<S_, R_>(e, nn, k, xt, k4);
+        rre_rhs_fixed<S_, R_>(s1, o1, s2, o2, nn, k, xt, k4);
 #pragma unroll
         for (int s = 0; s < S_; ++s)
             x[s] = fmaxf(x[s] + h6 * (k1[s] + 2.0f * k2[s] + 2.0f * k3[s] + k4[s]), 0.0f);
