@@ -1232,34 +1232,45 @@ __device__ __forceinline__ int count_le_n(const float *cum, int n, float u) {
     return c;
 }
 
-// grid: x over the queries, y over the draws of one query; KT_ the tail
-// components when a power of two (the search unrolled), else 0 (kt at run time)
+// Persistent grid: a block takes query after query, copies its prepared
+// distributions (both species) to shared memory and its threads take the
+// query's draws; KT_ is the tail size when a power of two (the search
+// unrolled), else 0 (kt at run time).
 template <int KT_>
-__global__ void count_draw_kernel(const float *P, int Q, int kt, uint64_t seed, float *out, int per_query,
-                                  const float *base) {
+__global__ void __launch_bounds__(256) count_draw_kernel(const float *P, int Q, int kt, uint64_t seed, float *out,
+                                                         int per_query, const float *base) {
+    __shared__ float tab[2 * (kNC + 3 * kKTMax)];
     const int KT = KT_ > 0 ? KT_ : kt;
     const int kHS = kNC + 3 * KT;
-    const int q = blockIdx.x;
-    const int d = blockIdx.y * blockDim.x + threadIdx.x;
-    if (d >= per_query || q >= Q) return;
-    const long long row = (long long)q * per_query + d;
+    for (int q = blockIdx.x; q < Q; q += gridDim.x) {
+        __syncthreads();  // every thread is done with the previous query's table
+        for (int i = threadIdx.x; i < 2 * kHS; i += blockDim.x) tab[i] = P[(size_t)q * 2 * kHS + i];
+        __syncthreads();
+        const float b0 = base[2 * q], b1 = base[2 * q + 1];
+        for (int d = threadIdx.x; d < per_query; d += blockDim.x) {
+            const long long row = (long long)q * per_query + d;
+            float v[2];
 #pragma unroll
-    for (int sp = 0; sp < 2; ++sp) {
-        const float *p = P + (size_t)q * 2 * kHS + sp * kHS;
-        uint64_t h = mix64(seed ^ mix64(((uint64_t)row << 1 | (uint64_t)sp) + 0x9E3779B97F4A7C15ull));
-        const float u0 = (float)(h >> 40) * 0x1p-24f;
-        const int c = min(count_le<kNC>(p, u0), kNC - 1);
-        if (c < kNC - 1) {
-            out[2 * row + sp] = (float)c;
-            continue;
+            for (int sp = 0; sp < 2; ++sp) {
+                const float *p = tab + sp * kHS;
+                uint64_t h = mix64(seed ^ mix64(((uint64_t)row << 1 | (uint64_t)sp) + 0x9E3779B97F4A7C15ull));
+                const float u0 = (float)(h >> 40) * 0x1p-24f;
+                const int c = min(count_le<kNC>(p, u0), kNC - 1);
+                if (c < kNC - 1) {
+                    v[sp] = (float)c;
+                    continue;
+                }
+                h = mix64(h);
+                const float u1 = (float)(h >> 40) * 0x1p-24f, u2 = ((float)((h >> 16) & 0xFFFFFF) + 0.5f) * 0x1p-24f;
+                h = mix64(h);
+                const float u3 = (float)(h >> 40) * 0x1p-24f;
+                const int t =
+                    min(KT_ > 0 ? count_le<(KT_ > 0 ? KT_ : 1)>(p + kNC, u1) : count_le_n(p + kNC, KT, u1), KT - 1);
+                const float z = p[kNC + KT + t] + p[kNC + 2 * KT + t] * sqrtf(-2.0f * logf(u2)) * cosf(6.2831853f * u3);
+                v[sp] = fmaxf(floorf(expf(z + (sp ? b1 : b0))), (float)(kNC - 1));
+            }
+            *reinterpret_cast<float2 *>(out + 2 * row) = make_float2(v[0], v[1]);
         }
-        h = mix64(h);
-        const float u1 = (float)(h >> 40) * 0x1p-24f, u2 = ((float)((h >> 16) & 0xFFFFFF) + 0.5f) * 0x1p-24f;
-        h = mix64(h);
-        const float u3 = (float)(h >> 40) * 0x1p-24f;
-        const int t = min(KT_ > 0 ? count_le<(KT_ > 0 ? KT_ : 1)>(p + kNC, u1) : count_le_n(p + kNC, KT, u1), KT - 1);
-        const float z = p[kNC + KT + t] + p[kNC + 2 * KT + t] * sqrtf(-2.0f * logf(u2)) * cosf(6.2831853f * u3);
-        out[2 * row + sp] = fmaxf(floorf(expf(z + base[2 * q + sp])), (float)(kNC - 1));
     }
 }
 
@@ -1284,9 +1295,12 @@ int rbg_mdn_count_sample(const float *O, int B, int KT, uint64_t seed, float *ou
     if (B == 0) return 0;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int Q = B / per_query;
-    if (B % per_query != 0 || (per_query + 255) / 256 > 65535) return (int)cudaErrorInvalidValue;
+    if (B % per_query != 0 || (reinterpret_cast<uintptr_t>(out) & 7) != 0) return (int)cudaErrorInvalidValue;
     rbg::count_prep_kernel<<<(2 * Q + 127) / 128, 128, 0, st>>>(O, Q, KT, work);
-    const dim3 grid(Q, (per_query + 255) / 256);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = std::max(1, std::min(Q, 8 * std::max(sms, 1)));
     switch (KT) {
     case 4: rbg::count_draw_kernel<4><<<grid, 256, 0, st>>>(work, Q, KT, seed, out, per_query, base); break;
     case 8: rbg::count_draw_kernel<8><<<grid, 256, 0, st>>>(work, Q, KT, seed, out, per_query, base); break;
