@@ -583,6 +583,10 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
     bool live = slot >= 0, have = false, nat = false, exact_traj = false, begin = false, abort_run = false;
 
     for (;;) {
+        // rows this lane's slot recorded in the phase, counted after it by the
+        // whole warp: rows [cnt_pw & 0xFFFF, cnt_pw >> 16) of its trajectory,
+        // and for a trajectory that ended, rows [cnt_fw - 1, n_samples)
+        uint32_t cnt_pw = 0, cnt_fw = 0;
         // ---------------------------------------------------------- phase
         if (slot >= 0) {
             int64_t *const sp = spa + slot;
@@ -810,12 +814,10 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
             // ---- the wall-clock budget, once per phase (a phase is at most
             // phase_steps steps, and an interval re-run checks it itself)
             if (global_ns() - t_start > a.budget_ns) abort_run = true;
-            // ---- count the rows recorded in this phase (one fence per lane)
-            if (a.row_done && (spend[slot] | sfin[slot])) {
-                const uint32_t pw = spend[slot], fw = sfin[slot];
-                __threadfence();
-                if (fw) count_rows_nofence(a, fw - 1u, (uint32_t)a.n_samples);
-                if (pw) count_rows_nofence(a, pw & 0xFFFFu, pw >> 16);
+            // ---- the rows recorded in this phase, counted below by the warp
+            if (a.row_done) {
+                cnt_pw = spend[slot];
+                cnt_fw = sfin[slot];
                 spend[slot] = 0;
                 sfin[slot] = 0;
             }
@@ -840,6 +842,21 @@ __device__ __forceinline__ void spec_body(const SsaArgs &a) {
             if (abort_run) ctr[1] = 1;
         }
         __syncwarp();
+        // ---- count the phase's rows: one fence per lane (its sample stores
+        // visible device-wide before any count), then per row one atomic add
+        // of the number of the warp's lanes that completed it
+        if (a.row_done && __any_sync(0xffffffffu, (cnt_pw | cnt_fw) != 0)) {
+            __threadfence();
+            const uint32_t plo = cnt_pw ? (cnt_pw & 0xFFFFu) : 0xFFFFFFFFu, phi = cnt_pw ? (cnt_pw >> 16) : 0u;
+            const uint32_t flo = cnt_fw ? cnt_fw - 1u : 0xFFFFFFFFu, fhi = cnt_fw ? (uint32_t)a.n_samples : 0u;
+            const uint32_t rlo = __reduce_min_sync(0xffffffffu, min(plo, flo));
+            const uint32_t rhi = __reduce_max_sync(0xffffffffu, max(phi, fhi));
+            for (uint32_t r = rlo; r < rhi; ++r) {
+                const uint32_t n = __reduce_add_sync(0xffffffffu, (uint32_t)(r >= plo && r < phi) +
+                                                                      (uint32_t)(r >= flo && r < fhi));
+                if (lane == 0 && n) atomicAdd(a.row_done + r, n);
+            }
+        }
         // ---------------------------------------------------------- compaction
         // Each warp owns slots [wbase, wbase + SPW) and never waits for
         // another warp: its live slots, in slot order, go to its list, so the
