@@ -26,6 +26,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 namespace rbg {
 
@@ -1342,6 +1344,24 @@ int rbg_mdn_gemm(const void *A, int lda, int ta, const void *B, int ldb, int tb,
 
 namespace {
 
+constexpr int kMaxDevices = 64;
+
+// Dynamic shared memory above 48 KB for `kern`, asked once per (kernel, device):
+// the attribute belongs to the current device's context.
+cudaError_t opt_in_smem(const void *kern, size_t bytes) {
+    static std::mutex mu;
+    static std::vector<std::pair<const void *, int>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    for (const auto &d : done)
+        if (d.first == kern && d.second == dev) return cudaSuccess;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) done.emplace_back(kern, dev);
+    return e;
+}
+
 // The TMA-fed kernel takes C = A B^T with both operands K-contiguous, rows
 // 16-byte multiples apart from a 16-byte aligned base (what a tensor map can
 // address) and K >= 8; RB_GEMM_TMA=0 sends every product to the staged kernel.
@@ -1382,8 +1402,7 @@ int gemm_tma(const void *A, int lda, const void *B, int ldb, float *C, int ldc, 
     using namespace rbg;
     CUtensorMap ma, mb;
     if (!encode_rows(ma, A, M, K, lda, kTmM) || !encode_rows(mb, B, N, K, ldb, kTmN)) return -1;
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmSmem);
+    const cudaError_t attr = opt_in_smem(reinterpret_cast<const void *>(gemm_tma_kernel), kTmSmem);
     if (attr != cudaSuccess) return (int)attr;
     const dim3 grid((N + kTmN - 1) / kTmN, (M + kTmM - 1) / kTmM);
     gemm_tma_kernel<<<grid, 128, kTmSmem, st>>>(ma, mb, C, ldc, M, N, K, beta, err);
@@ -1395,8 +1414,9 @@ int gemm_tma(const void *A, int lda, const void *B, int ldb, float *C, int ldc, 
 // The same product on tcgen05 (see gemm_tc05_kernel); *err (device int) is set
 // if a completion wait ran out.  K is split over gridDim.z when the product
 // has fewer than 64 tiles and K >= 1024; the splits' partial tiles go to a
-// workspace owned by this function (grown on demand, released at exit), so
-// split products on different streams must not overlap.
+// workspace this function keeps per device (grown on demand, released at
+// exit), so split products on different streams of one device must not
+// overlap.
 int rbg_mdn_gemm_tc05(const void *A, int lda, int ta, const void *B, int ldb, int tb, float *C, int ldc, int M,
                       int N, int K, float beta, int *err, void *stream) {
     using namespace rbg;
@@ -1418,35 +1438,36 @@ int rbg_mdn_gemm_tc05(const void *A, int lda, int ta, const void *B, int ldb, in
                 : ta     ? gemm_tc05_kernel<true, false>
                 : tb     ? gemm_tc05_kernel<false, true>
                          : gemm_tc05_kernel<false, false>;
-    static std::mutex mu;
-    static bool opted[4] = {false, false, false, false};  // per variant: dynamic shared memory above 48 KB
-    static float *work = nullptr;
-    static size_t work_n = 0;
-    std::lock_guard<std::mutex> lk(mu);
-    bool &o = opted[(ta ? 2 : 0) + (tb ? 1 : 0)];
-    if (!o) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    {
+        const cudaError_t e = opt_in_smem(reinterpret_cast<const void *>(kern), kTcSmem);
         if (e != cudaSuccess) return (int)e;
-        o = true;
     }
     if (splits == 1) {
         kern<<<dim3(gx, gy, 1), 128, kTcSmem, st>>>(a, lda, b, ldb, C, ldc, M, N, K, k_split, beta, err);
         return (int)cudaGetLastError();
     }
+    // the split workspace of the current device (grown on demand)
+    static std::mutex mu;
+    static float *work[kMaxDevices] = {};
+    static size_t work_n[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return (int)cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(mu);
     const size_t need = (size_t)splits * M * N;
-    if (need > work_n) {
-        if (work) cudaFree(work);  // synchronises the device: no launch still reads the old workspace
-        work = nullptr;
-        work_n = 0;
-        cudaError_t e = cudaMalloc(&work, need * sizeof(float));
+    if (need > work_n[dev]) {
+        if (work[dev]) cudaFree(work[dev]);  // synchronises the device: no launch still reads the old workspace
+        work[dev] = nullptr;
+        work_n[dev] = 0;
+        cudaError_t e = cudaMalloc(&work[dev], need * sizeof(float));
         if (e != cudaSuccess) return (int)e;
-        work_n = need;
+        work_n[dev] = need;
     }
-    kern<<<dim3(gx, gy, splits), 128, kTcSmem, st>>>(a, lda, b, ldb, work, N, M, N, K, k_split, 0.0f, err);
+    float *const wk = work[dev];
+    kern<<<dim3(gx, gy, splits), 128, kTcSmem, st>>>(a, lda, b, ldb, wk, N, M, N, K, k_split, 0.0f, err);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
     const size_t n = (size_t)M * N;
-    split_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(work, splits, C, ldc, M, N, beta);
+    split_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(wk, splits, C, ldc, M, N, beta);
     return (int)cudaGetLastError();
 }
 
@@ -1473,8 +1494,7 @@ int rbg_mdn_infer(const float *F, int Q, int n_in, const float *x_mean, const fl
         !encode_rows(maps.w[3], W3, kInfHid, kInfHid, kInfHid, kInfHid) ||
         !encode_rows(maps.w[4], W4, n_out, kInfHid, kInfHid, n_mma))
         return (int)cudaErrorNotSupported;
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInfSmem);
+    const cudaError_t attr = opt_in_smem(reinterpret_cast<const void *>(mlp_infer_kernel), kInfSmem);
     if (attr != cudaSuccess) return (int)attr;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
