@@ -86,6 +86,74 @@ def test_batch_matches_individual_runs(rb):
         _check(b, k, net, x0, b.seeds(k), tmax, nb, rates, save)
 
 
+def _macro_dsl(rng, S, R):
+    """A define_system! body over species s0..s{S-1} with R reactions of order
+    <= 2 and numeric rates, and its oracle (macro arithmetic) copy."""
+    from oracle import oracle as O
+
+    lines = [";", "Net { " + ", ".join(f"s{i}" for i in range(S)) + " }"]
+    onet = O.OracleNet(S, macro=True)
+    for k in range(R):
+        a = int(rng.integers(S))
+        factors = [(a, 2)] if rng.random() < 0.3 else [(a, 1)] + ([(int(rng.integers(S)), 1)] if rng.random() < 0.5 else [])
+        if len(factors) == 2 and factors[0][0] == factors[1][0]:
+            factors = [(factors[0][0], 2)]
+        prods = [int(p) for p in rng.integers(S, size=int(rng.integers(0, 3)))]
+        rate = float(10 ** rng.uniform(-3, -1))
+        lhs = " + ".join(f"{n} s{sp}" if n > 1 else f"s{sp}" for sp, n in factors)
+        rhs = " + ".join(f"s{sp}" for sp in prods)
+        lines.append(f"r{k} : {lhs} => {rhs} @ {rate!r}")
+        d = [0] * S
+        for sp, n in factors:
+            d[sp] -= n
+        for sp in prods:
+            d[sp] += 1
+        onet.add_macro(rate, factors, d)
+    return "\n".join(lines), onet
+
+
+def test_batch_of_define_system_networks(rb):
+    # define_system! arithmetic (falling factorials in integers, the first-match
+    # choice) inside the persistent launch: dimer parameter sets as thread
+    # units, 20-species 40-reaction networks a warp per trajectory; every item
+    # against the oracle's macro arithmetic
+    from oracle import oracle as O
+
+    rng = np.random.default_rng(12)
+    b = rb.Batch()
+    specs = []
+    dim = rb.Network.from_dsl("""
+        ;
+        Dimers { gene, mRNA, protein, dimer }
+        transcription : gene => gene + mRNA @ 25.0
+        translation : mRNA => mRNA + protein @ 1000.0
+        dimerization : 2 protein => dimer @ 0.001
+        decay_mRNA : mRNA => @ 0.1
+        decay_prot : protein => @ 1.0
+    """)
+    for k in range(12):
+        rates = np.array([25.0, 1000.0, 0.001, 0.1, 1.0]) * 10 ** rng.uniform(-0.5, 0.5, 5)
+        seeds = rng.integers(np.iinfo(np.uint64).max, size=8, dtype=np.uint64)
+        o = (O.OracleNet(4, macro=True).add_macro(rates[0], [(0, 1)], [0, 1, 0, 0])
+             .add_macro(rates[1], [(1, 1)], [0, 0, 1, 0]).add_macro(rates[2], [(2, 2)], [0, 0, -2, 1])
+             .add_macro(rates[3], [(1, 1)], [0, -1, 0, 0]).add_macro(rates[4], [(2, 1)], [0, 0, -1, 0]))
+        specs.append((b.add(dim, [1, 0, 0, 0], seeds, 0.3, 6, rates=rates), o, [1, 0, 0, 0], seeds, 0.3, 6))
+    for k in range(3):
+        text, o = _macro_dsl(rng, 20, 40)
+        net = rb.Network.from_dsl(text)
+        x0 = rng.integers(20, 80, size=20).tolist()
+        seeds = rng.integers(np.iinfo(np.uint64).max, size=16, dtype=np.uint64)
+        specs.append((b.add(net, x0, seeds, 0.05, 5), o, x0, seeds, 0.05, 5))
+    assert b.plan() == (0, 15)  # one persistent launch in macro arithmetic
+    b.run()
+    for k, o, x0, seeds, tmax, nb in specs:
+        ref, ev, _, _ = o.run_ensemble(x0, seeds, tmax, nb)
+        assert ev.min() > 10
+        np.testing.assert_array_equal(b.counts(k), ref)
+        np.testing.assert_array_equal(b.events(k), ev)
+    assert {b.mapping(k) for k in range(12)} == {7} and {b.mapping(k) for k in range(12, 15)} == {5}
+
+
 def test_batch_merges_parameter_sets(rb, monkeypatch):
     # The merged plan: with every class worth a launch, parameter sets of one
     # network run as one thread-per-trajectory ensemble with per-trajectory
