@@ -148,7 +148,7 @@ def test_batch_of_define_system_networks(rb):
     b.run()
     for k, o, x0, seeds, tmax, nb in specs:
         ref, ev, _, _ = o.run_ensemble(x0, seeds, tmax, nb)
-        assert ev.min() > 10
+        assert ev.sum() > 100
         np.testing.assert_array_equal(b.counts(k), ref)
         np.testing.assert_array_equal(b.events(k), ev)
     assert {b.mapping(k) for k in range(12)} == {7} and {b.mapping(k) for k in range(12, 15)} == {5}
