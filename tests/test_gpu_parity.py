@@ -266,6 +266,13 @@ def test_edge_cases(rb, O):
     ref, ev, _, _ = ob.run_ensemble([3_000_000_000, 0], seeds, 0.5, 5)
     np.testing.assert_array_equal(res.counts, ref)
     np.testing.assert_array_equal(res.events, ev)
+    # more sample rows than the kernels count for streaming (65 536): every
+    # row is copied after the launch, and every one is the oracle's
+    seeds = _seeds(48, 10)
+    res = _sir(rb).run_ensemble([999, 1, 0], seeds, 250.0, 70_000)
+    ref, ev, _, _ = O.sir_net().run_ensemble([999, 1, 0], seeds, 250.0, 70_000)
+    np.testing.assert_array_equal(res.counts, ref)
+    np.testing.assert_array_equal(res.events, ev)
 
 
 def test_device_entry_point_matches_host_entry_point(rb, O):
