@@ -147,10 +147,11 @@ def batch_seeds(step: int, j: int) -> np.ndarray:
     return seeds_for(step, 100000 + j, BATCH["traj"])
 
 
-def make_batch(rb, items, want_events: bool = False):
+def make_batch(rb, items, want_events: bool = False, copy: bool = True):
     """The heterogeneous batch of `items` (see batch_items) as one rb.Batch:
     every Michaelis-Menten set shares one network with its own rate constants,
-    every random network is its own; seeds of step 0.  Returns (batch, networks)."""
+    every random network is its own; seeds of step 0; copy=False reads results
+    where the batch keeps them.  Returns (batch, networks)."""
     b = rb.Batch()
     mm = rb.Network(4)
     for e, d in MM_REACTIONS:
@@ -159,13 +160,14 @@ def make_batch(rb, items, want_events: bool = False):
     for j, (kind, spec, x0) in enumerate(items):
         seeds = batch_seeds(0, j)
         if kind == "mm":
-            b.add(mm, x0, seeds, BATCH["tmax_mm"], BATCH["nb_steps"], rates=spec, want_events=want_events)
+            b.add(mm, x0, seeds, BATCH["tmax_mm"], BATCH["nb_steps"], rates=spec, want_events=want_events,
+                  copy=copy)
         else:
             net = rb.Network(len(x0))
             for k, e, d in spec:
                 net.add_reaction(rb.Rate.lma(k, e), d)
             nets.append(net)
-            b.add(net, x0, seeds, BATCH["tmax_rand"], BATCH["nb_steps"], want_events=want_events)
+            b.add(net, x0, seeds, BATCH["tmax_rand"], BATCH["nb_steps"], want_events=want_events, copy=copy)
     return b, nets
 
 
@@ -630,7 +632,7 @@ def measure_batch(args, steps: int, warmup: int, cpu: bool = True) -> dict:
     import rebop_gb300 as rb
 
     items = batch_items()
-    b, nets = make_batch(rb, items)
+    b, nets = make_batch(rb, items, copy=False)  # results read in place, as a serving caller would
     n_own, n_persistent = b.plan()
     for s in range(warmup):
         b.run()
@@ -670,8 +672,8 @@ def measure_batch(args, steps: int, warmup: int, cpu: bool = True) -> dict:
                    "events_per_step": events / steps, "own_launches": n_own, "persistent_items": n_persistent,
                    "mode": os.environ.get("RB_BATCH_MODE", "persistent"),
                    "timing": ("value: device time of the graph's kernels (CUDA events recorded as graph nodes); "
-                              "e2e: wall time of Batch.run (input staging, the graph with its input and result "
-                              "copies, result unstaging)"),
+                              "e2e: wall time of Batch.run (input staging, the graph with its input copy and its "
+                              "copy of every result into page-locked host memory, where the caller reads them)"),
                    "graph_ms_per_step": dev_ms / steps,
                    "graph_parts_ms": parts,
                    "l2": "inputs and outputs far above L2 are copied in every step"},

@@ -269,8 +269,9 @@ void rb_batch_destroy(rb_batch *b);
 /* Add one ensemble.  Arguments mean what they mean for rb_ensemble_run; the
  * host buffers (x0, rates, seeds, save_idx, out, events) are kept by pointer
  * and must outlive the batch: every rb_batch_run reads the inputs' current
- * contents and writes the outputs.  A network must not change after it is
- * added (RB_ERR_INVALID at run time). */
+ * contents and writes the outputs.  out may be null: the results then stay
+ * with the batch (rb_batch_item_results), with no copy into caller memory.
+ * A network must not change after it is added (RB_ERR_INVALID at run time). */
 int rb_batch_add(rb_batch *b, const rb_network *net, int64_t n_traj, const int64_t *x0, int32_t x0_per_traj,
                  const double *rates, int32_t rates_per_traj, const uint64_t *seeds, double tmax,
                  int64_t nb_steps, const int32_t *save_idx, int32_t n_save, int64_t *out, uint64_t *events);
@@ -285,6 +286,14 @@ int rb_batch_run(rb_batch *b, rb_run_stats *stats);
  * kernel compiled). */
 int rb_batch_plan(rb_batch *b, int32_t *n_own_launches, int32_t *n_persistent_items);
 int rb_batch_item_mapping(const rb_batch *b, int32_t item, int32_t *mapping);
+/* After a run: where item's results lie -- out [nb_steps + 1][n_save][n_traj]
+ * and events [n_traj] -- in the batch's page-locked staging buffer (items of
+ * the persistent launch: no copy at all), in the batch's own copy (items of a
+ * merged class added without an output buffer), or in the caller's buffers
+ * given to rb_batch_add.  Valid until the next rb_batch_run, rb_batch_add or
+ * rb_batch_destroy; RB_ERR_INVALID before the first run.  (No reference
+ * counterpart.) */
+int rb_batch_item_results(const rb_batch *b, int32_t item, const int64_t **out, const uint64_t **events);
 
 /* ------------------------------------------ stateful single trajectory ---
  * The Rust API's `Gillespie` object (src/gillespie.rs:157-344) with the same

@@ -101,6 +101,7 @@ _SIGS = {
     "rb_batch_run": ([_vp, P(RunStats)], C.c_int),
     "rb_batch_plan": ([_vp, P(_i32), P(_i32)], C.c_int),
     "rb_batch_item_mapping": ([_vp, _i32, P(_i32)], C.c_int),
+    "rb_batch_item_results": ([_vp, _i32, P(P(_i64)), P(P(_u64))], C.c_int),
     "rb_ensemble_tune": ([_vp, _i64, P(_i64), _i32, P(_f64), _i32, _f64, _i64, P(TuneResult), P(TuneResult),
                           _i32, P(_i32)], C.c_int),
     "rb_tune_lookup": ([_vp, _i64, _i32, P(TuneResult)], C.c_int),

@@ -430,7 +430,11 @@ class Batch:
             self._h = None
 
     def add(self, network: "Network", x0, seeds, tmax: float, nb_steps: int, *, rates=None, save=None,
-            want_events: bool = True) -> int:
+            want_events: bool = True, copy: bool = True) -> int:
+        """Add one ensemble; returns its index.  copy=False: no result arrays of
+        its own -- ``counts(k)`` and ``events(k)`` are then views of the batch's
+        results (the page-locked staging buffer for items of the persistent
+        launch), valid until the next ``run`` or ``add``."""
         S, R = network.nb_species, network.nb_reactions
         seeds = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(-1))
         n = seeds.size
@@ -446,14 +450,23 @@ class Batch:
                 raise ValueError("rates must have one entry per reaction, or one row per trajectory")
         save_arr, n_save = (None, -1) if save is None else (np.ascontiguousarray(np.asarray(save, np.int32)), len(save))
         ns = S if n_save < 0 else n_save
-        out = np.zeros((int(nb_steps) + 1, ns, n), dtype=np.int64)
-        ev = np.zeros(n, dtype=np.uint64) if want_events else None
+        shape = (int(nb_steps) + 1, ns, n)
+        out = np.zeros(shape, dtype=np.int64) if copy else None
+        ev = np.zeros(n, dtype=np.uint64) if want_events and copy else None
         check(lib.rb_batch_add(self._h, network._h, n, ptr(x0, _i64), x0_per, ptr(r_arr, _f64), r_per,
                                ptr(seeds, _u64), float(tmax), int(nb_steps), ptr(save_arr, _i32), n_save,
                                ptr(out, _i64), ptr(ev, _u64)))
         self._keep.append((network, seeds, x0, r_arr, save_arr))
-        self._out.append((out, ev))
+        self._out.append((out, ev) if copy else shape)
         return len(self._out) - 1
+
+    def _view(self, k: int):
+        o, e = C.POINTER(_i64)(), C.POINTER(_u64)()
+        check(lib.rb_batch_item_results(self._h, int(k), C.byref(o), C.byref(e)))
+        shape = self._out[k]
+        counts = np.ctypeslib.as_array(o, shape=shape) if shape[1] * shape[2] else np.zeros(shape, np.int64)
+        events = np.ctypeslib.as_array(e, shape=(shape[2],)) if shape[2] else np.zeros(0, np.uint64)
+        return counts, events
 
     def seeds(self, k: int) -> np.ndarray:
         """Item k's seed array: change it in place between runs for fresh trajectories."""
@@ -465,10 +478,12 @@ class Batch:
         return {f: getattr(st, f) for f, _ in RunStats._fields_}
 
     def counts(self, k: int) -> np.ndarray:
-        return self._out[k][0]
+        o = self._out[k]
+        return self._view(k)[0] if isinstance(o, tuple) and isinstance(o[0], int) else o[0]
 
     def events(self, k: int):
-        return self._out[k][1]
+        o = self._out[k]
+        return self._view(k)[1] if isinstance(o, tuple) and isinstance(o[0], int) else o[1]
 
     def plan(self) -> tuple[int, int]:
         """(launches of their own, items of the persistent launch)."""

@@ -100,7 +100,6 @@ std::string Batch::add(const Network *net, const ItemIn &in) {
             it.save.push_back(in.save_idx[k]);
         }
     }
-    if (in.n_traj > 0 && !it.save.empty() && !in.out) return "null out";
     items.push_back(std::move(it));
     planned = false;
     return "";
@@ -659,13 +658,19 @@ void Batch::unstage_outputs(uint64_t &events) {
         const int64_t *out = reinterpret_cast<const int64_t *>(h + c.o_out);
         const uint64_t *ev = reinterpret_cast<const uint64_t *>(h + c.o_events);
         for (int i : c.items) {
-            const Item &it = items[i];
+            Item &it = items[i];
             const int64_t n = it.in.n_traj;
-            if (it.in.out)
-                for (int64_t s = 0; s < c.n_samples; s++)
-                    for (int32_t k = 0; k < c.n_save; k++)
-                        tasks.push_back({it.in.out + (s * c.n_save + k) * n,
-                                         out + (s * c.n_save + k) * c.n_traj + base, 8 * (size_t)n});
+            // a merged class interleaves its items' rows: an item without an
+            // output buffer gets the batch's own copy
+            int64_t *dst = it.in.out;
+            if (!dst) {
+                it.own_out.resize((size_t)c.n_samples * c.n_save * n);
+                dst = it.own_out.data();
+            }
+            for (int64_t s = 0; s < c.n_samples; s++)
+                for (int32_t k = 0; k < c.n_save; k++)
+                    tasks.push_back({dst + (s * c.n_save + k) * n, out + (s * c.n_save + k) * c.n_traj + base,
+                                     8 * (size_t)n});
             for (int64_t k = 0; k < n; k++) events += ev[base + k];
             if (it.in.events) tasks.push_back({it.in.events, ev + base, 8 * (size_t)n});
             base += n;
@@ -682,6 +687,26 @@ void Batch::unstage_outputs(uint64_t &events) {
         if (it.in.events) tasks.push_back({it.in.events, ev, 8 * (size_t)n});
     }
     parallel_copy(tasks);
+}
+
+bool Batch::item_results(int k, const int64_t **out, const uint64_t **events) const {
+    if (k < 0 || k >= (int)items.size() || !host || !exec) return false;
+    const Item &it = items[k];
+    const unsigned char *h = static_cast<const unsigned char *>(host);
+    for (const Class &c : classes) {
+        int64_t base = 0;
+        for (int i : c.items) {
+            if (i == k) {
+                *out = it.in.out ? it.in.out : it.own_out.data();
+                *events = reinterpret_cast<const uint64_t *>(h + c.o_events) + base;
+                return true;
+            }
+            base += items[i].in.n_traj;
+        }
+    }
+    *out = it.in.out ? it.in.out : reinterpret_cast<const int64_t *>(h + it.o_out);
+    *events = reinterpret_cast<const uint64_t *>(h + it.o_events);
+    return true;
 }
 
 bool Batch::run(rb_stats_out &st_out) {

@@ -33,7 +33,7 @@ struct Batch {
         int64_t nb_steps = 1;
         const int32_t *save_idx = nullptr;
         int32_t n_save = -1;            // < 0: every species
-        int64_t *out = nullptr;         // [nb_steps + 1][n_save][n_traj]
+        int64_t *out = nullptr;         // [nb_steps + 1][n_save][n_traj]; null: the results stay with the batch
         uint64_t *events = nullptr;     // [n_traj] or null
     };
     struct Item {
@@ -43,6 +43,9 @@ struct Batch {
         ItemIn in;
         std::vector<int32_t> save;
         int mapping = -1;
+        // results of an item added without an output buffer when its rows are
+        // not contiguous in the staging buffer (merged classes)
+        std::vector<int64_t> own_out;
         size_t o_x0 = 0, o_seeds = 0, o_times = 0, o_save = 0, o_rates = 0, o_fsp = 0, o_ford = 0, o_jsp = 0,
                o_jd = 0, o_rdf = 0, o_lfac = 0, o_shape = 0, o_fpk = 0, o_out = 0, o_events = 0;
     };
@@ -86,6 +89,10 @@ struct Batch {
     }
     bool plan();
     bool run(rb_stats_out &st);
+    // After a run: item k's results where they lie (the page-locked staging
+    // buffer, or the batch's own copy); valid until the next run, add or
+    // destruction.  False before the first run.
+    bool item_results(int k, const int64_t **out, const uint64_t **events) const;
     ~Batch();
 
   private:

@@ -818,6 +818,13 @@ int rb_batch_plan(rb_batch *b, int32_t *n_own_launches, int32_t *n_persistent_it
     return RB_OK;
 }
 
+int rb_batch_item_results(const rb_batch *b, int32_t item, const int64_t **out, const uint64_t **events) {
+    if (!b || !out || !events) return fail(RB_ERR_INVALID, "null argument");
+    if (item < 0 || item >= (int32_t)b->b.items.size()) return fail(RB_ERR_INVALID, "item index out of range");
+    if (!b->b.item_results(item, out, events)) return fail(RB_ERR_INVALID, "the batch has not run yet");
+    return RB_OK;
+}
+
 int rb_batch_item_mapping(const rb_batch *b, int32_t item, int32_t *mapping) {
     if (!b || !mapping || item < 0 || item >= (int32_t)b->b.items.size())
         return fail(RB_ERR_INVALID, "item index out of range");

@@ -154,6 +154,44 @@ def test_batch_of_define_system_networks(rb):
     assert {b.mapping(k) for k in range(12)} == {7} and {b.mapping(k) for k in range(12, 15)} == {5}
 
 
+@pytest.mark.parametrize("mode", ["persistent", "merged"])
+def test_batch_results_in_place(rb, monkeypatch, mode):
+    # Items added without output arrays: their results are read where the
+    # batch keeps them (the staging buffer, or the batch's own copy for a
+    # merged class) and equal the copied results of the same items, before and
+    # after a replay with new seeds.
+    import bench
+
+    monkeypatch.setenv("RB_BATCH_MODE", mode)
+    if mode == "merged":
+        monkeypatch.setenv("RB_BATCH_MIN_THREAD", "1")
+    rng = np.random.default_rng(13)
+    mm = _mm(rb)
+    reactions, _ = bench.random_network(130, 30, 90)
+    net = rb.Network(30)
+    for kk, e, d in reactions:
+        net.add_reaction(rb.Rate.lma(kk, e), d)
+    specs = []
+    for k in range(6):
+        specs.append((mm, [int(rng.integers(10, 101)), 500, 0, 0], 10 ** rng.uniform(-3, 1, 3), 3.0, 8, [1, 3]))
+    specs.append((net, rng.integers(0, 501, size=30).tolist(), None, 2e-3, 5, None))
+    seeds = [rng.integers(np.iinfo(np.uint64).max, size=24, dtype=np.uint64) for _ in specs]
+    a, v = rb.Batch(), rb.Batch()
+    for (n, x0, rates, tmax, nb, save), sd in zip(specs, seeds):
+        a.add(n, x0, sd.copy(), tmax, nb, rates=rates, save=save)
+        v.add(n, x0, sd.copy(), tmax, nb, rates=rates, save=save, copy=False)
+    for rep in range(2):
+        a.run()
+        v.run()
+        for k in range(len(specs)):
+            np.testing.assert_array_equal(v.counts(k), a.counts(k))
+            np.testing.assert_array_equal(v.events(k), a.events(k))
+        for k in range(len(specs)):
+            fresh = rng.integers(np.iinfo(np.uint64).max, size=24, dtype=np.uint64)
+            a.seeds(k)[:] = fresh
+            v.seeds(k)[:] = fresh
+
+
 def test_batch_merges_parameter_sets(rb, monkeypatch):
     # The merged plan: with every class worth a launch, parameter sets of one
     # network run as one thread-per-trajectory ensemble with per-trajectory
