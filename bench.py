@@ -371,6 +371,21 @@ def read_profile(kernel: str, workload: str) -> dict:
     return out
 
 
+def release_host_memory():
+    """Between workloads: drop the previous one's page-locked host buffers,
+    which torch's host allocator would otherwise keep cached (gigabytes after
+    the large-network workload), so each workload starts from the same state."""
+    import gc
+
+    import torch
+
+    gc.collect()
+    torch.cuda.synchronize()
+    empty = getattr(torch._C, "_host_emptyCache", None)
+    if empty is not None:
+        empty()
+
+
 def hbm_peak() -> tuple[float, str]:
     """Measured HBM copy bandwidth (GB/s) of the GB300s, else the fallback."""
     p = ROOT / "MEASURED_PEAKS.json"
@@ -570,6 +585,7 @@ def run_ours(args, w):
     subs = {}
     if rank == 0 and world == 1 and args.workloads != "none":
         for name in [x for x in args.workloads.split(",") if x and x != w["name"]]:
+            release_host_memory()
             if name == "batch":
                 subs[name] = measure_batch(args, min(args.steps, 3), min(args.warmup, 2),
                                            cpu=not args.no_cpu_baseline)
