@@ -1,13 +1,21 @@
 // Kernels of the learned surrogate: a BF16 multilayer perceptron with a
-// mixture-density head over (log1p protein, log1p dimer) counts, trained on
-// ensembles the SSA engine generates.
+// count-aware head (or a mixture-density head) over the dimer's protein and
+// dimer counts, trained on ensembles the SSA engine generates.
 //
 //   * gemm_bf16: C[M][N] (+)= op(A) op(B) with BF16 operands and FP32
-//     accumulation on the tensor cores (mma m16n8k16); op = transpose or not,
-//     so one kernel serves the forward pass (H W^T), the input gradient
-//     (dZ W) and the weight gradient (dZ^T H).
+//     accumulation on mma.sync m16n8k16 (the legacy-path comparison).
+//   * gemm_tc05: the same product on tcgen05 with the accumulator in tensor
+//     memory, operands staged by vector loads, every orientation, split K for
+//     the weight gradients (split_reduce sums the splits in a fixed order).
+//   * gemm_tma: C = A B^T on tcgen05 with the operands loaded by
+//     cp.async.bulk.tensor through a four-stage mbarrier ring (the forward
+//     pass).
+//   * mlp_infer: the whole forward pass for 128-query tiles in one persistent
+//     kernel -- activations in shared memory, weights by TMA, each layer's
+//     accumulator in tensor memory, bias and SiLU in the drain.
 //   * bias_silu: Z += b; H = bf16(silu(Z)) (or identity for the head).
-//   * silu_backward: dZ = dH * silu'(Z), plus the bias gradient.
+//   * silu_backward / head_backward: dZ = dH * silu'(Z) and the bias
+//     gradients (column sums in a fixed order).
 //   * count_loss: negative log-likelihood of the count-aware head (per
 //     species a categorical over the counts 0 .. 30 and a tail class, the
 //     tail a Gaussian mixture over the log-count residual) and its gradient
@@ -15,7 +23,10 @@
 //   * mdn_loss: the same for a K-component diagonal Gaussian mixture in two
 //     dimensions.
 //   * adam: FP32 master weights, BF16 copies refreshed in place.
-//   * mdn_sample / count_sample: draws from each row's distribution.
+//   * rre: the reaction rate equations (RK4) at each query; an unrolled
+//     variant for networks of 4 species and 5 reactions.
+//   * mdn_sample / count_prep + count_draw: draws from each query's
+//     distribution.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
