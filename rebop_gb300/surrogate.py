@@ -1,6 +1,6 @@
-"""Learned surrogate of the dimerization ensemble (configs: dimer network,
-5 rate constants log-uniform over one decade either side of their values, t
-in [0, 1]).
+"""Learned surrogate of the dimerization ensemble (the dimer network, its 5
+rate constants log-uniform over one decade either side of their values, t in
+[0, 1]).
 
 A query (u, t) -- the log10 factors u of the five rate constants and the time
 -- gets the count distributions of protein and dimer.  Their deterministic
@@ -18,9 +18,10 @@ independent: the head models each marginal distribution, not their
 correlation.  (head="mixture" selects an 8-component diagonal Gaussian
 mixture over both residuals jointly instead.)  Weights are BF16 with FP32 master copies; every
 forward and backward GEMM runs on the 5th-generation tensor cores (tcgen05.mma
-into tensor memory, FP32 accumulation), and the rate-equation solver, the
-loss, its gradient, the optimiser and the sampler are the engine's own kernels
-(rebop_gb300/csrc/mdn.cu).  PyTorch only holds the device memory.  Training
+into tensor memory, FP32 accumulation; the forward products with operands
+loaded by TMA), inference runs the whole network in one fused tcgen05 kernel
+(MDN.infer), and the rate-equation solver, the loss, its gradient, the
+optimiser and the sampler are the engine's own kernels (rebop_gb300/csrc/mdn.cu).  PyTorch only holds the device memory.  Training
 data, the validation that decides where the surrogate is trusted, and the
 fallback for the rest all come from the SSA engine itself.
 """
