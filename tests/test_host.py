@@ -246,6 +246,21 @@ def test_generated_network_compiles(rb, tmp_path, monkeypatch):
     assert len(list(tmp_path.glob("net_*.cubin"))) == 1
 
 
+def test_batch_results_in_place_need_a_run(rb):
+    # An item added without output arrays (copy=False) has no results to read
+    # before the batch has run: the entry point says so instead of handing out
+    # a pointer; its shape and the plan are known without a GPU.
+    b = rb.Batch()
+    n = rb.Network(2)
+    n.add_reaction(rb.Rate.lma(1.0, [1, 0]), [-1, 1])
+    k = b.add(n, [10, 0], np.arange(4, dtype=np.uint64), 1.0, 3, copy=False)
+    assert b.plan() == (0, 1)
+    with pytest.raises(ValueError, match="has not run"):
+        b.counts(k)
+    with pytest.raises(ValueError, match="out of range"):
+        b._view(5)
+
+
 def test_batch_plan_groups_by_structure(rb, monkeypatch):
     # The persistent plan: small networks (at most 16 species and reactions)
     # become thread units, larger ones a warp per trajectory, rate expressions
