@@ -21,57 +21,9 @@
 #include <map>
 #include <thread>
 
-#include <sys/mman.h>
-#include <unistd.h>
-
 #include "ssa_jit.hpp"
 
 namespace rbg {
-
-namespace {
-
-// The staging buffer, zeroed: anonymous memory aligned to, and advised into,
-// transparent huge pages, then page-locked for the GPU, so that the GPU's
-// copies to and from it need fewer host address translations.  Falls back to
-// cudaMallocHost.  `map` / `map_bytes` describe the mapping to release (null
-// for cudaMallocHost).
-void *alloc_staging(size_t bytes, void *&map, size_t &map_bytes) {
-    map = nullptr;
-    map_bytes = 0;
-    const size_t page = (size_t)sysconf(_SC_PAGESIZE);
-    const size_t huge = page >= 65536 ? ((size_t)512 << 20) : ((size_t)2 << 20);  // PMD size for the base page
-    const size_t len = bytes + huge;
-    void *m = mmap(nullptr, len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
-    if (m != MAP_FAILED) {
-        const uintptr_t a = (reinterpret_cast<uintptr_t>(m) + huge - 1) & ~(uintptr_t)(huge - 1);
-        void *p = reinterpret_cast<void *>(a);
-        madvise(p, bytes, MADV_HUGEPAGE);  // advice only: kernels without THP ignore it
-        std::memset(p, 0, bytes);          // fault the pages in before they are locked
-        if (cudaHostRegister(p, bytes, cudaHostRegisterDefault) == cudaSuccess) {
-            map = m;
-            map_bytes = len;
-            return p;
-        }
-        cudaGetLastError();
-        munmap(m, len);
-    }
-    void *h = nullptr;
-    if (cudaMallocHost(&h, bytes) != cudaSuccess) return nullptr;
-    std::memset(h, 0, bytes);
-    return h;
-}
-
-void free_staging(void *p, void *map, size_t map_bytes) {
-    if (!p) return;
-    if (map) {
-        cudaHostUnregister(p);
-        munmap(map, map_bytes);
-    } else {
-        cudaFreeHost(p);
-    }
-}
-
-}  // namespace
 
 namespace {
 
@@ -360,9 +312,10 @@ bool Batch::build(cudaStream_t st) {
     }
     o_work = take(8 * 4);
     total_bytes = off;
-    host = alloc_staging(total_bytes, host_map, host_map_bytes);
-    if (!host) return cuda_ok(cudaErrorMemoryAllocation, "page-locked batch staging");
-    if (!cuda_ok(cudaMalloc(&dev, total_bytes), "cudaMalloc(batch arena)")) return false;
+    if (!cuda_ok(cudaMallocHost(&host, total_bytes), "cudaMallocHost(batch staging)") ||
+        !cuda_ok(cudaMalloc(&dev, total_bytes), "cudaMalloc(batch arena)"))
+        return false;
+    std::memset(host, 0, total_bytes);
     unsigned char *h = static_cast<unsigned char *>(host);
     unsigned char *d = static_cast<unsigned char *>(dev);
 
@@ -816,9 +769,7 @@ void Batch::free_device() {
     dev = nullptr;
     if (warp_cnt0) cudaFree(warp_cnt0);
     warp_cnt0 = nullptr;
-    free_staging(host, host_map, host_map_bytes);
-    host_map = nullptr;
-    host_map_bytes = 0;
+    if (host) cudaFreeHost(host);
     host = nullptr;
     if (side) cudaStreamDestroy(side);
     side = nullptr;

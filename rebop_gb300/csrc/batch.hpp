@@ -70,8 +70,6 @@ struct Batch {
 
     // device state of the captured graph
     void *host = nullptr, *dev = nullptr;
-    void *host_map = nullptr;  // the mapping behind `host` (null: cudaMallocHost)
-    size_t host_map_bytes = 0;
     int64_t *warp_cnt0 = nullptr;  // the warp kernel's interval-start counts
     size_t in_bytes = 0, total_bytes = 0, o_items = 0, o_start = 0, o_work = 0, o_titems = 0, o_tunit = 0;
     SsaArgs warp_args{};
