@@ -913,7 +913,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner's pilot runs")
-    ap.add_argument("--workloads", default="sir,large,batch,surrogate",
+    # the batch first: measured after the SIR and large-network CPU baselines,
+    # its 2.77 GB result copy into page-locked memory ran up to 7x slower
+    ap.add_argument("--workloads", default="batch,sir,large,surrogate",
                     help="configurations measured beside the headline (comma list, or 'none')")
     args = ap.parse_args()
     if args.workload == "batch":
