@@ -38,7 +38,7 @@ namespace {
 
 constexpr int kWarpMaxWarps = 16;
 // batch launches: small per-warp regions, so registers set the warps per SM
-constexpr int kWarpMaxWarpsBatch = 20;
+constexpr int kWarpMaxWarpsBatch = 24;
 
 struct WarpLayout {
     size_t block_bytes, warp_bytes;
